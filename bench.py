@@ -1,0 +1,379 @@
+"""EM iterations per second of the DA-GTM annealed EM step on GB300.
+
+Workload (the headline configuration): N = 1,000,000 synthetic binary
+fingerprints (D = 166, 20 prototypes, per-feature Bernoulli p ~ U[0.05,0.5],
+10 % bit flips), K = 8000 latent points (20^3, L = 3), M = 64 RBF centres
+(4^3) plus bias, width 2 x spacing, deterministic annealing at the start
+temperature.  One step = one EM iteration (E-step, qualities, M-step, beta)
+with the data resident in HBM; the data (>= 332 MB in BF16, 1.3 GB in FP64)
+is larger than L2, so no flush is needed between iterations.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Under torchrun each rank runs an independent replica (the path is one GPU
+per problem; no data-path collective); rank 0 prints one JSON line.
+``--impl reference`` times the CPU restatement of the reference's algorithm
+(the oracle: the reference itself needs MPI/GSL/HDF5, which are absent) on
+all host cores, on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "EM iters/sec at N=1M,K=8k,D=166: FP64 plain vs BF16x3 form at stated error"
+WORKLOAD = dict(N=1_000_000, D=166, K=8000, L=3, M=64, s=2.0, nproto=20, seed=0)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--form", default="bf16x3", choices=["bf16x3", "fp64", "fp32"])
+    ap.add_argument("--n", type=int, default=WORKLOAD["N"], help="data points (default 1M)")
+    ap.add_argument("--fp64-steps", type=int, default=2,
+                    help="timed EM iterations of the FP64 form beside the headline (0: skip)")
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--cpu-sample", type=int, default=1024,
+                    help="points in the bounded CPU-baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+def make_problem(n):
+    ds = importlib.import_module("da-gtm_gb300.datasets")
+    st = importlib.import_module("da-gtm_gb300.gtm_setup")
+    w = WORKLOAD
+    T = ds.fingerprints(n, w["D"], w["nproto"], seed=w["seed"])
+    X, FI, W0, beta0 = st.random_init(T, w["L"], w["K"], w["M"], w["s"], seed=1)
+    Y0 = FI @ W0
+    temp0 = st.start_temp(T[: min(n, 200_000)], 0.99)
+    return T, X, FI, Y0, beta0, temp0
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax = float(p[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except (OSError, ValueError):
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, \
+            "fallback"
+
+
+def traffic_summary():
+    """Per-launch DRAM traffic of the dominant kernel from a committed ncu summary."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+def time_steps(torch, ctx, n, beta, temp, stream):
+    """n EM iterations with resident data; returns (ms, beta)."""
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(n):
+        ctx.estep(beta, 1, temp)
+        beta, _, _ = ctx.mstep(want_W=False)
+    ev1.record(stream)
+    ev1.synchronize()
+    torch.cuda.synchronize()
+    return ev0.elapsed_time(ev1), beta
+
+
+def run_form(torch, pkg, form, T, FI, Y0, beta0, temp0, steps, warmup, rank, world, stream_cls,
+             clocks=False):
+    ctx = pkg.Context(T, FI, form)
+    ctx.set_Y(Y0)
+    stream = stream_cls(ctx.stream())
+    beta = beta0
+    for _ in range(warmup):
+        ctx.estep(beta, 1, temp0)
+        beta, _, _ = ctx.mstep(want_W=False)
+    ctx.set_timing(True)
+    ctx.reset_timing()
+    if world > 1:
+        torch.distributed.barrier()
+    sampler = ClockSampler(torch.cuda.current_device()) if clocks else None
+    if sampler:
+        sampler.__enter__()
+    ms, beta = time_steps(torch, ctx, steps, beta, temp0, stream)
+    if sampler:
+        sampler.__exit__(None, None, None)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    phases = ctx.timing()
+    ctx.set_timing(False)
+    return ctx, ms, phases, (sampler.summary() if sampler else None), beta
+
+
+def e2e_steps(torch, pkg, ctx, steps, beta, temp, stream_cls):
+    """Through the host-buffer API: Y in from pinned host memory, W / Y out."""
+    K, D, M1 = ctx.K, ctx.D, ctx.M1
+    Yh_t = torch.empty((K, D), dtype=torch.float64, pin_memory=True)
+    Wh_t = torch.empty((M1, D), dtype=torch.float64, pin_memory=True)
+    Yh = Yh_t.numpy()
+    Wh = Wh_t.numpy()
+    Yh[:] = ctx.get_Y()
+    import ctypes
+    lib = pkg.load_library()
+    dp = ctypes.POINTER(ctypes.c_double)
+    stream = stream_cls(ctx.stream())
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    b = ctypes.c_double(beta)
+    llh, nfree = ctypes.c_double(), ctypes.c_double()
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(steps):
+        pkg._check(lib.dgtm_set_Y(ctx._h, Yh.ctypes.data_as(dp), D))
+        pkg._check(lib.dgtm_estep(ctx._h, b.value, 1, temp, ctypes.byref(llh), ctypes.byref(nfree)))
+        pkg._check(lib.dgtm_mstep(ctx._h, Wh.ctypes.data_as(dp), D, Yh.ctypes.data_as(dp), D,
+                                  ctypes.byref(b)))
+    ev1.record(stream)
+    ev1.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    h2d = K * D * 8
+    d2h = (K * D + M1 * D) * 8 + 3 * 8
+    return ms, h2d, d2h
+
+
+def algorithmic_flops(form, phase, N, K, D):
+    """Tensor-core / FMA work the algorithm needs per launch (unpadded shapes)."""
+    kdn = 2.0 * K * N * D
+    if phase == "estep":
+        return (2 if form == "bf16x3" else 1) * kdn
+    if phase == "mstep_pass":
+        return (4 if form == "bf16x3" else 2) * kdn
+    return None
+
+
+def cpu_baseline(T, FI, Y0, beta0, temp0, sample, N_full):
+    from oracle import oracle as O  # the checker: CPU restatement of the reference
+    O.build()
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    ws = O.Workspace(T[:sample], FI, Y0, beta0)
+    ws.iteration(1, temp0)  # warm-up
+    times = []
+    t_end = time.perf_counter() + 20.0
+    while True:
+        t0 = time.perf_counter()
+        ws.iteration(1, temp0)
+        times.append(time.perf_counter() - t0)
+        if len(times) >= 3 or time.perf_counter() > t_end:
+            break
+    t = statistics.median(times)
+    return {"value": (1.0 / t) * (sample / N_full), "unit": "EM iters/s", "cores": threads,
+            "kind": "port",
+            "sample": f"{sample} of the {N_full} points (K, D, M unchanged), {len(times)} timed "
+                      f"iterations of the reference-semantics CPU restatement (dense K x N "
+                      f"matrices), scaled linearly in N; median {t:.3f} s per iteration"}
+
+
+def main_gb300(args):
+    import torch
+    rank, world, local = dist_env()
+    if world > 1:
+        torch.cuda.set_device(local)
+        torch.distributed.init_process_group("nccl")
+    pkg = importlib.import_module("da-gtm_gb300")
+    pkg.load_library()
+    stream_cls = torch.cuda.ExternalStream
+    T, X, FI, Y0, beta0, temp0 = make_problem(args.n)
+    N, D = T.shape
+    K = FI.shape[0]
+    form = args.form
+    ctx, ms, phases, clocks, beta = run_form(torch, pkg, form, T, FI, Y0, beta0, temp0,
+                                             args.steps, args.warmup, rank, world, stream_cls,
+                                             clocks=(rank == 0))
+    ms_step = ms / args.steps
+    value = world * args.steps / (ms / 1000.0)
+    launches = sum(p["launches"] for p in phases.values())
+    e2e_ms, h2d, d2h = e2e_steps(torch, pkg, ctx, args.e2e_steps, beta, temp0, stream_cls)
+    e2e_value = world * args.e2e_steps / (e2e_ms / 1000.0)
+    ctx.close()
+
+    peaks, peak_src = measured_peaks()
+    dom = max(("estep", "mstep_pass"), key=lambda p: phases[p]["ms"])
+    per_launch_ms = phases[dom]["ms"] / max(1, phases[dom]["calls"])
+    flops = algorithmic_flops(form, dom, N, K, D)
+    if form == "bf16x3":
+        peak = peaks.get("bf16_tflops_sustained", peaks.get("bf16_tflops"))
+        peak_note = f"bf16 dense, sustained ({peak_src})"
+    else:
+        peak = 1.25 if form == "fp64" else 75.0
+        peak_note = f"{form} nominal (no measured {form} peak)"
+    achieved = flops / (per_launch_ms / 1000.0) / 1e12
+    traffic = traffic_summary().get(f"{form}:{dom}")
+    if traffic is not None:
+        traffic = traffic.get("bytes_per_point", 0.0) * N
+    roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak, "traffic": traffic, "kernel": dom,
+                "per_launch_ms": per_launch_ms, "peak_source": peak_note}
+
+    fp64 = None
+    if args.fp64_steps > 0 and form != "fp64":
+        c64, ms64, ph64, _, _ = run_form(torch, pkg, "fp64", T, FI, Y0, beta0, temp0,
+                                         args.fp64_steps, 1, rank, world, stream_cls)
+        c64.close()
+        fp64 = {"value": world * args.fp64_steps / (ms64 / 1000.0), "unit": "EM iters/s",
+                "ms_per_step": ms64 / args.fp64_steps, "steps": args.fp64_steps}
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(T, FI, Y0, beta0, temp0, min(args.cpu_sample, N), N)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "EM iters/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": {"bf16x3": "bf16x3 (fp32 accumulate, fp64 reductions)", "fp64": "f64",
+                      "fp32": "f32"}[form],
+            "data": "synthetic (seeded binary fingerprints, stand-in for the 166-bit "
+                    "chemical-fingerprint data set)",
+            "config": {"workload": f"DA-GTM EM iteration, N={N}, D={D}, K={K} (20^3), "
+                                   f"M=64 (4^3) + bias, {form} form",
+                       "N": N, "D": D, "K": K, "M": 64, "L": 3, "form": form,
+                       "temp": temp0, "l2": "inputs larger than L2 (no flush)",
+                       "parallelism": f"replicas x{world}"},
+            "e2e": {"value": e2e_value, "unit": "EM iters/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "steps": args.e2e_steps},
+            "gpu_launches": int(launches),
+            "clocks": clocks,
+            "roofline": roofline,
+            "phases_ms_per_step": {p: v["ms"] / args.steps for p, v in phases.items()},
+            "fp64_form": fp64,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    O.build()
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    n_sample = args.cpu_sample
+    T, X, FI, Y0, beta0, temp0 = make_problem(n_sample)
+    N_full = args.n
+    ws = O.Workspace(T, FI, Y0, beta0)
+    for _ in range(args.warmup):
+        ws.iteration(1, temp0)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ws.iteration(1, temp0)
+    dt = (time.perf_counter() - t0) / args.steps
+    value = (1.0 / dt) * (n_sample / N_full)
+    sample = (f"{n_sample} of the {N_full} points per step (K, D, M unchanged), reference-"
+              f"semantics CPU restatement with dense K x N matrices, scaled linearly in N")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "EM iters/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": dt * 1000.0 * (N_full / n_sample), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded binary fingerprints)",
+            "config": {"workload": f"DA-GTM EM iteration, N={N_full}, D=166, K=8000, M=64 + bias",
+                       "N": N_full, "D": 166, "K": 8000, "M": 64, "L": 3},
+            "cpu_baseline": {"value": value, "unit": "EM iters/s", "cores": threads,
+                             "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "EM iters/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    a = parse()
+    if a.impl == "reference":
+        main_reference(a)
+    else:
+        main_gb300(a)

@@ -1,0 +1,659 @@
+// dgtm_abi.cu -- the C ABI: context life cycle and the order of launches of one
+// EM iteration.  The host side mirrors the reference's loop body
+// (dagtm/dagtm.cxx:1531-1795): E-step -> qualities -> (caller's convergence
+// test) -> M-step -> beta; every MPI_Allreduce of comm/mpicomm.c becomes a
+// fixed-order on-device reduction and only scalars cross to the host.
+#include "common.cuh"
+#include "kernels.cuh"
+#include "tc.cuh"
+
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+namespace dgtm {
+
+static thread_local char g_err[512] = "";
+
+void set_error(int code, const char *fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    int n = snprintf(g_err, sizeof(g_err), "[%d] ", code);
+    if (n < 0)
+        n = 0;
+    vsnprintf(g_err + n, sizeof(g_err) - (size_t) n, fmt, ap);
+    va_end(ap);
+}
+
+}  // namespace dgtm
+
+using namespace dgtm;
+
+struct dgtm_ctx {
+    int N, D, K, M1, precision, solver, device, sms;
+    cudaStream_t stream;
+    // data (device)
+    double *T64;       // N x D (all forms: exact distances, norms)
+    float *T32;        // N x D (FP32 form)
+    double *tt;        // N
+    double sum_tt;
+    double *FI;        // K x M1
+    double *Y64;       // K x D (master copy of the centres)
+    float *Y32;        // K x D (FP32 form)
+    double *yy;        // K
+    double *W;         // M1 x D
+    // E-step
+    double2 *colstat;  // N
+    double *part;      // 2 x nblk1
+    int nblk1;
+    // M-step
+    int nsplit, n_per_split;
+    double *Gpart, *RTpart;
+    double *G, *RT, *A, *B, *work, *bterm;
+    double *scal;      // device scalars
+    int *flag;         // device status
+    double *hscal;     // pinned host scalars
+    int *hflag;
+    // split-BF16 form
+    TcState *tc;
+    // phase timers (dgtm_set_timing)
+    int timing;
+    cudaEvent_t ev[DGTM_NPHASES][2];
+    int pending[DGTM_NPHASES];
+    double ms[DGTM_NPHASES];
+    long long launches[DGTM_NPHASES], calls[DGTM_NPHASES];
+    // state
+    int stats_valid;   // colstat belongs to the current Y
+    int rt_valid;      // G / RT computed
+    int w_valid;
+    double beta, temp;
+    int isDA;
+};
+
+namespace {
+
+template <typename P>
+int dev_alloc(P **p, size_t count)
+{
+    *p = nullptr;
+    if (count == 0)
+        count = 1;
+    cudaError_t e = cudaMalloc((void **) p, sizeof(P) * count);
+    if (e != cudaSuccess) {
+        set_error(DGTM_ENOMEM, "cudaMalloc(%zu bytes): %s", sizeof(P) * count,
+                  cudaGetErrorString(e));
+        *p = nullptr;
+        return DGTM_ENOMEM;
+    }
+    return DGTM_OK;
+}
+
+#define DGTM_TRY(expr)              \
+    do {                            \
+        int _r = (expr);            \
+        if (_r != DGTM_OK)          \
+            return _r;              \
+    } while (0)
+
+int check_ctx(dgtm_ctx *c)
+{
+    if (!c) {
+        set_error(DGTM_EINVAL, "null context");
+        return DGTM_EINVAL;
+    }
+    int dev = -1;
+    DGTM_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev != c->device)
+        DGTM_CUDA_TRY(cudaSetDevice(c->device));
+    return DGTM_OK;
+}
+
+int sync_and_check(dgtm_ctx *c)
+{
+    DGTM_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    for (int p = 0; p < DGTM_NPHASES; p++) {
+        if (!c->pending[p])
+            continue;
+        float t = 0.f;
+        DGTM_CUDA_TRY(cudaEventElapsedTime(&t, c->ev[p][0], c->ev[p][1]));
+        c->ms[p] += t;
+        c->pending[p] = 0;
+    }
+    return DGTM_OK;
+}
+
+int phase_begin(dgtm_ctx *c, int p)
+{
+    if (c->timing)
+        DGTM_CUDA_TRY(cudaEventRecord(c->ev[p][0], c->stream));
+    return DGTM_OK;
+}
+
+int phase_end(dgtm_ctx *c, int p, int nlaunch)
+{
+    c->launches[p] += nlaunch;
+    c->calls[p] += 1;
+    if (c->timing) {
+        DGTM_CUDA_TRY(cudaEventRecord(c->ev[p][1], c->stream));
+        c->pending[p] = 1;
+    }
+    return DGTM_OK;
+}
+
+// returns the number of kernels launched through *n
+int refresh_y_copies(dgtm_ctx *c, int *n)
+{
+    *n = 0;
+    if (c->precision == DGTM_FP32) {
+        DGTM_TRY(launch_to_f32(c->Y64, (size_t) c->K * c->D, c->Y32, c->stream));
+        *n = 1;
+    }
+    if (c->precision == DGTM_BF16X3) {
+        DGTM_TRY(tc_prepare_y(c->tc, c->Y64, c->stream));
+        *n = 1;
+    }
+    return DGTM_OK;
+}
+
+void free_ctx(dgtm_ctx *c)
+{
+    if (!c)
+        return;
+    void *ptrs[] = {c->T64, c->T32, c->tt, c->FI, c->Y64, c->Y32, c->yy, c->W, c->colstat,
+                    c->part, c->Gpart, c->RTpart, c->G, c->RT, c->A, c->B, c->work, c->bterm,
+                    c->scal, c->flag};
+    for (void *p : ptrs)
+        if (p)
+            cudaFree(p);
+    if (c->hscal)
+        cudaFreeHost(c->hscal);
+    if (c->hflag)
+        cudaFreeHost(c->hflag);
+    if (c->tc)
+        tc_destroy(c->tc);
+    for (int p = 0; p < DGTM_NPHASES; p++)
+        for (int q = 0; q < 2; q++)
+            if (c->ev[p][q])
+                cudaEventDestroy(c->ev[p][q]);
+    if (c->stream)
+        cudaStreamDestroy(c->stream);
+    free(c);
+}
+
+}  // namespace
+
+extern "C" {
+
+int dgtm_version(void) { return 10000; }
+
+const char *dgtm_last_error_string(void) { return g_err; }
+
+int dgtm_ctx_create(int N, int D, int K, int M1, const double *T, int ldT, const double *FI,
+                    int ldFI, int precision, dgtm_ctx **out)
+{
+    g_err[0] = 0;
+    if (!out) {
+        set_error(DGTM_EINVAL, "out is null");
+        return DGTM_EINVAL;
+    }
+    *out = nullptr;
+    if (N < 1 || D < 1 || K < 1 || M1 < 1 || !T || !FI || ldT < D || ldFI < M1) {
+        set_error(DGTM_EINVAL, "bad shape: N=%d D=%d K=%d M1=%d ldT=%d ldFI=%d", N, D, K, M1,
+                  ldT, ldFI);
+        return DGTM_EINVAL;
+    }
+    if (precision != DGTM_FP64 && precision != DGTM_FP32 && precision != DGTM_BF16X3) {
+        set_error(DGTM_EINVAL, "unknown precision form %d", precision);
+        return DGTM_EINVAL;
+    }
+    if (D > 256) {
+        set_error(DGTM_ENOTSUP, "D = %d > 256 is not supported", D);
+        return DGTM_ENOTSUP;
+    }
+    if ((long long) K * D > (1LL << 31) || (long long) N * D > (1LL << 40)) {
+        set_error(DGTM_ENOTSUP, "problem too large: N=%d K=%d D=%d", N, K, D);
+        return DGTM_ENOTSUP;
+    }
+    dgtm_ctx *c = (dgtm_ctx *) calloc(1, sizeof(dgtm_ctx));
+    if (!c) {
+        set_error(DGTM_ENOMEM, "host allocation failed");
+        return DGTM_ENOMEM;
+    }
+    c->N = N;
+    c->D = D;
+    c->K = K;
+    c->M1 = M1;
+    c->precision = precision;
+    c->solver = DGTM_SOLVE_CHOLESKY;
+    int r = DGTM_OK;
+#define CK(expr)               \
+    do {                       \
+        r = (expr);            \
+        if (r != DGTM_OK) {    \
+            free_ctx(c);       \
+            return r;          \
+        }                      \
+    } while (0)
+#define CKC(expr)                                                                       \
+    do {                                                                                \
+        cudaError_t _e = (expr);                                                        \
+        if (_e != cudaSuccess) {                                                        \
+            set_error(DGTM_ECUDA, "%s: %s", #expr, cudaGetErrorString(_e));              \
+            free_ctx(c);                                                                \
+            return DGTM_ECUDA;                                                          \
+        }                                                                               \
+    } while (0)
+    CKC(cudaGetDevice(&c->device));
+    CKC(cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, c->device));
+    CKC(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+
+    const size_t ND = (size_t) N * D, KD = (size_t) K * D;
+    CK(dev_alloc(&c->T64, ND));
+    CK(dev_alloc(&c->tt, N));
+    CK(dev_alloc(&c->FI, (size_t) K * M1));
+    CK(dev_alloc(&c->Y64, KD));
+    CK(dev_alloc(&c->yy, K));
+    CK(dev_alloc(&c->W, (size_t) M1 * D));
+    CK(dev_alloc(&c->colstat, N));
+    CK(dev_alloc(&c->G, K));
+    CK(dev_alloc(&c->RT, KD));
+    CK(dev_alloc(&c->A, (size_t) M1 * M1));
+    CK(dev_alloc(&c->B, (size_t) M1 * D));
+    CK(dev_alloc(&c->work, 2 * (size_t) M1 * M1 + (size_t) M1 * D));
+    CK(dev_alloc(&c->bterm, K));
+    CK(dev_alloc(&c->scal, 8));
+    CK(dev_alloc(&c->flag, 4));
+    CKC(cudaMallocHost((void **) &c->hscal, 8 * sizeof(double)));
+    CKC(cudaMallocHost((void **) &c->hflag, 4 * sizeof(int)));
+
+    CKC(cudaMemcpy2DAsync(c->T64, sizeof(double) * D, T, sizeof(double) * (size_t) ldT,
+                          sizeof(double) * D, N, cudaMemcpyHostToDevice, c->stream));
+    CKC(cudaMemcpy2DAsync(c->FI, sizeof(double) * M1, FI, sizeof(double) * (size_t) ldFI,
+                          sizeof(double) * M1, K, cudaMemcpyHostToDevice, c->stream));
+    CK(launch_norms(c->T64, N, D, c->tt, c->stream));
+    CK(launch_sum_ratio(c->tt, N, 0.0, 1.0, c->scal, c->stream));
+    CKC(cudaMemcpyAsync(c->hscal, c->scal, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+
+    if (precision == DGTM_FP64 || precision == DGTM_FP32) {
+        c->nblk1 = pass1_simt_blocks(N);
+        const int kt = pass2_simt_ktiles(K);
+        int nsplit = (2 * c->sms + kt - 1) / kt;
+        const int max_split = ceil_div(N, 64);
+        if (nsplit > max_split)
+            nsplit = max_split;
+        if (nsplit < 1)
+            nsplit = 1;
+        c->nsplit = nsplit;
+        c->n_per_split = ceil_div(ceil_div(N, nsplit), 64) * 64;
+        c->nsplit = ceil_div(N, c->n_per_split);
+        CK(dev_alloc(&c->part, 2 * (size_t) c->nblk1));
+        CK(dev_alloc(&c->Gpart, (size_t) c->nsplit * K));
+        CK(dev_alloc(&c->RTpart, (size_t) c->nsplit * KD));
+        if (precision == DGTM_FP32) {
+            CK(dev_alloc(&c->T32, ND));
+            CK(dev_alloc(&c->Y32, KD));
+            CK(launch_to_f32(c->T64, ND, c->T32, c->stream));
+        }
+    } else {
+        CK(tc_create(&c->tc, N, D, K, c->sms, c->T64, c->tt, c->stream));
+        c->nblk1 = tc_pass1_blocks(c->tc);
+        CK(dev_alloc(&c->part, 2 * (size_t) c->nblk1));
+    }
+    CKC(cudaStreamSynchronize(c->stream));
+    c->sum_tt = c->hscal[0];
+    *out = c;
+    return DGTM_OK;
+#undef CK
+#undef CKC
+}
+
+int dgtm_ctx_destroy(dgtm_ctx *ctx)
+{
+    if (!ctx)
+        return DGTM_OK;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    free_ctx(ctx);
+    return DGTM_OK;
+}
+
+int dgtm_set_solver(dgtm_ctx *ctx, int solver)
+{
+    DGTM_TRY(check_ctx(ctx));
+    if (solver != DGTM_SOLVE_CHOLESKY && solver != DGTM_SOLVE_SVD) {
+        set_error(DGTM_EINVAL, "unknown solver %d", solver);
+        return DGTM_EINVAL;
+    }
+    ctx->solver = solver;
+    return DGTM_OK;
+}
+
+int dgtm_set_Y(dgtm_ctx *ctx, const double *Y, int ldY)
+{
+    DGTM_TRY(check_ctx(ctx));
+    if (!Y || ldY < ctx->D) {
+        set_error(DGTM_EINVAL, "bad Y (ldY=%d, D=%d)", ldY, ctx->D);
+        return DGTM_EINVAL;
+    }
+    DGTM_CUDA_TRY(cudaMemcpy2DAsync(ctx->Y64, sizeof(double) * ctx->D, Y,
+                                    sizeof(double) * (size_t) ldY, sizeof(double) * ctx->D,
+                                    ctx->K, cudaMemcpyHostToDevice, ctx->stream));
+    DGTM_TRY(launch_norms(ctx->Y64, ctx->K, ctx->D, ctx->yy, ctx->stream));
+    int nl = 0;
+    DGTM_TRY(refresh_y_copies(ctx, &nl));
+    ctx->stats_valid = 0;
+    ctx->rt_valid = 0;
+    return sync_and_check(ctx);
+}
+
+int dgtm_get_Y(dgtm_ctx *ctx, double *Y, int ldY)
+{
+    DGTM_TRY(check_ctx(ctx));
+    if (!Y || ldY < ctx->D) {
+        set_error(DGTM_EINVAL, "bad Y (ldY=%d, D=%d)", ldY, ctx->D);
+        return DGTM_EINVAL;
+    }
+    DGTM_CUDA_TRY(cudaMemcpy2DAsync(Y, sizeof(double) * (size_t) ldY, ctx->Y64,
+                                    sizeof(double) * ctx->D, sizeof(double) * ctx->D, ctx->K,
+                                    cudaMemcpyDeviceToHost, ctx->stream));
+    return sync_and_check(ctx);
+}
+
+int dgtm_get_W(dgtm_ctx *ctx, double *W, int ldW)
+{
+    DGTM_TRY(check_ctx(ctx));
+    if (!W || ldW < ctx->D) {
+        set_error(DGTM_EINVAL, "bad W (ldW=%d, D=%d)", ldW, ctx->D);
+        return DGTM_EINVAL;
+    }
+    if (!ctx->w_valid) {
+        set_error(DGTM_ESTATE, "no M-step has run yet");
+        return DGTM_ESTATE;
+    }
+    DGTM_CUDA_TRY(cudaMemcpy2DAsync(W, sizeof(double) * (size_t) ldW, ctx->W,
+                                    sizeof(double) * ctx->D, sizeof(double) * ctx->D, ctx->M1,
+                                    cudaMemcpyDeviceToHost, ctx->stream));
+    return sync_and_check(ctx);
+}
+
+int dgtm_estep(dgtm_ctx *ctx, double beta, int isDA, double temp, double *llh, double *nfree)
+{
+    DGTM_TRY(check_ctx(ctx));
+    if (!(beta > 0.0) || !isfinite(beta) || !(temp > 0.0) || !isfinite(temp)) {
+        set_error(DGTM_EINVAL, "beta (%g) and temp (%g) must be positive and finite", beta, temp);
+        return DGTM_EINVAL;
+    }
+    isDA = isDA ? 1 : 0;
+    const double c1 = beta / 2.0, c2 = beta / (2.0 * temp);
+    int r, nl = 1;
+    DGTM_TRY(phase_begin(ctx, DGTM_PHASE_ESTEP));
+    if (ctx->precision == DGTM_FP64) {
+        Pass1Args<double> a{ctx->T64, ctx->Y64, ctx->tt, ctx->yy, ctx->N, ctx->D, ctx->K,
+                            c1, c2, isDA, ctx->colstat, ctx->part};
+        r = launch_pass1_simt<double>(a, ctx->stream);
+    } else if (ctx->precision == DGTM_FP32) {
+        Pass1Args<float> a{ctx->T32, ctx->Y32, ctx->tt, ctx->yy, ctx->N, ctx->D, ctx->K,
+                           c1, c2, isDA, ctx->colstat, ctx->part};
+        r = launch_pass1_simt<float>(a, ctx->stream);
+    } else {
+        r = tc_estep(ctx->tc, ctx->Y64, c1, c2, isDA, ctx->colstat, ctx->part, ctx->stream, &nl);
+    }
+    DGTM_TRY(r);
+    DGTM_TRY(phase_end(ctx, DGTM_PHASE_ESTEP, nl));
+    DGTM_TRY(phase_begin(ctx, DGTM_PHASE_ESTEP_REDUCE));
+    DGTM_TRY(launch_sum_pairs(ctx->part, ctx->nblk1, ctx->scal, ctx->stream));
+    DGTM_TRY(phase_end(ctx, DGTM_PHASE_ESTEP_REDUCE, 1));
+    DGTM_CUDA_TRY(cudaMemcpyAsync(ctx->hscal, ctx->scal, 2 * sizeof(double),
+                                  cudaMemcpyDeviceToHost, ctx->stream));
+    if (ctx->tc)
+        DGTM_TRY(tc_fetch_status(ctx->tc, ctx->stream));
+    DGTM_TRY(sync_and_check(ctx));
+    if (ctx->tc)
+        DGTM_TRY(tc_check_status(ctx->tc));
+    const double S1 = ctx->hscal[0], S2 = ctx->hscal[1];
+    // comm/mpicomm.c:483-497
+    const int N = ctx->N, K = ctx->K, D = ctx->D;
+    const double base = N * ((D / 2.0) * log(beta / (2.0 * M_PI)) - log((double) K));
+    const double q_llh = (base + S1) / (double) N;
+    const double q_free = isDA ? (base + temp * S2) / (double) N : -q_llh;
+    if (llh)
+        *llh = q_llh;
+    if (nfree)
+        *nfree = q_free;
+    ctx->beta = beta;
+    ctx->temp = temp;
+    ctx->isDA = isDA;
+    ctx->stats_valid = 1;
+    ctx->rt_valid = 0;
+    return DGTM_OK;
+}
+
+int dgtm_mstep(dgtm_ctx *ctx, double *W, int ldW, double *Y, int ldY, double *beta)
+{
+    DGTM_TRY(check_ctx(ctx));
+    if (!ctx->stats_valid) {
+        set_error(DGTM_ESTATE, "dgtm_mstep needs an E-step on the current centres first");
+        return DGTM_ESTATE;
+    }
+    if ((W && ldW < ctx->D) || (Y && ldY < ctx->D)) {
+        set_error(DGTM_EINVAL, "bad leading dimension (ldW=%d ldY=%d D=%d)", ldW, ldY, ctx->D);
+        return DGTM_EINVAL;
+    }
+    const int N = ctx->N, K = ctx->K, D = ctx->D, M1 = ctx->M1;
+    const double c = ctx->isDA ? ctx->beta / (2.0 * ctx->temp) : ctx->beta / 2.0;
+    int npass = 1, nsmall = 5;
+    DGTM_TRY(phase_begin(ctx, DGTM_PHASE_MSTEP_PASS));
+    if (ctx->precision == DGTM_FP64) {
+        Pass2Args<double> a{ctx->T64, ctx->Y64, ctx->tt, ctx->yy, ctx->colstat, N, D, K, c,
+                            ctx->n_per_split, ctx->Gpart, ctx->RTpart};
+        DGTM_TRY(launch_pass2_simt<double>(a, ctx->nsplit, ctx->stream));
+    } else if (ctx->precision == DGTM_FP32) {
+        Pass2Args<float> a{ctx->T32, ctx->Y32, ctx->tt, ctx->yy, ctx->colstat, N, D, K, c,
+                           ctx->n_per_split, ctx->Gpart, ctx->RTpart};
+        DGTM_TRY(launch_pass2_simt<float>(a, ctx->nsplit, ctx->stream));
+    } else {
+        DGTM_TRY(tc_mstep_pass(ctx->tc, ctx->colstat, c, ctx->stream, &npass));
+    }
+    DGTM_TRY(phase_end(ctx, DGTM_PHASE_MSTEP_PASS, npass));
+    DGTM_TRY(phase_begin(ctx, DGTM_PHASE_MSTEP_SOLVE));
+    if (ctx->precision == DGTM_BF16X3) {
+        int nr = 0;
+        DGTM_TRY(tc_mstep_reduce(ctx->tc, ctx->G, ctx->RT, ctx->stream, &nr));
+        nsmall += nr;
+    } else {
+        DGTM_TRY(launch_reduce_slices(ctx->Gpart, ctx->RTpart, ctx->nsplit, K, D, ctx->G,
+                                      ctx->RT, ctx->stream));
+        nsmall += 1;
+    }
+    DGTM_TRY(launch_form_ab(ctx->FI, ctx->G, ctx->RT, K, M1, D, ctx->A, ctx->B, ctx->stream));
+    DGTM_TRY(launch_solve(ctx->A, ctx->B, M1, D, ctx->solver, ctx->W, ctx->work, ctx->flag,
+                          ctx->stream));
+    DGTM_TRY(launch_update_y(ctx->FI, ctx->W, ctx->G, ctx->RT, K, M1, D, ctx->Y64, ctx->yy,
+                             ctx->bterm, ctx->stream));
+    DGTM_TRY(launch_sum_ratio(ctx->bterm, K, ctx->sum_tt, (double) ((long long) N * D),
+                              ctx->scal, ctx->stream));
+    int ny = 0;
+    DGTM_TRY(refresh_y_copies(ctx, &ny));
+    DGTM_TRY(phase_end(ctx, DGTM_PHASE_MSTEP_SOLVE, nsmall + ny - 1));
+    DGTM_CUDA_TRY(cudaMemcpyAsync(ctx->hscal, ctx->scal, 2 * sizeof(double),
+                                  cudaMemcpyDeviceToHost, ctx->stream));
+    DGTM_CUDA_TRY(cudaMemcpyAsync(ctx->hflag, ctx->flag, sizeof(int), cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+    if (W)
+        DGTM_CUDA_TRY(cudaMemcpy2DAsync(W, sizeof(double) * (size_t) ldW, ctx->W,
+                                        sizeof(double) * D, sizeof(double) * D, M1,
+                                        cudaMemcpyDeviceToHost, ctx->stream));
+    if (Y)
+        DGTM_CUDA_TRY(cudaMemcpy2DAsync(Y, sizeof(double) * (size_t) ldY, ctx->Y64,
+                                        sizeof(double) * D, sizeof(double) * D, K,
+                                        cudaMemcpyDeviceToHost, ctx->stream));
+    if (ctx->tc)
+        DGTM_TRY(tc_fetch_status(ctx->tc, ctx->stream));
+    DGTM_TRY(sync_and_check(ctx));
+    if (ctx->tc)
+        DGTM_TRY(tc_check_status(ctx->tc));
+    ctx->stats_valid = 0;
+    ctx->rt_valid = 1;
+    ctx->w_valid = 1;
+    if (ctx->hflag[0] != 0) {
+        set_error(DGTM_ENOTSPD, "A = FI^T diag(G) FI is not positive definite (Cholesky)");
+        return DGTM_ENOTSPD;
+    }
+    const double b = ctx->hscal[1];
+    if (!isfinite(b)) {
+        set_error(DGTM_ENONFINITE, "beta update is not finite (sum R o D = %g)", ctx->hscal[0]);
+        return DGTM_ENONFINITE;
+    }
+    if (beta)
+        *beta = b;
+    return DGTM_OK;
+}
+
+int dgtm_get_stats(dgtm_ctx *ctx, double *G, double *RT, int ldRT)
+{
+    DGTM_TRY(check_ctx(ctx));
+    if (!ctx->rt_valid) {
+        set_error(DGTM_ESTATE, "no M-step statistics available");
+        return DGTM_ESTATE;
+    }
+    if (RT && ldRT < ctx->D) {
+        set_error(DGTM_EINVAL, "bad ldRT %d", ldRT);
+        return DGTM_EINVAL;
+    }
+    if (G)
+        DGTM_CUDA_TRY(cudaMemcpyAsync(G, ctx->G, sizeof(double) * ctx->K, cudaMemcpyDeviceToHost,
+                                      ctx->stream));
+    if (RT)
+        DGTM_CUDA_TRY(cudaMemcpy2DAsync(RT, sizeof(double) * (size_t) ldRT, ctx->RT,
+                                        sizeof(double) * ctx->D, sizeof(double) * ctx->D,
+                                        ctx->K, cudaMemcpyDeviceToHost, ctx->stream));
+    return sync_and_check(ctx);
+}
+
+int dgtm_set_timing(dgtm_ctx *ctx, int on)
+{
+    DGTM_TRY(check_ctx(ctx));
+    if (on && !ctx->ev[0][0]) {
+        for (int p = 0; p < DGTM_NPHASES; p++)
+            for (int q = 0; q < 2; q++)
+                DGTM_CUDA_TRY(cudaEventCreate(&ctx->ev[p][q]));
+    }
+    DGTM_TRY(sync_and_check(ctx));
+    ctx->timing = on ? 1 : 0;
+    return DGTM_OK;
+}
+
+int dgtm_reset_timing(dgtm_ctx *ctx)
+{
+    DGTM_TRY(check_ctx(ctx));
+    DGTM_TRY(sync_and_check(ctx));
+    for (int p = 0; p < DGTM_NPHASES; p++) {
+        ctx->ms[p] = 0.0;
+        ctx->launches[p] = 0;
+        ctx->calls[p] = 0;
+    }
+    return DGTM_OK;
+}
+
+int dgtm_get_timing(dgtm_ctx *ctx, double *ms, long long *launches, long long *calls)
+{
+    DGTM_TRY(check_ctx(ctx));
+    DGTM_TRY(sync_and_check(ctx));
+    for (int p = 0; p < DGTM_NPHASES; p++) {
+        if (ms)
+            ms[p] = ctx->ms[p];
+        if (launches)
+            launches[p] = ctx->launches[p];
+        if (calls)
+            calls[p] = ctx->calls[p];
+    }
+    return DGTM_OK;
+}
+
+int dgtm_get_stream(dgtm_ctx *ctx, void **stream)
+{
+    DGTM_TRY(check_ctx(ctx));
+    if (!stream) {
+        set_error(DGTM_EINVAL, "stream is null");
+        return DGTM_EINVAL;
+    }
+    *stream = (void *) ctx->stream;
+    return DGTM_OK;
+}
+
+int dgtm_map(dgtm_ctx *ctx, const double *X, int L, double *M, int ldM)
+{
+    DGTM_TRY(check_ctx(ctx));
+    if (!ctx->stats_valid) {
+        set_error(DGTM_ESTATE, "dgtm_map needs an E-step on the current centres first");
+        return DGTM_ESTATE;
+    }
+    if (!X || !M || L < 1 || L > 8 || ldM < L) {
+        set_error(DGTM_EINVAL, "bad MAP arguments (L=%d ldM=%d)", L, ldM);
+        return DGTM_EINVAL;
+    }
+    const double c = ctx->isDA ? ctx->beta / (2.0 * ctx->temp) : ctx->beta / 2.0;
+    double *dX = nullptr, *dM = nullptr;
+    DGTM_TRY(dev_alloc(&dX, (size_t) ctx->K * L));
+    int r = dev_alloc(&dM, (size_t) ctx->N * L);
+    if (r != DGTM_OK) {
+        cudaFree(dX);
+        return r;
+    }
+    r = DGTM_OK;
+    cudaError_t e = cudaMemcpyAsync(dX, X, sizeof(double) * ctx->K * L, cudaMemcpyHostToDevice,
+                                    ctx->stream);
+    if (e == cudaSuccess) {
+        r = launch_map(ctx->T64, ctx->Y64, ctx->tt, ctx->yy, ctx->colstat, ctx->N, ctx->D, ctx->K,
+                       c, dX, L, dM, ctx->stream);
+        if (r == DGTM_OK)
+            e = cudaMemcpy2DAsync(M, sizeof(double) * (size_t) ldM, dM, sizeof(double) * L,
+                                  sizeof(double) * L, ctx->N, cudaMemcpyDeviceToHost,
+                                  ctx->stream);
+    }
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(ctx->stream);
+    cudaFree(dX);
+    cudaFree(dM);
+    if (e != cudaSuccess) {
+        set_error(DGTM_ECUDA, "dgtm_map: %s", cudaGetErrorString(e));
+        return DGTM_ECUDA;
+    }
+    return r;
+}
+
+int dgtm_get_R_block(dgtm_ctx *ctx, int k0, int nk, int n0, int nn, double *R, int ldR)
+{
+    DGTM_TRY(check_ctx(ctx));
+    if (!ctx->stats_valid) {
+        set_error(DGTM_ESTATE, "dgtm_get_R_block needs an E-step on the current centres first");
+        return DGTM_ESTATE;
+    }
+    if (!R || k0 < 0 || n0 < 0 || nk < 1 || nn < 1 || k0 + nk > ctx->K || n0 + nn > ctx->N ||
+        ldR < nn) {
+        set_error(DGTM_EINVAL, "bad R block k0=%d nk=%d n0=%d nn=%d ldR=%d", k0, nk, n0, nn, ldR);
+        return DGTM_EINVAL;
+    }
+    const double c = ctx->isDA ? ctx->beta / (2.0 * ctx->temp) : ctx->beta / 2.0;
+    double *dR = nullptr;
+    DGTM_TRY(dev_alloc(&dR, (size_t) nk * nn));
+    int r = launch_r_block(ctx->T64, ctx->Y64, ctx->tt, ctx->yy, ctx->colstat, ctx->D, ctx->K, c,
+                           k0, nk, n0, nn, dR, ctx->stream);
+    cudaError_t e = cudaSuccess;
+    if (r == DGTM_OK)
+        e = cudaMemcpy2DAsync(R, sizeof(double) * (size_t) ldR, dR, sizeof(double) * nn,
+                              sizeof(double) * nn, nk, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(ctx->stream);
+    cudaFree(dR);
+    if (e != cudaSuccess) {
+        set_error(DGTM_ECUDA, "dgtm_get_R_block: %s", cudaGetErrorString(e));
+        return DGTM_ECUDA;
+    }
+    return r;
+}
+
+}  // extern "C"

@@ -1,0 +1,74 @@
+// kernels.cuh -- argument blocks and launchers shared by the translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace dgtm {
+
+// ---- CUDA-core (FP64 / FP32) forms -------------------------------------------
+template <typename F>
+struct Pass1Args {
+    const F *T;          // N x D
+    const F *Y;          // K x D
+    const double *tt;    // N   |t_n|^2
+    const double *yy;    // K   |y_k|^2
+    int N, D, K;
+    double c1, c2;       // beta/2, beta/(2 temp)
+    int isDA;
+    double2 *colstat;    // N   (dmin_n, log s_n)  (log s_n = NaN: zero column)
+    double *part;        // 2 per block: sum of the llh and nfree terms
+};
+
+template <typename F>
+struct Pass2Args {
+    const F *T;
+    const F *Y;
+    const double *tt;
+    const double *yy;
+    const double2 *colstat;
+    int N, D, K;
+    double c;            // beta/(2 temp) (DA) or beta/2
+    int n_per_split;
+    double *Gpart;       // nsplit x K
+    double *RTpart;      // nsplit x K x D
+};
+
+template <typename F> int launch_pass1_simt(const Pass1Args<F> &a, cudaStream_t s);
+template <typename F> int launch_pass2_simt(const Pass2Args<F> &a, int nsplit, cudaStream_t s);
+int pass1_simt_blocks(int N);
+int pass2_simt_ktiles(int K);
+// M = R^T X (N x L, L <= 8) and explicit R blocks, FP64, from the column statistics.
+int launch_map(const double *T, const double *Y, const double *tt, const double *yy,
+               const double2 *colstat, int N, int D, int K, double c, const double *X, int L,
+               double *M, cudaStream_t s);
+int launch_r_block(const double *T, const double *Y, const double *tt, const double *yy,
+                   const double2 *colstat, int D, int K, double c, int k0, int nk, int n0, int nn,
+                   double *R, cudaStream_t s);
+
+// ---- M-step (FP64, all forms) ---------------------------------------------------
+// Sum nsplit slices in a fixed order: G[k] = sum_s Gpart[s][k], RT = sum_s RTpart[s].
+int launch_reduce_slices(const double *Gpart, const double *RTpart, int nsplit, int K,
+                         int D, double *G, double *RT, cudaStream_t s);
+// A = FI^T diag(G) FI (M1 x M1), B = FI^T RT (M1 x D).
+int launch_form_ab(const double *FI, const double *G, const double *RT, int K, int M1,
+                   int D, double *A, double *B, cudaStream_t s);
+// W = A^{-1} B by Cholesky (solver 0) or symmetric-eigen pseudo-inverse (solver 1).
+// work: M1*M1 + M1 doubles (+ M1*M1 for solver 1).  flag[0] != 0 on failure.
+int launch_solve(const double *A, const double *B, int M1, int D, int solver, double *W,
+                 double *work, int *flag, cudaStream_t s);
+// Y = FI W, yy = |y|^2, bterm_k = G_k yy_k - 2 y_k.RT_k (G/RT may be null: no bterm).
+int launch_update_y(const double *FI, const double *W, const double *G, const double *RT,
+                    int K, int M1, int D, double *Y, double *yy, double *bterm,
+                    cudaStream_t s);
+// yy = |y|^2 for a given Y.
+int launch_norms(const double *X, int rows, int D, double *out, cudaStream_t s);
+// out[0] = sum_i v[i] (fixed order) + add; out[1] = num / out[0].
+int launch_sum_ratio(const double *v, int n, double add, double num, double *out,
+                     cudaStream_t s);
+// Sum of the pass-1 block partials: out[0] = sum part[2b], out[1] = sum part[2b+1].
+int launch_sum_pairs(const double *part, int nblocks, double *out, cudaStream_t s);
+// Element-wise conversion to FP32.
+int launch_to_f32(const double *src, size_t n, float *dst, cudaStream_t s);
+
+}  // namespace dgtm

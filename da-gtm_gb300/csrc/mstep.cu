@@ -1,0 +1,462 @@
+// mstep.cu -- the small FP64 kernels of the M-step, shared by every form.
+//
+//   reduce_slices : G_k = sum_s Gpart[s][k], RT = sum_s RTpart[s] (fixed order)
+//   form_ab       : A = FI^T diag(G) FI, B = FI^T RT     (dagtm/dagtm.cxx:1715-1761)
+//   solve         : A W = B, FP64 Cholesky or symmetric-eigen pseudo-inverse
+//                   with exactly-zero eigenvalues dropped (the semantics of
+//                   gsl_linalg_SV_solve used by dagtm_solve2, comm/comm.c:1299-1348)
+//   update_y      : Y = FI W (dagtm/dagtm.cxx:1769), |y_k|^2 and the beta terms
+//   sum_ratio     : beta = N D / (sum_k G_k|y_k|^2 - 2 y_k.RT_k + sum_n |t_n|^2)
+//                   = N D / sum_kn R_kn |y_k - t_n|^2 (comm/mpicomm.c:276-302
+//                   evaluates the same sum over an explicit K x N distance matrix;
+//                   every column of R sums to one, which gives the closed form)
+//
+// Every reduction runs in a fixed order, so repeated runs are bit-identical.
+#include "common.cuh"
+#include "kernels.cuh"
+
+#include <math.h>
+
+namespace dgtm {
+
+__global__ void reduce_slices_kernel(const double *__restrict__ Gpart,
+                                     const double *__restrict__ RTpart, int nsplit, int K, int D,
+                                     double *__restrict__ G, double *__restrict__ RT)
+{
+    const size_t KD = (size_t) K * D;
+    for (size_t i = blockIdx.x * (size_t) blockDim.x + threadIdx.x; i < KD + K;
+         i += (size_t) gridDim.x * blockDim.x) {
+        double s = 0.0;
+        if (i < KD) {
+            for (int p = 0; p < nsplit; p++)
+                s += RTpart[(size_t) p * KD + i];
+            RT[i] = s;
+        } else {
+            const size_t k = i - KD;
+            for (int p = 0; p < nsplit; p++)
+                s += Gpart[(size_t) p * K + k];
+            G[k] = s;
+        }
+    }
+}
+
+int launch_reduce_slices(const double *Gpart, const double *RTpart, int nsplit, int K, int D,
+                         double *G, double *RT, cudaStream_t s)
+{
+    const size_t n = (size_t) K * D + K;
+    int blocks = (int) ((n + 255) / 256);
+    if (blocks > 4096)
+        blocks = 4096;
+    reduce_slices_kernel<<<blocks, 256, 0, s>>>(Gpart, RTpart, nsplit, K, D, G, RT);
+    DGTM_CUDA_TRY(cudaGetLastError());
+    return DGTM_OK;
+}
+
+// grid (M1, ceil((D + M1) / 32)); warp w sums k in its chunk, lane = output column.
+__global__ void __launch_bounds__(256) form_ab_kernel(const double *__restrict__ FI,
+                                                      const double *__restrict__ G,
+                                                      const double *__restrict__ RT, int K,
+                                                      int M1, int D, double *__restrict__ A,
+                                                      double *__restrict__ B)
+{
+    __shared__ double part[8][33];
+    const int m = blockIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int c = blockIdx.y * 32 + lane;
+    const int chunk = (K + 7) / 8;
+    const int kb = warp * chunk, ke = min(K, kb + chunk);
+    double s = 0.0;
+    if (c < D) {
+        for (int k = kb; k < ke; k++)
+            s += FI[(size_t) k * M1 + m] * RT[(size_t) k * D + c];
+    } else if (c < D + M1) {
+        const int j = c - D;
+        for (int k = kb; k < ke; k++)
+            s += FI[(size_t) k * M1 + m] * (FI[(size_t) k * M1 + j] * G[k]);
+    }
+    part[warp][lane] = s;
+    __syncthreads();
+    if (warp == 0) {
+        double t = 0.0;
+        for (int w = 0; w < 8; w++)
+            t += part[w][lane];
+        if (c < D)
+            B[(size_t) m * D + c] = t;
+        else if (c < D + M1)
+            A[(size_t) m * M1 + (c - D)] = t;
+    }
+}
+
+int launch_form_ab(const double *FI, const double *G, const double *RT, int K, int M1, int D,
+                   double *A, double *B, cudaStream_t s)
+{
+    dim3 grid(M1, ceil_div(D + M1, 32));
+    form_ab_kernel<<<grid, 256, 0, s>>>(FI, G, RT, K, M1, D, A, B);
+    DGTM_CUDA_TRY(cudaGetLastError());
+    return DGTM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// solvers (one block)
+// ---------------------------------------------------------------------------
+constexpr int SOLVE_THREADS = 512;
+constexpr int SMEM_SOLVE_MAX = 110;  // M1 up to which L lives in shared memory
+
+// Left-looking Cholesky, L[i][j] = (A[i][j] - sum_{p<j} L[i][p] L[j][p]) / L[j][j],
+// then forward and back substitution, one right-hand side per thread.
+__global__ void __launch_bounds__(SOLVE_THREADS) cholesky_kernel(const double *__restrict__ A,
+                                                                const double *__restrict__ B,
+                                                                int M1, int D,
+                                                                double *__restrict__ W,
+                                                                double *__restrict__ work,
+                                                                int *flag)
+{
+    extern __shared__ double sh[];
+    double *L = (M1 <= SMEM_SOLVE_MAX) ? sh : work;
+    __shared__ int bad;
+    if (threadIdx.x == 0)
+        bad = 0;
+    for (int i = threadIdx.x; i < M1 * M1; i += blockDim.x)
+        L[i] = A[i];
+    __syncthreads();
+    for (int j = 0; j < M1; j++) {
+        for (int i = j + threadIdx.x; i < M1; i += blockDim.x) {
+            double v = L[(size_t) i * M1 + j];
+            for (int p = 0; p < j; p++)
+                v -= L[(size_t) i * M1 + p] * L[(size_t) j * M1 + p];
+            L[(size_t) i * M1 + j] = v;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const double d = L[(size_t) j * M1 + j];
+            if (!(d > 0.0) || !isfinite(d)) {
+                bad = 1;
+                L[(size_t) j * M1 + j] = 1.0;
+            } else {
+                L[(size_t) j * M1 + j] = sqrt(d);
+            }
+        }
+        __syncthreads();
+        const double ljj = L[(size_t) j * M1 + j];
+        for (int i = j + 1 + threadIdx.x; i < M1; i += blockDim.x)
+            L[(size_t) i * M1 + j] /= ljj;
+        __syncthreads();
+    }
+    if (bad) {
+        if (threadIdx.x == 0)
+            flag[0] = DGTM_ENOTSPD;
+        return;
+    }
+    for (int c = threadIdx.x; c < D; c += blockDim.x) {
+        for (int i = 0; i < M1; i++) {
+            double v = B[(size_t) i * D + c];
+            for (int p = 0; p < i; p++)
+                v -= L[(size_t) i * M1 + p] * W[(size_t) p * D + c];
+            W[(size_t) i * D + c] = v / L[(size_t) i * M1 + i];
+        }
+        for (int i = M1 - 1; i >= 0; i--) {
+            double v = W[(size_t) i * D + c];
+            for (int p = i + 1; p < M1; p++)
+                v -= L[(size_t) p * M1 + i] * W[(size_t) p * D + c];
+            W[(size_t) i * D + c] = v / L[(size_t) i * M1 + i];
+        }
+    }
+}
+
+// Parallel cyclic Jacobi (round-robin pairing) on the symmetric A, then
+// W = V diag(1/lambda, 0 where lambda == 0) V^T B.
+__global__ void __launch_bounds__(SOLVE_THREADS) jacobi_solve_kernel(const double *__restrict__ A,
+                                                                    const double *__restrict__ B,
+                                                                    int M1, int D,
+                                                                    double *__restrict__ W,
+                                                                    double *__restrict__ work,
+                                                                    int *flag)
+{
+    double *S = work;                        // M1 x M1 (becomes diagonal)
+    double *V = work + (size_t) M1 * M1;     // M1 x M1 eigenvectors (columns)
+    double *tmp = V + (size_t) M1 * M1;      // M1 x D
+    __shared__ double cs[SOLVE_THREADS], sn[SOLVE_THREADS];
+    __shared__ int pp[SOLVE_THREADS], qq[SOLVE_THREADS];
+    __shared__ double red[32];
+    __shared__ int done;
+    const int n = M1 + (M1 & 1);  // even number of slots; slot M1 (if any) is a dummy
+    for (int i = threadIdx.x; i < M1 * M1; i += blockDim.x) {
+        S[i] = A[i];
+        V[i] = ((i / M1) == (i % M1)) ? 1.0 : 0.0;
+    }
+    __syncthreads();
+    for (int sweep = 0; sweep < 60; sweep++) {
+        double off = 0.0, tot = 0.0;
+        for (int i = threadIdx.x; i < M1 * M1; i += blockDim.x) {
+            const double v = S[i] * S[i];
+            tot += v;
+            if ((i / M1) != (i % M1))
+                off += v;
+        }
+        off = block_sum_fixed(off, red);
+        tot = block_sum_fixed(tot, red);
+        if (threadIdx.x == 0)
+            done = (off <= 1e-32 * tot);
+        __syncthreads();
+        if (done)
+            break;
+        for (int r = 0; r < n - 1; r++) {
+            // round-robin: slot 0 fixed, the others rotate
+            for (int t = threadIdx.x; t < n / 2; t += blockDim.x) {
+                int a = (t == 0) ? 0 : 1 + ((t - 1 + r) % (n - 1));
+                int b = 1 + ((n - 2 - t + r) % (n - 1));
+                int p = min(a, b), q = max(a, b);
+                double c = 1.0, s = 0.0;
+                if (q < M1) {
+                    const double apq = S[(size_t) p * M1 + q];
+                    if (apq != 0.0) {
+                        const double app = S[(size_t) p * M1 + p], aqq = S[(size_t) q * M1 + q];
+                        const double th = (aqq - app) / (2.0 * apq);
+                        const double tt = (th >= 0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
+                        c = 1.0 / sqrt(tt * tt + 1.0);
+                        s = tt * c;
+                    }
+                }
+                pp[t] = p;
+                qq[t] = q;
+                cs[t] = c;
+                sn[t] = s;
+            }
+            __syncthreads();
+            // rows: S <- J^T S
+            for (int idx = threadIdx.x; idx < (n / 2) * M1; idx += blockDim.x) {
+                const int t = idx / M1, k = idx % M1;
+                const int p = pp[t], q = qq[t];
+                if (q >= M1 || sn[t] == 0.0)
+                    continue;
+                const double c = cs[t], s = sn[t];
+                const double sp = S[(size_t) p * M1 + k], sq = S[(size_t) q * M1 + k];
+                S[(size_t) p * M1 + k] = c * sp - s * sq;
+                S[(size_t) q * M1 + k] = s * sp + c * sq;
+            }
+            __syncthreads();
+            // columns: S <- S J, V <- V J
+            for (int idx = threadIdx.x; idx < (n / 2) * M1; idx += blockDim.x) {
+                const int t = idx / M1, k = idx % M1;
+                const int p = pp[t], q = qq[t];
+                if (q >= M1 || sn[t] == 0.0)
+                    continue;
+                const double c = cs[t], s = sn[t];
+                const double sp = S[(size_t) k * M1 + p], sq = S[(size_t) k * M1 + q];
+                S[(size_t) k * M1 + p] = c * sp - s * sq;
+                S[(size_t) k * M1 + q] = s * sp + c * sq;
+                const double vp = V[(size_t) k * M1 + p], vq = V[(size_t) k * M1 + q];
+                V[(size_t) k * M1 + p] = c * vp - s * vq;
+                V[(size_t) k * M1 + q] = s * vp + c * vq;
+            }
+            __syncthreads();
+        }
+    }
+    // tmp = diag(1/lambda) V^T B
+    for (int idx = threadIdx.x; idx < M1 * D; idx += blockDim.x) {
+        const int i = idx / D, c = idx % D;
+        double acc = 0.0;
+        for (int r = 0; r < M1; r++)
+            acc += V[(size_t) r * M1 + i] * B[(size_t) r * D + c];
+        double lam = S[(size_t) i * M1 + i];
+        if (lam != 0.0)
+            lam = 1.0 / lam;
+        tmp[idx] = lam * acc;
+    }
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < M1 * D; idx += blockDim.x) {
+        const int r = idx / D, c = idx % D;
+        double acc = 0.0;
+        for (int i = 0; i < M1; i++)
+            acc += V[(size_t) r * M1 + i] * tmp[(size_t) i * D + c];
+        W[idx] = acc;
+    }
+    if (threadIdx.x == 0)
+        flag[0] = 0;
+}
+
+int launch_solve(const double *A, const double *B, int M1, int D, int solver, double *W,
+                 double *work, int *flag, cudaStream_t s)
+{
+    DGTM_CUDA_TRY(cudaMemsetAsync(flag, 0, sizeof(int), s));
+    if (solver == DGTM_SOLVE_SVD && M1 > 2 * SOLVE_THREADS - 2) {
+        set_error(DGTM_ENOTSUP, "the eigen-SVD solver supports M1 <= %d", 2 * SOLVE_THREADS - 2);
+        return DGTM_ENOTSUP;
+    }
+    if (solver == DGTM_SOLVE_SVD) {
+        jacobi_solve_kernel<<<1, SOLVE_THREADS, 0, s>>>(A, B, M1, D, W, work, flag);
+    } else {
+        const size_t smem = (M1 <= SMEM_SOLVE_MAX) ? sizeof(double) * (size_t) M1 * M1 : 0;
+        DGTM_CUDA_TRY(cudaFuncSetAttribute(cholesky_kernel,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int) (smem > 0 ? smem : 1)));
+        cholesky_kernel<<<1, SOLVE_THREADS, smem, s>>>(A, B, M1, D, W, work, flag);
+    }
+    DGTM_CUDA_TRY(cudaGetLastError());
+    return DGTM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Y = FI W and the per-centre terms of beta
+// ---------------------------------------------------------------------------
+constexpr int WSMEM_MAX = 96 * 1024;
+
+__global__ void __launch_bounds__(256) update_y_kernel(const double *__restrict__ FI,
+                                                      const double *__restrict__ Wg,
+                                                      const double *__restrict__ G,
+                                                      const double *__restrict__ RT, int K,
+                                                      int M1, int D, int w_in_smem,
+                                                      double *__restrict__ Y,
+                                                      double *__restrict__ yy,
+                                                      double *__restrict__ bterm)
+{
+    extern __shared__ double Ws[];
+    const double *W = Wg;
+    if (w_in_smem) {
+        for (int i = threadIdx.x; i < M1 * D; i += blockDim.x)
+            Ws[i] = Wg[i];
+        __syncthreads();
+        W = Ws;
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int k = blockIdx.x * 8 + warp; k < K; k += gridDim.x * 8) {
+        double syy = 0.0, syrt = 0.0;
+        const double *fi = FI + (size_t) k * M1;
+        for (int d = lane; d < D; d += 32) {
+            double y = 0.0;
+            for (int m = 0; m < M1; m++)
+                y += fi[m] * W[(size_t) m * D + d];
+            Y[(size_t) k * D + d] = y;
+            syy += y * y;
+            if (RT)
+                syrt += y * RT[(size_t) k * D + d];
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            syy += __shfl_xor_sync(0xffffffffu, syy, o);
+            syrt += __shfl_xor_sync(0xffffffffu, syrt, o);
+        }
+        if (lane == 0) {
+            yy[k] = syy;
+            if (bterm)
+                bterm[k] = G[k] * syy - 2.0 * syrt;
+        }
+    }
+}
+
+int launch_update_y(const double *FI, const double *W, const double *G, const double *RT, int K,
+                    int M1, int D, double *Y, double *yy, double *bterm, cudaStream_t s)
+{
+    const size_t wbytes = sizeof(double) * (size_t) M1 * D;
+    const int in_smem = wbytes <= WSMEM_MAX;
+    const size_t smem = in_smem ? wbytes : 0;
+    DGTM_CUDA_TRY(cudaFuncSetAttribute(update_y_kernel,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int) (smem > 0 ? smem : 1)));
+    int blocks = ceil_div(K, 8);
+    if (blocks > 1216)
+        blocks = 1216;
+    update_y_kernel<<<blocks, 256, smem, s>>>(FI, W, G, RT, K, M1, D, in_smem, Y, yy, bterm);
+    DGTM_CUDA_TRY(cudaGetLastError());
+    return DGTM_OK;
+}
+
+__global__ void norms_kernel(const double *__restrict__ X, int rows, int D,
+                             double *__restrict__ out)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int wpb = blockDim.x >> 5;
+    for (int r = blockIdx.x * wpb + warp; r < rows; r += gridDim.x * wpb) {
+        double s = 0.0;
+        for (int d = lane; d < D; d += 32) {
+            const double v = X[(size_t) r * D + d];
+            s += v * v;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0)
+            out[r] = s;
+    }
+}
+
+int launch_norms(const double *X, int rows, int D, double *out, cudaStream_t s)
+{
+    int blocks = ceil_div(rows, 8);
+    if (blocks > 4864)
+        blocks = 4864;
+    norms_kernel<<<blocks, 256, 0, s>>>(X, rows, D, out);
+    DGTM_CUDA_TRY(cudaGetLastError());
+    return DGTM_OK;
+}
+
+__global__ void __launch_bounds__(1024) sum_ratio_kernel(const double *__restrict__ v, int n,
+                                                        double add, double num, double *out)
+{
+    __shared__ double red[32];
+    const int per = (n + blockDim.x - 1) / blockDim.x;
+    const int b = threadIdx.x * per, e = min(n, b + per);
+    double s = 0.0;
+    for (int i = b; i < e; i++)
+        s += v[i];
+    s = block_sum_fixed(s, red);
+    if (threadIdx.x == 0) {
+        const double den = s + add;
+        out[0] = den;
+        out[1] = num / den;
+    }
+}
+
+int launch_sum_ratio(const double *v, int n, double add, double num, double *out, cudaStream_t s)
+{
+    sum_ratio_kernel<<<1, 1024, 0, s>>>(v, n, add, num, out);
+    DGTM_CUDA_TRY(cudaGetLastError());
+    return DGTM_OK;
+}
+
+__global__ void __launch_bounds__(1024) sum_pairs_kernel(const double *__restrict__ part,
+                                                        int nb, double *out)
+{
+    __shared__ double red[32];
+    const int per = (nb + blockDim.x - 1) / blockDim.x;
+    const int b = threadIdx.x * per, e = min(nb, b + per);
+    double s0 = 0.0, s1 = 0.0;
+    for (int i = b; i < e; i++) {
+        s0 += part[2 * i];
+        s1 += part[2 * i + 1];
+    }
+    s0 = block_sum_fixed(s0, red);
+    s1 = block_sum_fixed(s1, red);
+    if (threadIdx.x == 0) {
+        out[0] = s0;
+        out[1] = s1;
+    }
+}
+
+int launch_sum_pairs(const double *part, int nblocks, double *out, cudaStream_t s)
+{
+    sum_pairs_kernel<<<1, 1024, 0, s>>>(part, nblocks, out);
+    DGTM_CUDA_TRY(cudaGetLastError());
+    return DGTM_OK;
+}
+
+__global__ void to_f32_kernel(const double *__restrict__ src, size_t n, float *__restrict__ dst)
+{
+    for (size_t i = blockIdx.x * (size_t) blockDim.x + threadIdx.x; i < n;
+         i += (size_t) gridDim.x * blockDim.x)
+        dst[i] = (float) src[i];
+}
+
+int launch_to_f32(const double *src, size_t n, float *dst, cudaStream_t s)
+{
+    size_t blocks = (n + 255) / 256;
+    if (blocks > 8192)
+        blocks = 8192;
+    if (blocks == 0)
+        return DGTM_OK;
+    to_f32_kernel<<<(unsigned) blocks, 256, 0, s>>>(src, n, dst);
+    DGTM_CUDA_TRY(cudaGetLastError());
+    return DGTM_OK;
+}
+
+}  // namespace dgtm

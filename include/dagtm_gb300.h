@@ -1,0 +1,155 @@
+/*
+ * dagtm_gb300.h -- C ABI of the GB300 (sm_103a) DA-GTM annealed EM step.
+ *
+ * One opaque context owns every device buffer of one GTM problem
+ * (N data points T in D dimensions, K latent points, M1 = M + 1 basis
+ * functions FI).  The data T stays resident on the GPU; the K x N distance
+ * and responsibility matrices of the reference are never stored: the E-step
+ * keeps two numbers per data point (the column log-sum-exp statistics) and
+ * the M-step recomputes responsibilities tile by tile.
+ *
+ * Host arrays are row-major doubles with an explicit leading dimension
+ * (GSL's tda is accepted as is) and are only borrowed for the call.
+ * Every entry point is synchronous at the ABI edge, returns 0 on success or
+ * one of the DGTM_E* codes, and never aborts; dgtm_last_error_string()
+ * describes the last failure of the calling thread.  A context is used by
+ * one host thread at a time; it runs on the CUDA device that was current
+ * when it was created, on a stream of its own.
+ *
+ * Citations name the reference routine each entry point replaces
+ * (jychoi-hpc/da-gtm, paths relative to the checkout).
+ */
+#ifndef DAGTM_GB300_H
+#define DAGTM_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct dgtm_ctx dgtm_ctx;
+
+/* precision forms */
+#define DGTM_FP64 0   /* plain FP64, as the reference computes               */
+#define DGTM_FP32 1   /* FP32 arithmetic, FP64 reductions and M-step         */
+#define DGTM_BF16X3 2 /* tensor-core split-BF16 distances, FP64 reductions  */
+
+/* M-step solvers */
+#define DGTM_SOLVE_CHOLESKY 0 /* FP64 Cholesky (default)                          */
+#define DGTM_SOLVE_SVD 1      /* symmetric-eigen SVD, exactly-zero values dropped  */
+
+/* status codes */
+#define DGTM_OK 0
+#define DGTM_EINVAL 1     /* bad argument or shape                              */
+#define DGTM_ECUDA 2      /* CUDA runtime error                                 */
+#define DGTM_ENOTSPD 3    /* A = FI^T diag(G) FI not positive definite         */
+#define DGTM_ENONFINITE 4 /* a non-finite value where a finite one is required  */
+#define DGTM_ETIMEOUT 5   /* a device-side wait gave up (kernel returned early) */
+#define DGTM_ENOMEM 6     /* device allocation failed                           */
+#define DGTM_ESTATE 7     /* call out of order (e.g. M-step before any E-step)  */
+#define DGTM_ENOTSUP 8    /* form or size not supported on this device          */
+
+/* Version of this ABI (major * 10000 + minor * 100 + patch). */
+int dgtm_version(void);
+
+/* Description of the calling thread's last error ("" if none). */
+const char *dgtm_last_error_string(void);
+
+/*
+ * Create a context: uploads T (N x D, leading dimension ldT) and FI
+ * (K x M1, leading dimension ldFI) to the current device.  precision is one
+ * of DGTM_FP64, DGTM_FP32, DGTM_BF16X3.
+ * Replaces the set-up of dagtm/dagtm.cxx:1031-1101 (allocation of the Kbar x
+ * Nbar D and R blocks, hyperslab read of T) for a single process.
+ */
+int dgtm_ctx_create(int N, int D, int K, int M1, const double *T, int ldT,
+                    const double *FI, int ldFI, int precision, dgtm_ctx **out);
+
+/* Free every device buffer of the context (NULL is accepted). */
+int dgtm_ctx_destroy(dgtm_ctx *ctx);
+
+/* Choose the M-step solver (DGTM_SOLVE_*); Cholesky is the default.
+ * The reference solves with a GSL SVD: comm/comm.c:1299-1348 (dagtm_solve2). */
+int dgtm_set_solver(dgtm_ctx *ctx, int solver);
+
+/* Load the centres Y (K x D).  Replaces the distance pass that follows a
+ * fresh set-up or a restart: dagtm/dagtm.cxx:1143,1232 (Y = FI W; dagtm_dist). */
+int dgtm_set_Y(dgtm_ctx *ctx, const double *Y, int ldY);
+
+/* Copy the current centres Y (K x D) and the last solved W (M1 x D) to the
+ * host; either pointer may be NULL. */
+int dgtm_get_Y(dgtm_ctx *ctx, double *Y, int ldY);
+int dgtm_get_W(dgtm_ctx *ctx, double *W, int ldW);
+
+/*
+ * E-step at (beta, temp): responsibilities R_kn ∝ exp(-beta d_kn/2)^(1/temp)
+ * normalised over k, without storing R.  Returns the two qualities of the
+ * reference: *llh (log-likelihood, normalised by N) and *nfree (the
+ * annealed quality, temp * sum_n log sum_k exp(-beta d/2)^(1/temp), same
+ * normalisation; = -llh when isDA == 0).  Zero columns (every exp()
+ * underflowing) follow the reference's fallback: R column = 1/K, llh term
+ * log 0 = -inf, nfree term log K.
+ * Replaces comm/mpicomm.c:316-414 (dagtm_mpi_resp) and the two
+ * comm/mpicomm.c:463-500 (dagtm_mpi_qual) calls of dagtm/dagtm.cxx:1541-1563.
+ */
+int dgtm_estep(dgtm_ctx *ctx, double beta, int isDA, double temp, double *llh,
+               double *nfree);
+
+/*
+ * M-step on the responsibilities of the last E-step:
+ *   G = rowsum R, RT = R T, A = FI^T diag(G) FI, B = FI^T RT, A W = B,
+ *   Y = FI W, beta = N D / sum_kn R_kn |y_k - t_n|^2  (with the new Y).
+ * W (M1 x D) and Y (K x D) are copied out when non-NULL; *beta receives the
+ * new beta.  The context keeps the new Y for the next E-step.
+ * Replaces the inline M-step dagtm/dagtm.cxx:1715-1770 (with dagtm_solve2,
+ * comm/comm.c:1299-1348) and comm/mpicomm.c:276-302 (dagtm_mpi_beta).
+ */
+int dgtm_mstep(dgtm_ctx *ctx, double *W, int ldW, double *Y, int ldY,
+               double *beta);
+
+/*
+ * Row sums G (K) and the raw statistics RT = R T (K x D) of the last E-step's
+ * responsibilities, as computed inside dgtm_mstep (for checking and for the
+ * gradient of the free energy).  Either pointer may be NULL.
+ */
+int dgtm_get_stats(dgtm_ctx *ctx, double *G, double *RT, int ldRT);
+
+/*
+ * Posterior-mean projection M = R^T X (N x L) with the responsibilities of
+ * the last E-step.  X is K x L (leading dimension L).
+ * Replaces dagtm/dagtm.cxx:2348-2355 (MAP before the output is written) and
+ * the -I interpolation pass of dagtm/dagtm.cxx:1247-1295.
+ */
+int dgtm_map(dgtm_ctx *ctx, const double *X, int L, double *M, int ldM);
+
+/*
+ * Responsibilities of the last E-step for the block k0..k0+nk-1 x
+ * n0..n0+nn-1, written to R (nk x nn, leading dimension ldR).
+ * Replaces the -R dump of dagtm/dagtm.cxx:2406-2414 (h5save_byblock of R).
+ */
+int dgtm_get_R_block(dgtm_ctx *ctx, int k0, int nk, int n0, int nn, double *R,
+                     int ldR);
+
+/*
+ * Per-phase device timers, the counterpart of the reference's LOG_TICTOC
+ * phase counters (comm/log.h:35-75, printed by logfullWithPID at
+ * dagtm/dagtm.cxx:2286).  When enabled, CUDA events bracket each phase on the
+ * context's stream; times (ms), kernel launches and phase calls accumulate
+ * until dgtm_reset_timing.  Phases:
+ */
+#define DGTM_PHASE_ESTEP 0        /* distance + column log-sum-exp kernel      */
+#define DGTM_PHASE_ESTEP_REDUCE 1 /* quality reductions                        */
+#define DGTM_PHASE_MSTEP_PASS 2   /* responsibility pass: G, RT                */
+#define DGTM_PHASE_MSTEP_SOLVE 3  /* slice sums, A, B, solve, Y, beta, Y split */
+#define DGTM_NPHASES 4
+int dgtm_set_timing(dgtm_ctx *ctx, int on);
+int dgtm_reset_timing(dgtm_ctx *ctx);
+int dgtm_get_timing(dgtm_ctx *ctx, double *ms, long long *launches, long long *calls);
+
+/* The CUDA stream (cudaStream_t) the context launches on, for callers that
+ * order their own work or events against it. */
+int dgtm_get_stream(dgtm_ctx *ctx, void **stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DAGTM_GB300_H */

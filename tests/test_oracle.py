@@ -1,0 +1,157 @@
+"""The CPU oracle, pinned against the reference's own sample output.
+
+``data/Oil.out.h5`` of the reference holds a DA-GTM state written by the
+reference itself (K = 125, M = 8, N = 1000, D = 12).  From its (Y, T, beta)
+the oracle's distance + responsibility code must reproduce the stored R, the
+MAP positions M = R^T X, FI and X from the set-up code, and Y = FI W.
+"""
+import numpy as np
+import pytest
+
+
+def test_golden_input_matches_output_T(golden):
+    # the reference read T as float32 and converted to double
+    assert np.array_equal(golden["T_in"].astype(np.float64), golden["T"])
+    assert np.array_equal(golden["lb_in"], golden["lb"])
+
+
+def test_setup_grid_and_basis(orc, golden):
+    X, FI = orc.stp(3, 125, 8, 2.0)
+    assert np.array_equal(X, golden["X"])
+    assert np.array_equal(FI, golden["FI"])
+
+
+def test_y_equals_fi_w(orc, golden):
+    Y = orc.fiw(golden["FI"], golden["W"])
+    assert np.max(np.abs(Y - golden["Y"])) <= 1e-13
+
+
+def test_resp_reproduces_reference_R(orc, golden):
+    Dm = orc.dist(golden["Y"], golden["T"])
+    R, vgc, vgc2 = orc.resp(Dm, golden["beta"][0], 1, 1.0)
+    cols = golden["R_cols"]
+    assert np.max(np.abs(R[:, cols] - golden["R_sub"])) <= 1e-14
+    assert np.max(np.abs(R.sum(0) - golden["R_colsum"])) <= 1e-13
+    assert np.max(np.abs(R.sum(1) - golden["R_rowsum"])) <= 1e-12
+    # at temp = 1 both column sums coincide
+    assert np.array_equal(vgc, vgc2)
+
+
+def test_map_reproduces_reference_M(orc, golden):
+    Dm = orc.dist(golden["Y"], golden["T"])
+    R, _, _ = orc.resp(Dm, golden["beta"][0], 1, 1.0)
+    M = R.T @ golden["X"]
+    assert np.max(np.abs(M - golden["M"])) <= 1e-14
+
+
+def test_dist_formula(orc):
+    rng = np.random.default_rng(3)
+    Y = rng.standard_normal((7, 5))
+    T = rng.standard_normal((11, 5))
+    Dm = orc.dist(Y, T)
+    ref = ((Y[:, None, :] - T[None, :, :]) ** 2).sum(-1)
+    assert np.allclose(Dm, ref, rtol=1e-13, atol=1e-13)
+
+
+def test_resp_tempered_and_zero_column(orc):
+    rng = np.random.default_rng(4)
+    K, N = 6, 9
+    Dm = rng.random((K, N)) * 3
+    Dm[:, 4] = 2000.0  # every exp(-beta d / 2) underflows in this column
+    beta, temp = 2.0, 3.0
+    R, vgc, vgc2 = orc.resp(Dm, beta, 1, temp)
+    E = np.exp(-beta / 2 * Dm) ** (1 / temp)
+    ref = E / E.sum(0)
+    ref[:, 4] = 1.0 / K
+    assert np.allclose(R, ref, rtol=1e-14, atol=0)
+    assert vgc[4] == 0.0 and vgc2[4] == K
+    # DA: llh gets log 0 = -inf; nfree gets log K for that column
+    llh = orc.qual(N, K, 3, beta, vgc, 0, temp)
+    nfree = orc.qual(N, K, 3, beta, vgc2, 1, temp)
+    assert llh == -np.inf and np.isfinite(nfree)
+    # non-DA: the fallback writes K into vgc itself
+    R2, vgc_b, _ = orc.resp(Dm, beta, 0, 1.0)
+    assert vgc_b[4] == K and np.allclose(R2[:, 4], 1.0 / K)
+
+
+def test_qual_formula(orc):
+    rng = np.random.default_rng(5)
+    v = rng.random(17) + 0.1
+    N, K, D, beta, temp = 17, 9, 4, 1.7, 2.5
+    q = orc.qual(N, K, D, beta, v, 1, temp)
+    ref = (N * ((D / 2.0) * np.log(beta / (2 * np.pi)) - np.log(K)) + temp * np.log(v).sum()) / N
+    assert q == pytest.approx(ref, rel=1e-14)
+
+
+def test_solvers_agree_on_well_conditioned_system(orc):
+    rng = np.random.default_rng(6)
+    Q = rng.standard_normal((12, 12))
+    A = Q @ Q.T + 12 * np.eye(12)
+    B = rng.standard_normal((12, 5))
+    ref = np.linalg.solve(A, B)
+    assert np.allclose(orc.solve2(A, B), ref, rtol=1e-12, atol=1e-12)
+    assert np.allclose(orc.solve_chol(A, B), ref, rtol=1e-12, atol=1e-12)
+
+
+def test_svd_solve_drops_exact_zero_singular_values(orc):
+    # rank-1 matrix: the pseudo-inverse solution, not a failure
+    v = np.array([1.0, 2.0, 0.0])
+    A = np.outer(v, v)
+    b = np.array([[1.0], [2.0], [0.0]])
+    x = orc.solve2(A, b)
+    assert np.allclose(A @ x, b, atol=1e-12)
+    with pytest.raises(np.linalg.LinAlgError):
+        orc.solve_chol(A, b)
+
+
+def test_mt19937_matches_published_stream(orc):
+    # first outputs of MT19937 with the 2002 seeding, seed 5489
+    u = orc.mt_uniform(5489, 3)
+    assert np.array_equal(np.round(u * 4294967296.0).astype(np.uint64),
+                          np.array([3499211612, 581869302, 3890346734], dtype=np.uint64))
+    # seed 0 is replaced by 4357 (gsl_rng_set)
+    assert np.array_equal(orc.mt_uniform(0, 4), orc.mt_uniform(4357, 4))
+
+
+def test_ctemp_and_eig(orc, golden):
+    T = golden["T"]
+    C = T - T.mean(0)
+    lam = np.linalg.eigvalsh(C.T @ C)
+    assert np.allclose(np.sort(orc.eig_sym(C.T @ C)), lam, rtol=1e-12, atol=1e-10)
+    ref = lam.max() / T.shape[0] * (T.size / (C * C).sum())
+    assert orc.ctemp(T) == pytest.approx(ref, rel=1e-12)
+
+
+def test_mstep_stats_against_numpy(orc, golden):
+    Dm = orc.dist(golden["Y"], golden["T"])
+    R, _, _ = orc.resp(Dm, golden["beta"][0], 1, 1.0)
+    FI, T = golden["FI"], golden["T"]
+    G, A, B = orc.mstep_stats(R, FI, T)
+    assert np.allclose(G, R.sum(1), rtol=1e-13)
+    assert np.allclose(A, FI.T @ np.diag(G) @ FI, rtol=1e-12)
+    assert np.allclose(B, FI.T @ R @ T, rtol=1e-12)
+
+
+def test_beta_update_matches_closed_form(orc, golden):
+    Dm = orc.dist(golden["Y"], golden["T"])
+    R, _, _ = orc.resp(Dm, golden["beta"][0], 1, 1.0)
+    Y2 = golden["Y"] + 0.01
+    b, RD, D2 = orc.beta_update(Y2, golden["T"], R)
+    T = golden["T"]
+    G, RT = R.sum(1), R @ T
+    den = (G * (Y2 * Y2).sum(1)).sum() - 2 * (Y2 * RT).sum() + (T * T).sum()
+    assert b == pytest.approx(T.size / den, rel=1e-11)
+    assert np.allclose(RD, R * D2)
+
+
+def test_run_loop_reference_order(orc, golden):
+    # a short annealing run from the golden state: the trace is well formed and
+    # the free energy at temp = 1 equals the log-likelihood
+    T, FI = golden["T"], golden["FI"]
+    out = orc.run(T, FI, golden["Y"], golden["beta"][0], 1.5, isDA=1, alpha=0.9, eps=1e-6,
+                  maxloop=12)
+    assert out["n"] == 12
+    tr = out["temp_trace"]
+    assert tr[0] == 1.5 and np.all(np.diff(tr) <= 0)
+    last = tr == 1.0
+    assert np.allclose(out["nfree_trace"][last], out["llh_trace"][last], rtol=1e-13)
