@@ -34,7 +34,7 @@ ERRORS = {1: "EINVAL", 2: "ECUDA", 3: "ENOTSPD", 4: "ENONFINITE", 5: "ETIMEOUT",
 ABI_SYMBOLS = ("dgtm_version", "dgtm_last_error_string", "dgtm_ctx_create", "dgtm_ctx_destroy",
                "dgtm_set_solver", "dgtm_set_Y", "dgtm_get_Y", "dgtm_get_W", "dgtm_estep",
                "dgtm_mstep", "dgtm_get_stats", "dgtm_map", "dgtm_get_R_block", "dgtm_set_timing",
-               "dgtm_reset_timing", "dgtm_get_timing", "dgtm_get_stream")
+               "dgtm_reset_timing", "dgtm_get_timing", "dgtm_get_stream", "dgtm_selftest")
 PHASES = ("estep", "estep_reduce", "mstep_pass", "mstep_solve")
 
 
@@ -78,6 +78,7 @@ def load_library(path: str = LIB_PATH):
         "dgtm_get_timing": (i, [vp, _dp, ctypes.POINTER(ctypes.c_longlong),
                                 ctypes.POINTER(ctypes.c_longlong)]),
         "dgtm_get_stream": (i, [vp, pp]),
+        "dgtm_selftest": (i, [_dp, i]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -99,6 +100,13 @@ def _f64(a) -> np.ndarray:
 
 def _p(a: np.ndarray):
     return a.ctypes.data_as(_dp)
+
+
+def selftest():
+    """Largest errors of the three tensor-core operand configurations (0 = exact)."""
+    errs = (ctypes.c_double * 3)()
+    _check(load_library().dgtm_selftest(errs, 3))
+    return list(errs)
 
 
 class Context:

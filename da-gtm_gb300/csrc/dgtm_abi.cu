@@ -69,6 +69,7 @@ struct dgtm_ctx {
     int stats_valid;   // colstat belongs to the current Y
     int rt_valid;      // G / RT computed
     int w_valid;
+    int dropped;       // pivots dropped by the last Cholesky solve
     double beta, temp;
     int isDA;
 };
@@ -480,7 +481,7 @@ int dgtm_mstep(dgtm_ctx *ctx, double *W, int ldW, double *Y, int ldY, double *be
     DGTM_TRY(phase_end(ctx, DGTM_PHASE_MSTEP_SOLVE, nsmall + ny - 1));
     DGTM_CUDA_TRY(cudaMemcpyAsync(ctx->hscal, ctx->scal, 2 * sizeof(double),
                                   cudaMemcpyDeviceToHost, ctx->stream));
-    DGTM_CUDA_TRY(cudaMemcpyAsync(ctx->hflag, ctx->flag, sizeof(int), cudaMemcpyDeviceToHost,
+    DGTM_CUDA_TRY(cudaMemcpyAsync(ctx->hflag, ctx->flag, 2 * sizeof(int), cudaMemcpyDeviceToHost,
                                   ctx->stream));
     if (W)
         DGTM_CUDA_TRY(cudaMemcpy2DAsync(W, sizeof(double) * (size_t) ldW, ctx->W,
@@ -498,9 +499,10 @@ int dgtm_mstep(dgtm_ctx *ctx, double *W, int ldW, double *Y, int ldY, double *be
     ctx->stats_valid = 0;
     ctx->rt_valid = 1;
     ctx->w_valid = 1;
+    ctx->dropped = ctx->hflag[1];
     if (ctx->hflag[0] != 0) {
-        set_error(DGTM_ENOTSPD, "A = FI^T diag(G) FI is not positive definite (Cholesky)");
-        return DGTM_ENOTSPD;
+        set_error(ctx->hflag[0], "M-step solve failed: A = FI^T diag(G) FI has non-finite entries");
+        return ctx->hflag[0];
     }
     const double b = ctx->hscal[1];
     if (!isfinite(b)) {

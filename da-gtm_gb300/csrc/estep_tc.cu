@@ -1,31 +1,1005 @@
-// estep_tc.cu -- split-BF16 tensor-core form (placeholder until the tcgen05
-// kernels land): creation reports DGTM_ENOTSUP.
+// estep_tc.cu -- split-BF16 tensor-core form of the E-step and of the
+// responsibility pass of the M-step (tcgen05 + TMA + TMEM, sm_103a).
+//
+// Operands.  The distance d_kn = |y_k|^2 + |t_n|^2 - 2 y_k.t_n is never formed
+// directly: the contraction computes
+//     acc_kn = y_k.t_n - |y_k|^2 / 2 = (|t_n|^2 - d_kn) / 2
+// by appending three columns to both operands (T: 1, 1, 1; Y: the BF16
+// pieces of -|y_k|^2/2), so -beta d_kn / 2 = beta acc_kn - beta |t_n|^2 / 2
+// and the per-point term cancels inside every normalisation.  Y is split
+// into y = hi + lo (two BF16 pieces, ~16 significant bits); T is split the
+// same way unless every value is exactly representable in BF16 (0/1 data),
+// in which case the third product Y_hi T_lo vanishes and is skipped.
+// Products accumulate in FP32 in tensor memory; column statistics and every
+// cross-block reduction are FP64.  |y|^2 is taken from the split centres so
+// that acc is exact for the rounded Y, and the minimum distance of each point
+// (the term that dominates its log-sum-exp) is recomputed in FP32 from the
+// unsplit centre.
+//
+// Pass 1 (one CTA per 128 points): warp 0 streams 256-centre x 64-depth
+// BF16 panels of Y through a TMA ring, warp 1 issues tcgen05.mma
+// (M = 128 points, N = 256 centres, K = 16) into one of two TMEM
+// accumulators, warps 2-5 (one thread per point = one TMEM lane) run the
+// online log-sum-exp over k at temperature 1 and at `temp`.
+//
+// Pass 2 (persistent, units of (128 centres) x (64 x 64 points)): the CTA
+// keeps its 128 centres resident, streams 64-point T tiles, recomputes
+// acc (M = 128 centres, N = 64 points), turns it into R_kn with the pass-1
+// statistics, writes R as BF16 hi/lo back into tensor memory and multiplies
+// R by the same T tile read MN-major (M = 128, N = D padded, K = 16 points),
+// accumulating R T (and, through the column of ones, G = rowsum R) in TMEM.
+// Every unit's FP32 R T is written to its own slot; a fixed-order FP64 sum
+// over the slots gives RT and G.
 #include "common.cuh"
+#include "sm100.cuh"
 #include "tc.cuh"
+
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <math.h>
 
 namespace dgtm {
 
-struct TcState {
-    int dummy;
+int make_tmap_bf16(CUtensorMap *map, const void *ptr, uint64_t rows, uint64_t cols, uint64_t ld,
+                   uint32_t box_rows, uint32_t box_cols);
+
+using namespace sm100;
+
+namespace {
+
+constexpr int P1_THREADS = 192;       // warp 0 TMA, warp 1 MMA, warps 2-5 statistics
+constexpr int P1_BN = 128;            // points per CTA (MMA M)
+constexpr int P1_BK = 256;            // centres per chunk (MMA N)
+constexpr int PANEL_ELEMS = 64;       // BF16 elements per 128-byte swizzle row
+constexpr int P2_BK = 128;            // centres per CTA (MMA M)
+constexpr int P2_BN = 64;             // points per streamed tile
+constexpr int P2_UNIT_TILES = 64;     // tiles per output slot (4096 points)
+constexpr float LOG2E = 1.4426950408889634f;
+constexpr int SMEM_LIMIT = 227 * 1024;
+
+__host__ __device__ constexpr int round_up(int a, int b) { return (a + b - 1) / b * b; }
+
+// Byte offset of element (row r, column c) inside one 128-byte-swizzled panel.
+__device__ __forceinline__ uint32_t sw128_off(int r, int c)
+{
+    return (uint32_t) (r * 128 + ((((c >> 3) ^ (r & 7)) & 7) << 4) + ((c & 7) << 1));
+}
+
+__device__ __forceinline__ float bf16_at(const unsigned char *panel, int r, int c)
+{
+    const uint16_t v = *(const uint16_t *) (panel + sw128_off(r, c));
+    return __uint_as_float((uint32_t) v << 16);
+}
+
+struct P1Params {
+    int N, D, Dp, npanel, nT, Npad, Kpad, K, nchunk, nstage;
+    float c1l, c2l;       // beta log2(e), beta/temp log2(e)
+    double c1, c2;        // beta/2, beta/(2 temp)
+    int isDA, two_temps;  // two_temps: isDA and temp != 1
+    const float *Y32;     // K x D
+    const double *T64;    // N x D (exact data, read when T is split in two pieces)
+    double2 *colstat;     // N
+    float4 *colq;         // Npad
+    double *part;         // 2 per CTA
+    int *status;
 };
 
-int tc_create(TcState **out, int, int, int, int, const double *, const double *, cudaStream_t)
+// ---------------------------------------------------------------------------
+// pass 1
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(P1_THREADS, 1)
+    tc_pass1_kernel(const __grid_constant__ CUtensorMap tmT, const __grid_constant__ CUtensorMap tmY,
+                    const P1Params p)
+{
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char *base = (unsigned char *) (((uintptr_t) smem_raw + 1023) & ~(uintptr_t) 1023);
+    const int tpanel_bytes = P1_BN * 128;             // 16 KB
+    const int ystage_bytes = P1_BK * 128;             // 32 KB
+    unsigned char *Ts = base;                          // nT x npanel panels
+    unsigned char *Ystage = base + p.nT * p.npanel * tpanel_bytes;
+    uint64_t *bars = (uint64_t *) (Ystage + p.nstage * ystage_bytes);
+    uint64_t *y_full = bars;
+    uint64_t *y_empty = bars + p.nstage;
+    uint64_t *t_full = bars + 2 * p.nstage;
+    uint64_t *acc_full = t_full + 1;
+    uint64_t *acc_empty = acc_full + 2;
+    uint64_t *drain = acc_empty + 2;
+    uint32_t *tmem_sh = (uint32_t *) (drain + 1);
+    double *red = (double *) (tmem_sh + 2);            // 2 x 128
+    __shared__ int failed;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int n0 = blockIdx.x * P1_BN;
+
+    if (threadIdx.x == 0) {
+        failed = 0;
+        for (int s = 0; s < p.nstage; s++) {
+            mbar_init(&y_full[s], 1);
+            mbar_init(&y_empty[s], 1);
+        }
+        mbar_init(t_full, 1);
+        for (int b = 0; b < 2; b++) {
+            mbar_init(&acc_full[b], 1);
+            mbar_init(&acc_empty[b], 128);
+        }
+        mbar_init(drain, 1);
+        fence_barrier_init();
+    }
+    if (warp == 0) {
+        tmem_alloc(tmem_sh, 512);
+        tc_fence_before();
+    }
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_sh;
+    const int per_chunk = 2 * p.npanel;  // Y hi/lo x depth panels
+    const int total_loads = p.nchunk * per_chunk;
+
+    if (warp == 0 && lane == 0) {
+        // ---------------- producer ----------------
+        prefetch_tmap(&tmT);
+        prefetch_tmap(&tmY);
+        mbar_expect_tx(t_full, (uint32_t) (p.nT * p.npanel * tpanel_bytes));
+        for (int tp = 0; tp < p.nT; tp++)
+            for (int pn = 0; pn < p.npanel; pn++)
+                tma_load_2d(Ts + (tp * p.npanel + pn) * tpanel_bytes, &tmT, t_full,
+                            PANEL_ELEMS * pn, tp * p.Npad + n0);
+        for (int it = 0; it < total_loads; it++) {
+            const int s = it % p.nstage, use = it / p.nstage;
+            if (use > 0 && !mbar_wait(&y_empty[s], (use - 1) & 1, p.status, 11)) {
+                failed = 1;
+                break;
+            }
+            const int c = it / per_chunk, r = it % per_chunk;
+            const int piece = r / p.npanel, pn = r % p.npanel;
+            mbar_expect_tx(&y_full[s], (uint32_t) ystage_bytes);
+            tma_load_2d(Ystage + s * ystage_bytes, &tmY, &y_full[s], PANEL_ELEMS * pn,
+                        piece * p.Kpad + c * P1_BK);
+        }
+    } else if (warp == 1 && lane == 0) {
+        // ---------------- MMA issuer ----------------
+        const uint32_t idesc = idesc_bf16(P1_BN, P1_BK, 0, 0);
+        bool ok = mbar_wait(t_full, 0, p.status, 12);
+        int it = 0;
+        for (int c = 0; ok && c < p.nchunk; c++) {
+            const int b = c & 1, use = c >> 1;
+            if (use > 0 && !mbar_wait(&acc_empty[b], (use - 1) & 1, p.status, 13)) {
+                ok = false;
+                break;
+            }
+            tc_fence_after();
+            const uint32_t d_tmem = tmem + (uint32_t) (b * P1_BK);
+            uint32_t acc = 0;
+            for (int r = 0; r < per_chunk; r++, it++) {
+                const int s = it % p.nstage;
+                if (!mbar_wait(&y_full[s], (it / p.nstage) & 1, p.status, 14)) {
+                    ok = false;
+                    break;
+                }
+                tc_fence_after();
+                const int piece = r / p.npanel, pn = r % p.npanel;
+                const uint32_t ys = smem_u32(Ystage + s * ystage_bytes);
+                // Y_hi pairs with T_hi (and T_lo when T is split); Y_lo with T_hi
+                const int ntp = (piece == 0) ? p.nT : 1;
+                for (int kk = 0; kk < 4; kk++) {
+                    const uint64_t bd = sdesc_sw128(ys + kk * 32, 16, 1024);
+                    for (int tp = 0; tp < ntp; tp++) {
+                        const uint32_t ta =
+                            smem_u32(Ts + (tp * p.npanel + pn) * tpanel_bytes) + kk * 32;
+                        mma_ss(d_tmem, sdesc_sw128(ta, 16, 1024), bd, idesc, acc);
+                        acc = 1;
+                    }
+                }
+                mma_commit(&y_empty[s]);
+            }
+            if (!ok)
+                break;
+            mma_commit(&acc_full[b]);
+        }
+        if (!ok)
+            failed = 1;
+    } else if (warp >= 2) {
+        // ---------------- statistics (one thread per point) ----------------
+        const int q = warp & 3;
+        const int row = q * 32 + lane;
+        const uint32_t lane_base = tmem + ((uint32_t) (q * 32) << 16);
+        float m = -INFINITY;
+        int kstar = 0;
+        double s1 = 0.0, s2 = 0.0;
+        bool ok = true;
+        for (int c = 0; c < p.nchunk; c++) {
+            const int b = c & 1;
+            if (!mbar_wait(&acc_full[b], (c >> 1) & 1, p.status, 15)) {
+                ok = false;
+                break;
+            }
+            tc_fence_after();
+            for (int sub = 0; sub < 4; sub++) {
+                uint32_t va[32], vb[32];
+                const uint32_t col = (uint32_t) (b * P1_BK + sub * 64);
+                tmem_ld32(lane_base + col, va);
+                tmem_ld32(lane_base + col + 32, vb);
+                tmem_ld_wait();
+                float mx = -INFINITY;
+#pragma unroll
+                for (int j = 0; j < 32; j++) {
+                    mx = fmaxf(mx, __uint_as_float(va[j]));
+                    mx = fmaxf(mx, __uint_as_float(vb[j]));
+                }
+                if (mx > m) {
+                    if (m > -INFINITY) {
+                        s1 *= (double) ex2((m - mx) * p.c1l);
+                        s2 *= (double) ex2((m - mx) * p.c2l);
+                    }
+                    int j0 = 64;
+#pragma unroll
+                    for (int j = 31; j >= 0; j--) {
+                        if (__uint_as_float(vb[j]) == mx)
+                            j0 = 32 + j;
+                    }
+#pragma unroll
+                    for (int j = 31; j >= 0; j--) {
+                        if (__uint_as_float(va[j]) == mx)
+                            j0 = j;
+                    }
+                    m = mx;
+                    kstar = c * P1_BK + sub * 64 + j0;
+                }
+                float e1 = 0.f, e2 = 0.f;
+                if (p.two_temps) {
+#pragma unroll
+                    for (int j = 0; j < 32; j++) {
+                        const float xa = __uint_as_float(va[j]) - m;
+                        const float xb = __uint_as_float(vb[j]) - m;
+                        e1 += ex2(xa * p.c1l) + ex2(xb * p.c1l);
+                        e2 += ex2(xa * p.c2l) + ex2(xb * p.c2l);
+                    }
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 32; j++) {
+                        const float xa = __uint_as_float(va[j]) - m;
+                        const float xb = __uint_as_float(vb[j]) - m;
+                        e1 += ex2(xa * p.c1l) + ex2(xb * p.c1l);
+                    }
+                }
+                s1 += (double) e1;
+                s2 += (double) e2;
+            }
+            tc_fence_before();
+            mbar_arrive(&acc_empty[b]);
+        }
+        if (!p.two_temps)
+            s2 = s1;
+        // exact (FP32) distance to the best centre, from the unsplit centre and
+        // the resident data tile; then the per-point terms
+        const int n = n0 + row;
+        double t1 = 0.0, t2 = 0.0;
+        if (ok && !mbar_wait(t_full, 0, p.status, 17))
+            ok = false;
+        if (ok && n < p.N) {
+            const int k = min(kstar, p.K - 1);
+            const float *yk = p.Y32 + (size_t) k * p.D;
+            float dsum = 0.f;
+            if (p.nT == 1) {
+                // the data are exact in BF16: read them from the resident tile
+                for (int d = 0; d < p.D; d++) {
+                    const float df = yk[d] - bf16_at(Ts + (d >> 6) * tpanel_bytes, row, d & 63);
+                    dsum = fmaf(df, df, dsum);
+                }
+            } else {
+                const double *tn = p.T64 + (size_t) n * p.D;
+                for (int d = 0; d < p.D; d++) {
+                    const float df = yk[d] - (float) tn[d];
+                    dsum = fmaf(df, df, dsum);
+                }
+            }
+            const double dstar = (double) dsum;
+            const double ls1 = log(s1), ls2 = log(s2);
+            const double ls_sel = p.isDA ? ls2 : ls1;
+            const double c_sel = p.isDA ? p.c2 : p.c1;
+            t1 = -p.c1 * dstar + ls1;
+            t2 = p.isDA ? (-p.c2 * dstar + ls2) : 0.0;
+            double lsn = ls_sel;
+            float4 cq = make_float4(m, (float) (2.0 * c_sel) * LOG2E, (float) (ls_sel * 1.4426950408889634),
+                                    0.f);
+            // comm/mpicomm.c:382-389 zero-column fallback
+            if (exp(-p.c1 * dstar) == 0.0) {
+                lsn = NAN;
+                if (p.isDA) {
+                    t1 = -INFINITY;
+                    t2 = log((double) p.K);
+                } else {
+                    t1 = log((double) p.K);
+                }
+                cq = make_float4(0.f, 0.f, (float) log2((double) p.K), 0.f);
+            }
+            p.colstat[n] = make_double2(dstar, lsn);
+            p.colq[n] = cq;
+        } else if (n < p.Npad) {
+            p.colq[n] = make_float4(0.f, 0.f, INFINITY, 0.f);  // padding: R = 0
+        }
+        red[row] = t1;
+        red[128 + row] = t2;
+        if (!ok)
+            failed = 1;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0, b2 = 0.0;
+        for (int i = 0; i < 128; i++) {
+            a += red[i];
+            b2 += red[128 + i];
+        }
+        p.part[2 * blockIdx.x] = a;
+        p.part[2 * blockIdx.x + 1] = b2;
+    }
+    if (failed && warp == 1 && lane == 0) {
+        // let every issued MMA finish before the accumulator is released
+        mma_commit(drain);
+        mbar_wait(drain, 0, p.status, 16, 1 << 20);
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0)
+        tmem_dealloc(tmem, 512);
+}
+
+// ---------------------------------------------------------------------------
+// pass 2
+// ---------------------------------------------------------------------------
+struct P2Params {
+    int D, Dp, npanel, nT, Npad, Kpad, ntiles, units_per_k, nunits, nstage;
+    const float4 *colq;   // Npad
+    float *RTpart;        // nunits x 128 x Dp
+    int *status;
+};
+
+__device__ __forceinline__ void unit_range(const P2Params &p, int u, int &kt, int &t0, int &t1)
+{
+    kt = u / p.units_per_k;
+    const int uu = u % p.units_per_k;
+    t0 = uu * P2_UNIT_TILES;
+    t1 = min(p.ntiles, t0 + P2_UNIT_TILES);
+}
+
+__global__ void __launch_bounds__(P1_THREADS, 1)
+    tc_pass2_kernel(const __grid_constant__ CUtensorMap tmT, const __grid_constant__ CUtensorMap tmY,
+                    const P2Params p)
+{
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char *base = (unsigned char *) (((uintptr_t) smem_raw + 1023) & ~(uintptr_t) 1023);
+    const int ypanel_bytes = P2_BK * 128;                  // 16 KB
+    const int tpanel_bytes = P2_BN * 128;                  // 8 KB
+    const int tstage_bytes = p.nT * p.npanel * tpanel_bytes;
+    unsigned char *Ys = base;                               // 2 x npanel panels
+    unsigned char *Tst = base + 2 * p.npanel * ypanel_bytes;
+    float4 *cq = (float4 *) (Tst + p.nstage * tstage_bytes); // nstage x 64
+    uint64_t *bars = (uint64_t *) (cq + p.nstage * P2_BN);
+    uint64_t *t_full = bars;
+    uint64_t *t_empty = bars + p.nstage;
+    uint64_t *y_full = bars + 2 * p.nstage;
+    uint64_t *y_empty = y_full + 1;
+    uint64_t *s_full = y_empty + 1;   // 2
+    uint64_t *p_full = s_full + 2;    // 2
+    uint64_t *rt_full = p_full + 2;
+    uint64_t *rt_empty = rt_full + 1;
+    uint64_t *drain = rt_empty + 1;
+    uint32_t *tmem_sh = (uint32_t *) (drain + 1);
+    __shared__ int failed;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int u_begin = (int) ((long long) blockIdx.x * p.nunits / gridDim.x);
+    const int u_end = (int) ((long long) (blockIdx.x + 1) * p.nunits / gridDim.x);
+
+    if (threadIdx.x == 0) {
+        failed = 0;
+        for (int s = 0; s < p.nstage; s++) {
+            mbar_init(&t_full[s], 1);
+            mbar_init(&t_empty[s], 1);
+        }
+        mbar_init(y_full, 1);
+        mbar_init(y_empty, 1);
+        for (int b = 0; b < 2; b++) {
+            mbar_init(&s_full[b], 1);
+            mbar_init(&p_full[b], 128);
+        }
+        mbar_init(rt_full, 1);
+        mbar_init(rt_empty, 128);
+        mbar_init(drain, 1);
+        fence_barrier_init();
+    }
+    if (warp == 0) {
+        tmem_alloc(tmem_sh, 512);
+        tc_fence_before();
+    }
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_sh;
+    const uint32_t rt_tmem = tmem + 256;
+
+    if (warp == 0 && lane == 0) {
+        // ---------------- producer ----------------
+        prefetch_tmap(&tmT);
+        prefetch_tmap(&tmY);
+        int jt = 0, cur_kt = -1, yuse = 0;
+        bool ok = true;
+        for (int u = u_begin; ok && u < u_end; u++) {
+            int kt, t0, t1;
+            unit_range(p, u, kt, t0, t1);
+            if (kt != cur_kt) {
+                if (yuse > 0 && !mbar_wait(y_empty, (yuse - 1) & 1, p.status, 21)) {
+                    ok = false;
+                    break;
+                }
+                mbar_expect_tx(y_full, (uint32_t) (2 * p.npanel * ypanel_bytes));
+                for (int piece = 0; piece < 2; piece++)
+                    for (int pn = 0; pn < p.npanel; pn++)
+                        tma_load_2d(Ys + (piece * p.npanel + pn) * ypanel_bytes, &tmY, y_full,
+                                    PANEL_ELEMS * pn, piece * p.Kpad + kt * P2_BK);
+                yuse++;
+                cur_kt = kt;
+            }
+            for (int t = t0; t < t1; t++, jt++) {
+                const int s = jt % p.nstage, use = jt / p.nstage;
+                if (use > 0 && !mbar_wait(&t_empty[s], (use - 1) & 1, p.status, 22)) {
+                    ok = false;
+                    break;
+                }
+                mbar_expect_tx(&t_full[s], (uint32_t) (tstage_bytes + P2_BN * 16));
+                for (int tp = 0; tp < p.nT; tp++)
+                    for (int pn = 0; pn < p.npanel; pn++)
+                        tma_load_2d(Tst + s * tstage_bytes + (tp * p.npanel + pn) * tpanel_bytes,
+                                    &tmT, &t_full[s], PANEL_ELEMS * pn, tp * p.Npad + t * P2_BN);
+                bulk_load(cq + s * P2_BN, p.colq + (size_t) t * P2_BN, P2_BN * 16, &t_full[s]);
+            }
+        }
+        if (!ok)
+            failed = 1;
+    } else if (warp == 1 && lane == 0) {
+        // ---------------- MMA issuer ----------------
+        const uint32_t id1 = idesc_bf16(P2_BK, P2_BN, 0, 0);
+        const uint32_t id2 = idesc_bf16(P2_BK, p.Dp, 0, 1);
+        int jt = 0, cur_kt = -1, yuse = 0, nunit = 0;
+        bool ok = true;
+        for (int u = u_begin; ok && u < u_end; u++) {
+            int kt, t0, t1;
+            unit_range(p, u, kt, t0, t1);
+            if (kt != cur_kt) {
+                if (yuse > 0)
+                    mma_commit(y_empty);
+                if (!mbar_wait(y_full, yuse & 1, p.status, 23)) {
+                    ok = false;
+                    break;
+                }
+                yuse++;
+                cur_kt = kt;
+            }
+            uint32_t rt_acc = 0;
+            const int first_j = jt;
+            for (int t = t0; t <= t1 && ok; t++) {
+                if (t < t1) {
+                    // distances of tile jt
+                    const int s = jt % p.nstage, b = jt & 1;
+                    if (!mbar_wait(&t_full[s], (jt / p.nstage) & 1, p.status, 24)) {
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t d = tmem + (uint32_t) (b * P2_BN);
+                    const uint32_t tst = smem_u32(Tst + s * tstage_bytes);
+                    uint32_t acc = 0;
+                    for (int piece = 0; piece < 2; piece++) {
+                        const int ntp = (piece == 0) ? p.nT : 1;
+                        for (int pn = 0; pn < p.npanel; pn++) {
+                            const uint32_t ya = smem_u32(Ys + (piece * p.npanel + pn) * ypanel_bytes);
+                            for (int kk = 0; kk < 4; kk++) {
+                                const uint64_t ad = sdesc_sw128(ya + kk * 32, 16, 1024);
+                                for (int tp = 0; tp < ntp; tp++) {
+                                    const uint32_t tb = tst + (tp * p.npanel + pn) * tpanel_bytes + kk * 32;
+                                    mma_ss(d, ad, sdesc_sw128(tb, 16, 1024), id1, acc);
+                                    acc = 1;
+                                }
+                            }
+                        }
+                    }
+                    mma_commit(&s_full[b]);
+                }
+                if (t > t0) {
+                    // R T of the previous tile
+                    const int j = (t < t1) ? jt - 1 : jt - 1;
+                    const int s = j % p.nstage, b = j & 1;
+                    if (j == first_j && nunit > 0 &&
+                        !mbar_wait(rt_empty, (nunit - 1) & 1, p.status, 25)) {
+                        ok = false;
+                        break;
+                    }
+                    if (!mbar_wait(&p_full[b], (j >> 1) & 1, p.status, 26)) {
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t tst = smem_u32(Tst + s * tstage_bytes);
+                    for (int rp = 0; rp < 2; rp++) {
+                        const int ntp = (rp == 0) ? p.nT : 1;
+                        for (int kk = 0; kk < P2_BN / 16; kk++) {
+                            const uint32_t a = tmem + (uint32_t) (b * P2_BN + rp * 32 + kk * 8);
+                            for (int tp = 0; tp < ntp; tp++) {
+                                const uint64_t bd = sdesc_sw128(
+                                    tst + tp * p.npanel * tpanel_bytes + kk * 2048, tpanel_bytes, 1024);
+                                mma_ts(rt_tmem, a, bd, id2, rt_acc);
+                                rt_acc = 1;
+                            }
+                        }
+                    }
+                    mma_commit(&t_empty[s]);
+                }
+                if (t < t1)
+                    jt++;
+            }
+            if (!ok)
+                break;
+            mma_commit(rt_full);
+            nunit++;
+        }
+        if (!ok)
+            failed = 1;
+    } else if (warp >= 2) {
+        // ---------------- responsibilities and the R T drain ----------------
+        const int q = warp & 3;
+        const int row = q * 32 + lane;  // centre within the tile
+        const uint32_t lane_base = tmem + ((uint32_t) (q * 32) << 16);
+        int jt = 0, nunit = 0;
+        bool ok = true;
+        for (int u = u_begin; ok && u < u_end; u++) {
+            int kt, t0, t1;
+            unit_range(p, u, kt, t0, t1);
+            for (int t = t0; t < t1; t++, jt++) {
+                const int s = jt % p.nstage, b = jt & 1;
+                if (!mbar_wait(&t_full[s], (jt / p.nstage) & 1, p.status, 27) ||
+                    !mbar_wait(&s_full[b], (jt >> 1) & 1, p.status, 28)) {
+                    ok = false;
+                    break;
+                }
+                tc_fence_after();
+                uint32_t va[32], vb[32];
+                tmem_ld32(lane_base + (uint32_t) (b * P2_BN), va);
+                tmem_ld32(lane_base + (uint32_t) (b * P2_BN + 32), vb);
+                tmem_ld_wait();
+                const float4 *cqs = cq + s * P2_BN;
+                uint32_t hi[32], lo[32];
+#pragma unroll
+                for (int j = 0; j < 16; j++) {
+                    float r[4];
+#pragma unroll
+                    for (int e = 0; e < 4; e++) {
+                        const int n = 4 * j + e;  // point within the tile
+                        const float a = (n < 32) ? __uint_as_float(va[n]) : __uint_as_float(vb[n - 32]);
+                        const float4 c = cqs[n];
+                        r[e] = ex2(fmaf(a - c.x, c.y, -c.z));
+                    }
+#pragma unroll
+                    for (int e = 0; e < 4; e += 2) {
+                        const uint32_t h = pack_bf16(r[e], r[e + 1]);
+                        const float rl0 = r[e] - bf16lo_to_f32(h);
+                        const float rl1 = r[e + 1] - bf16hi_to_f32(h);
+                        hi[2 * j + e / 2] = h;
+                        lo[2 * j + e / 2] = pack_bf16(rl0, rl1);
+                    }
+                }
+                // R_hi over the first half of the buffer, R_lo over the second
+                uint32_t h16[16], l16[16];
+#pragma unroll
+                for (int i = 0; i < 16; i++) {
+                    h16[i] = hi[i];
+                    l16[i] = lo[i];
+                }
+                tmem_st16(lane_base + (uint32_t) (b * P2_BN), h16);
+                tmem_st16(lane_base + (uint32_t) (b * P2_BN + 32), l16);
+#pragma unroll
+                for (int i = 0; i < 16; i++) {
+                    h16[i] = hi[16 + i];
+                    l16[i] = lo[16 + i];
+                }
+                tmem_st16(lane_base + (uint32_t) (b * P2_BN + 16), h16);
+                tmem_st16(lane_base + (uint32_t) (b * P2_BN + 48), l16);
+                tmem_st_wait();
+                tc_fence_before();
+                mbar_arrive(&p_full[b]);
+            }
+            if (!ok)
+                break;
+            // drain this unit's R T (FP32) to its slot
+            if (!mbar_wait(rt_full, nunit & 1, p.status, 29)) {
+                ok = false;
+                break;
+            }
+            tc_fence_after();
+            float *dst = p.RTpart + ((size_t) u * P2_BK + row) * p.Dp;
+            for (int c0 = 0; c0 < p.Dp; c0 += 32) {
+                uint32_t v[32];
+                tmem_ld32(lane_base + 256 + (uint32_t) c0, v);
+                tmem_ld_wait();
+#pragma unroll
+                for (int j = 0; j < 32; j += 4)
+                    *(float4 *) (dst + c0 + j) = make_float4(__uint_as_float(v[j]), __uint_as_float(v[j + 1]),
+                                                             __uint_as_float(v[j + 2]), __uint_as_float(v[j + 3]));
+            }
+            tc_fence_before();
+            mbar_arrive(rt_empty);
+            nunit++;
+        }
+        if (!ok)
+            failed = 1;
+    }
+    __syncthreads();
+    if (failed && warp == 1 && lane == 0) {
+        mma_commit(drain);
+        mbar_wait(drain, 0, p.status, 30, 1 << 20);
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0)
+        tmem_dealloc(tmem, 512);
+}
+
+// ---------------------------------------------------------------------------
+// operand preparation and the slot reduction
+// ---------------------------------------------------------------------------
+__global__ void t_exact_kernel(const double *__restrict__ T64, size_t n, int *inexact)
+{
+    for (size_t i = blockIdx.x * (size_t) blockDim.x + threadIdx.x; i < n;
+         i += (size_t) gridDim.x * blockDim.x) {
+        const double t = T64[i];
+        const double h = (double) __bfloat162float(__float2bfloat16_rn((float) t));
+        if (h != t)
+            atomicExch(inexact, 1);
+    }
+}
+
+// T pieces (nT x Npad x Dp): value pieces, three columns of ones, zero padding.
+__global__ void t_split_kernel(const double *__restrict__ T64, int N, int D, int Dp, int Npad,
+                               int nT, __nv_bfloat16 *__restrict__ Tb)
+{
+    const size_t total = (size_t) Npad * Dp;
+    for (size_t i = blockIdx.x * (size_t) blockDim.x + threadIdx.x; i < total;
+         i += (size_t) gridDim.x * blockDim.x) {
+        const int n = (int) (i / Dp), d = (int) (i % Dp);
+        float hi = 0.f, lo = 0.f;
+        if (n < N) {
+            if (d < D) {
+                const double t = T64[(size_t) n * D + d];
+                const __nv_bfloat16 h = __float2bfloat16_rn((float) t);
+                hi = __bfloat162float(h);
+                lo = (float) (t - (double) hi);
+            } else if (d < D + 3) {
+                hi = 1.f;
+            }
+        }
+        Tb[i] = __float2bfloat16_rn(hi);
+        if (nT == 2)
+            Tb[total + i] = __float2bfloat16_rn(lo);
+    }
+}
+
+// Y pieces (2 x Kpad x Dp) with the folded -|y_hat|^2/2 column, and Y in FP32.
+// One warp per centre row.
+__global__ void y_split_kernel(const double *__restrict__ Y64, int K, int D, int Dp, int Kpad,
+                               __nv_bfloat16 *__restrict__ Yb, float *__restrict__ Y32)
+{
+    const int lane = threadIdx.x & 31;
+    const int wpb = blockDim.x >> 5;
+    const size_t plane = (size_t) Kpad * Dp;
+    for (int k = blockIdx.x * wpb + (threadIdx.x >> 5); k < Kpad; k += gridDim.x * wpb) {
+        __nv_bfloat16 *hi = Yb + (size_t) k * Dp;
+        __nv_bfloat16 *lo = hi + plane;
+        if (k >= K) {
+            for (int d = lane; d < Dp; d += 32) {
+                hi[d] = __float2bfloat16_rn(d == D ? -1.0e30f : 0.f);
+                lo[d] = __float2bfloat16_rn(0.f);
+            }
+            continue;
+        }
+        double q = 0.0;
+        for (int d = lane; d < D; d += 32) {
+            const double y = Y64[(size_t) k * D + d];
+            const __nv_bfloat16 h = __float2bfloat16_rn((float) y);
+            const double hd = (double) __bfloat162float(h);
+            const __nv_bfloat16 l = __float2bfloat16_rn((float) (y - hd));
+            const double yh = hd + (double) __bfloat162float(l);
+            hi[d] = h;
+            lo[d] = l;
+            Y32[(size_t) k * D + d] = (float) y;
+            q += yh * yh;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            q += __shfl_xor_sync(0xffffffffu, q, o);
+        // -q/2 in three BF16 pieces (24+ significant bits)
+        const double v = -0.5 * q;
+        const __nv_bfloat16 p1 = __float2bfloat16_rn((float) v);
+        const double r1 = v - (double) __bfloat162float(p1);
+        const __nv_bfloat16 p2 = __float2bfloat16_rn((float) r1);
+        const double r2 = r1 - (double) __bfloat162float(p2);
+        const __nv_bfloat16 p3 = __float2bfloat16_rn((float) r2);
+        for (int d = D + lane; d < Dp; d += 32) {
+            const int a = d - D;
+            hi[d] = (a == 0) ? p1 : (a == 1) ? p2 : (a == 2) ? p3 : __float2bfloat16_rn(0.f);
+            lo[d] = __float2bfloat16_rn(0.f);
+        }
+    }
+}
+
+// RT[k][d] = sum_u RTpart[kt][u][k % 128][d]; G[k] from the column of ones.
+__global__ void slot_reduce_kernel(const float *__restrict__ RTpart, int K, int D, int Dp, int U,
+                                   double *__restrict__ G, double *__restrict__ RT)
+{
+    const size_t total = (size_t) K * (D + 1);
+    for (size_t i = blockIdx.x * (size_t) blockDim.x + threadIdx.x; i < total;
+         i += (size_t) gridDim.x * blockDim.x) {
+        const int k = (int) (i / (D + 1)), d = (int) (i % (D + 1));
+        const int kt = k / P2_BK, kl = k % P2_BK;
+        const float *src = RTpart + ((size_t) kt * U * P2_BK + kl) * Dp + d;
+        double s = 0.0;
+        for (int u = 0; u < U; u++)
+            s += (double) src[(size_t) u * P2_BK * Dp];
+        if (d < D)
+            RT[(size_t) k * D + d] = s;
+        else
+            G[k] = s;
+    }
+}
+
+}  // namespace
+
+struct TcState {
+    int N, D, K, sms;
+    int Dp, npanel, Npad, Kpad, nT;
+    int nchunk, nstage1, nstage2;
+    int ntiles2, units_per_k, nunits, grid2;
+    size_t smem1, smem2;
+    __nv_bfloat16 *Tb, *Yb;
+    float *Y32;
+    float4 *colq;
+    float *RTpart;
+    int *status, *hstatus;
+    const double *tt, *T64;
+    CUtensorMap tmT1, tmT2, tmY1, tmY2;
+};
+
+static int grid_for(size_t n, int per = 256, int cap = 8192)
+{
+    size_t b = (n + per - 1) / per;
+    if (b > (size_t) cap)
+        b = cap;
+    return b == 0 ? 1 : (int) b;
+}
+
+int tc_create(TcState **out, int N, int D, int K, int sms, const double *T64, const double *tt,
+              cudaStream_t s)
 {
     *out = nullptr;
-    set_error(DGTM_ENOTSUP, "the split-BF16 form is not built yet");
-    return DGTM_ENOTSUP;
+    int dev = 0, major = 0, minor = 0;
+    DGTM_CUDA_TRY(cudaGetDevice(&dev));
+    DGTM_CUDA_TRY(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev));
+    DGTM_CUDA_TRY(cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev));
+    if (major != 10) {
+        set_error(DGTM_ENOTSUP, "the split-BF16 form needs a Blackwell (sm_10x) GPU, found sm_%d%d",
+                  major, minor);
+        return DGTM_ENOTSUP;
+    }
+    if (D + 3 > 256) {
+        set_error(DGTM_ENOTSUP, "the split-BF16 form supports D <= 253 (D = %d)", D);
+        return DGTM_ENOTSUP;
+    }
+    TcState *st = new TcState();
+    st->N = N;
+    st->D = D;
+    st->K = K;
+    st->sms = sms;
+    st->tt = tt;
+    st->T64 = T64;
+    st->Dp = round_up(D + 3, PANEL_ELEMS);
+    st->npanel = st->Dp / PANEL_ELEMS;
+    st->Npad = round_up(N, P1_BN);
+    st->Kpad = round_up(K, P1_BK);
+    st->nchunk = st->Kpad / P1_BK;
+    int rc = DGTM_OK;
+    auto fail = [&](int code) {
+        tc_destroy(st);
+        return code;
+    };
+    cudaError_t e = cudaMalloc((void **) &st->status, sizeof(int));
+    if (e == cudaSuccess)
+        e = cudaMallocHost((void **) &st->hstatus, sizeof(int));
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(st->status, 0, sizeof(int), s);
+    if (e == cudaSuccess) {
+        t_exact_kernel<<<grid_for((size_t) N * D), 256, 0, s>>>(T64, (size_t) N * D, st->status);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(st->hstatus, st->status, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        set_error(DGTM_ECUDA, "tc_create: %s", cudaGetErrorString(e));
+        return fail(DGTM_ECUDA);
+    }
+    st->nT = (*st->hstatus) ? 2 : 1;
+
+    const size_t tpl = (size_t) st->Npad * st->Dp, ypl = (size_t) st->Kpad * st->Dp;
+    // pass 2 work units
+    st->ntiles2 = st->Npad / P2_BN;
+    st->units_per_k = (st->ntiles2 + P2_UNIT_TILES - 1) / P2_UNIT_TILES;
+    const int ktiles2 = (K + P2_BK - 1) / P2_BK;
+    st->nunits = ktiles2 * st->units_per_k;
+    st->grid2 = st->nunits < sms ? st->nunits : sms;
+
+    e = cudaMalloc((void **) &st->Tb, sizeof(__nv_bfloat16) * tpl * st->nT);
+    if (e == cudaSuccess)
+        e = cudaMalloc((void **) &st->Yb, sizeof(__nv_bfloat16) * ypl * 2);
+    if (e == cudaSuccess)
+        e = cudaMalloc((void **) &st->Y32, sizeof(float) * (size_t) K * D);
+    if (e == cudaSuccess)
+        e = cudaMalloc((void **) &st->colq, sizeof(float4) * st->Npad);
+    if (e == cudaSuccess)
+        e = cudaMalloc((void **) &st->RTpart, sizeof(float) * (size_t) st->nunits * P2_BK * st->Dp);
+    if (e != cudaSuccess) {
+        set_error(DGTM_ENOMEM, "tc_create: %s", cudaGetErrorString(e));
+        return fail(DGTM_ENOMEM);
+    }
+    t_split_kernel<<<grid_for(tpl), 256, 0, s>>>(T64, N, D, st->Dp, st->Npad, st->nT, st->Tb);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        set_error(DGTM_ECUDA, "t_split: %s", cudaGetErrorString(e));
+        return fail(DGTM_ECUDA);
+    }
+    // tensor maps: T pieces stacked by rows, Y pieces stacked by rows
+    if ((rc = make_tmap_bf16(&st->tmT1, st->Tb, (uint64_t) st->nT * st->Npad, st->Dp, st->Dp,
+                             P1_BN, PANEL_ELEMS)) != DGTM_OK ||
+        (rc = make_tmap_bf16(&st->tmT2, st->Tb, (uint64_t) st->nT * st->Npad, st->Dp, st->Dp,
+                             P2_BN, PANEL_ELEMS)) != DGTM_OK ||
+        (rc = make_tmap_bf16(&st->tmY1, st->Yb, 2 * (uint64_t) st->Kpad, st->Dp, st->Dp, P1_BK,
+                             PANEL_ELEMS)) != DGTM_OK ||
+        (rc = make_tmap_bf16(&st->tmY2, st->Yb, 2 * (uint64_t) st->Kpad, st->Dp, st->Dp, P2_BK,
+                             PANEL_ELEMS)) != DGTM_OK)
+        return fail(rc);
+    // shared memory plans
+    const size_t bar_bytes = 64 * 8 + 16 + 2 * 128 * 8;
+    const size_t t1 = (size_t) st->nT * st->npanel * P1_BN * 128;
+    int ns1 = (int) ((SMEM_LIMIT - 1024 - bar_bytes - t1) / (P1_BK * 128));
+    if (ns1 > 6)
+        ns1 = 6;
+    const size_t y2 = (size_t) 2 * st->npanel * P2_BK * 128;
+    const size_t ts2 = (size_t) st->nT * st->npanel * P2_BN * 128 + P2_BN * 16;
+    int ns2 = (int) ((SMEM_LIMIT - 1024 - bar_bytes - y2) / ts2);
+    if (ns2 > 4)
+        ns2 = 4;
+    if (ns1 < 2 || ns2 < 2) {
+        set_error(DGTM_ENOTSUP, "the split-BF16 form does not fit shared memory (D = %d)", D);
+        return fail(DGTM_ENOTSUP);
+    }
+    st->nstage1 = ns1;
+    st->nstage2 = ns2;
+    st->smem1 = 1024 + t1 + (size_t) ns1 * P1_BK * 128 + bar_bytes;
+    st->smem2 = 1024 + y2 + (size_t) ns2 * ts2 + bar_bytes;
+    e = cudaFuncSetAttribute(tc_pass1_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int) st->smem1);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(tc_pass2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int) st->smem2);
+    if (e != cudaSuccess) {
+        set_error(DGTM_ECUDA, "tc_create: %s", cudaGetErrorString(e));
+        return fail(DGTM_ECUDA);
+    }
+    *out = st;
+    return DGTM_OK;
 }
-void tc_destroy(TcState *) {}
-int tc_prepare_y(TcState *, const double *, cudaStream_t) { return DGTM_ENOTSUP; }
-int tc_estep(TcState *, const double *, double, double, int, double2 *, double *, cudaStream_t,
-             int *)
+
+void tc_destroy(TcState *st)
 {
-    return DGTM_ENOTSUP;
+    if (!st)
+        return;
+    cudaFree(st->Tb);
+    cudaFree(st->Yb);
+    cudaFree(st->Y32);
+    cudaFree(st->colq);
+    cudaFree(st->RTpart);
+    cudaFree(st->status);
+    if (st->hstatus)
+        cudaFreeHost(st->hstatus);
+    delete st;
 }
-int tc_pass1_blocks(const TcState *) { return 1; }
-int tc_mstep_pass(TcState *, const double2 *, double, cudaStream_t, int *) { return DGTM_ENOTSUP; }
-int tc_mstep_reduce(TcState *, double *, double *, cudaStream_t, int *) { return DGTM_ENOTSUP; }
-int tc_fetch_status(TcState *, cudaStream_t) { return DGTM_OK; }
-int tc_check_status(TcState *) { return DGTM_OK; }
+
+int tc_prepare_y(TcState *st, const double *Y64, cudaStream_t s)
+{
+    y_split_kernel<<<grid_for((size_t) st->Kpad * 32, 256, 4096), 256, 0, s>>>(
+        Y64, st->K, st->D, st->Dp, st->Kpad, st->Yb, st->Y32);
+    DGTM_CUDA_TRY(cudaGetLastError());
+    return DGTM_OK;
+}
+
+int tc_pass1_blocks(const TcState *st) { return st->Npad / P1_BN; }
+
+int tc_estep(TcState *st, const double *, double c1, double c2, int isDA, double2 *colstat,
+             double *part, cudaStream_t s, int *nlaunch)
+{
+    P1Params p;
+    p.N = st->N;
+    p.D = st->D;
+    p.Dp = st->Dp;
+    p.npanel = st->npanel;
+    p.nT = st->nT;
+    p.Npad = st->Npad;
+    p.Kpad = st->Kpad;
+    p.K = st->K;
+    p.nchunk = st->nchunk;
+    p.nstage = st->nstage1;
+    p.c1 = c1;
+    p.c2 = c2;
+    p.c1l = (float) (2.0 * c1 * 1.4426950408889634);
+    p.c2l = (float) (2.0 * c2 * 1.4426950408889634);
+    p.isDA = isDA;
+    p.two_temps = isDA && (c1 != c2);
+    p.Y32 = st->Y32;
+    p.T64 = st->T64;
+    p.colstat = colstat;
+    p.colq = st->colq;
+    p.part = part;
+    p.status = st->status;
+    DGTM_CUDA_TRY(cudaMemsetAsync(st->status, 0, sizeof(int), s));
+    tc_pass1_kernel<<<st->Npad / P1_BN, P1_THREADS, st->smem1, s>>>(st->tmT1, st->tmY1, p);
+    DGTM_CUDA_TRY(cudaGetLastError());
+    *nlaunch = 1;
+    return DGTM_OK;
+}
+
+int tc_mstep_pass(TcState *st, const double2 *, double, cudaStream_t s, int *nlaunch)
+{
+    P2Params p;
+    p.D = st->D;
+    p.Dp = st->Dp;
+    p.npanel = st->npanel;
+    p.nT = st->nT;
+    p.Npad = st->Npad;
+    p.Kpad = st->Kpad;
+    p.ntiles = st->ntiles2;
+    p.units_per_k = st->units_per_k;
+    p.nunits = st->nunits;
+    p.nstage = st->nstage2;
+    p.colq = st->colq;
+    p.RTpart = st->RTpart;
+    p.status = st->status;
+    tc_pass2_kernel<<<st->grid2, P1_THREADS, st->smem2, s>>>(st->tmT2, st->tmY2, p);
+    DGTM_CUDA_TRY(cudaGetLastError());
+    *nlaunch = 1;
+    return DGTM_OK;
+}
+
+int tc_mstep_reduce(TcState *st, double *G, double *RT, cudaStream_t s, int *nlaunch)
+{
+    slot_reduce_kernel<<<grid_for((size_t) st->K * (st->D + 1)), 256, 0, s>>>(
+        st->RTpart, st->K, st->D, st->Dp, st->units_per_k, G, RT);
+    DGTM_CUDA_TRY(cudaGetLastError());
+    *nlaunch = 1;
+    return DGTM_OK;
+}
+
+int tc_fetch_status(TcState *st, cudaStream_t s)
+{
+    DGTM_CUDA_TRY(cudaMemcpyAsync(st->hstatus, st->status, sizeof(int), cudaMemcpyDeviceToHost, s));
+    return DGTM_OK;
+}
+
+int tc_check_status(TcState *st)
+{
+    if (*st->hstatus != 0) {
+        set_error(DGTM_ETIMEOUT, "a tensor-core kernel gave up waiting (site %d)", *st->hstatus);
+        return DGTM_ETIMEOUT;
+    }
+    return DGTM_OK;
+}
 
 }  // namespace dgtm

@@ -2,7 +2,8 @@
 //
 //   reduce_slices : G_k = sum_s Gpart[s][k], RT = sum_s RTpart[s] (fixed order)
 //   form_ab       : A = FI^T diag(G) FI, B = FI^T RT     (dagtm/dagtm.cxx:1715-1761)
-//   solve         : A W = B, FP64 Cholesky or symmetric-eigen pseudo-inverse
+//   solve         : A W = B, FP64 Cholesky (numerically dependent pivots dropped)
+//                   or symmetric-eigen pseudo-inverse
 //                   with exactly-zero eigenvalues dropped (the semantics of
 //                   gsl_linalg_SV_solve used by dagtm_solve2, comm/comm.c:1299-1348)
 //   update_y      : Y = FI W (dagtm/dagtm.cxx:1769), |y_k|^2 and the beta terms
@@ -104,6 +105,12 @@ constexpr int SMEM_SOLVE_MAX = 110;  // M1 up to which L lives in shared memory
 
 // Left-looking Cholesky, L[i][j] = (A[i][j] - sum_{p<j} L[i][p] L[j][p]) / L[j][j],
 // then forward and back substitution, one right-hand side per thread.
+// A pivot that keeps less than CHOL_DROP of its diagonal (the column adds no
+// new direction at FP64 precision) is dropped: that unknown is fixed at 0,
+// which keeps the solve defined when A = FI^T diag(G) FI is numerically
+// singular (wide basis functions).  flag[1] counts the dropped pivots.
+constexpr double CHOL_DROP = 1e-12;
+
 __global__ void __launch_bounds__(SOLVE_THREADS) cholesky_kernel(const double *__restrict__ A,
                                                                 const double *__restrict__ B,
                                                                 int M1, int D,
@@ -113,13 +120,16 @@ __global__ void __launch_bounds__(SOLVE_THREADS) cholesky_kernel(const double *_
 {
     extern __shared__ double sh[];
     double *L = (M1 <= SMEM_SOLVE_MAX) ? sh : work;
-    __shared__ int bad;
-    if (threadIdx.x == 0)
+    __shared__ int bad, ndrop;
+    if (threadIdx.x == 0) {
         bad = 0;
+        ndrop = 0;
+    }
     for (int i = threadIdx.x; i < M1 * M1; i += blockDim.x)
         L[i] = A[i];
     __syncthreads();
     for (int j = 0; j < M1; j++) {
+        const double ajj = A[(size_t) j * M1 + j];
         for (int i = j + threadIdx.x; i < M1; i += blockDim.x) {
             double v = L[(size_t) i * M1 + j];
             for (int p = 0; p < j; p++)
@@ -129,9 +139,12 @@ __global__ void __launch_bounds__(SOLVE_THREADS) cholesky_kernel(const double *_
         __syncthreads();
         if (threadIdx.x == 0) {
             const double d = L[(size_t) j * M1 + j];
-            if (!(d > 0.0) || !isfinite(d)) {
+            if (!isfinite(d)) {
                 bad = 1;
-                L[(size_t) j * M1 + j] = 1.0;
+                L[(size_t) j * M1 + j] = 0.0;
+            } else if (!(d > CHOL_DROP * ajj)) {
+                ndrop++;
+                L[(size_t) j * M1 + j] = 0.0;  // marks a dropped unknown
             } else {
                 L[(size_t) j * M1 + j] = sqrt(d);
             }
@@ -139,26 +152,30 @@ __global__ void __launch_bounds__(SOLVE_THREADS) cholesky_kernel(const double *_
         __syncthreads();
         const double ljj = L[(size_t) j * M1 + j];
         for (int i = j + 1 + threadIdx.x; i < M1; i += blockDim.x)
-            L[(size_t) i * M1 + j] /= ljj;
+            L[(size_t) i * M1 + j] = (ljj != 0.0) ? L[(size_t) i * M1 + j] / ljj : 0.0;
         __syncthreads();
     }
+    if (threadIdx.x == 0)
+        flag[1] = ndrop;
     if (bad) {
         if (threadIdx.x == 0)
-            flag[0] = DGTM_ENOTSPD;
+            flag[0] = DGTM_ENONFINITE;
         return;
     }
     for (int c = threadIdx.x; c < D; c += blockDim.x) {
         for (int i = 0; i < M1; i++) {
+            const double lii = L[(size_t) i * M1 + i];
             double v = B[(size_t) i * D + c];
             for (int p = 0; p < i; p++)
                 v -= L[(size_t) i * M1 + p] * W[(size_t) p * D + c];
-            W[(size_t) i * D + c] = v / L[(size_t) i * M1 + i];
+            W[(size_t) i * D + c] = (lii != 0.0) ? v / lii : 0.0;
         }
         for (int i = M1 - 1; i >= 0; i--) {
+            const double lii = L[(size_t) i * M1 + i];
             double v = W[(size_t) i * D + c];
             for (int p = i + 1; p < M1; p++)
                 v -= L[(size_t) p * M1 + i] * W[(size_t) p * D + c];
-            W[(size_t) i * D + c] = v / L[(size_t) i * M1 + i];
+            W[(size_t) i * D + c] = (lii != 0.0) ? v / lii : 0.0;
         }
     }
 }
@@ -278,7 +295,7 @@ __global__ void __launch_bounds__(SOLVE_THREADS) jacobi_solve_kernel(const doubl
 int launch_solve(const double *A, const double *B, int M1, int D, int solver, double *W,
                  double *work, int *flag, cudaStream_t s)
 {
-    DGTM_CUDA_TRY(cudaMemsetAsync(flag, 0, sizeof(int), s));
+    DGTM_CUDA_TRY(cudaMemsetAsync(flag, 0, 2 * sizeof(int), s));
     if (solver == DGTM_SOLVE_SVD && M1 > 2 * SOLVE_THREADS - 2) {
         set_error(DGTM_ENOTSUP, "the eigen-SVD solver supports M1 <= %d", 2 * SOLVE_THREADS - 2);
         return DGTM_ENOTSUP;

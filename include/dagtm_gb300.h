@@ -149,6 +149,15 @@ int dgtm_get_timing(dgtm_ctx *ctx, double *ms, long long *launches, long long *c
  * order their own work or events against it. */
 int dgtm_get_stream(dgtm_ctx *ctx, void **stream);
 
+/*
+ * Diagnostic: runs the three tensor-core operand configurations the split-BF16
+ * kernels rely on (K-major x K-major from shared memory; K-major x MN-major;
+ * tensor-memory A x MN-major) on small integer matrices and writes the largest
+ * absolute error against a host product to errs[0..2] (0 when correct).
+ * No reference counterpart (the reference has no GPU code).
+ */
+int dgtm_selftest(double *errs, int nerrs);
+
 #ifdef __cplusplus
 }
 #endif

@@ -334,17 +334,26 @@ int orc_solve2(int n, int k, const double *A, const double *B, double *X)
     return 0;
 }
 
-/* Cholesky A = L L^T and two triangular solves per column (FP64). */
+/* Cholesky A = L L^T and two triangular solves per column (FP64).  A pivot
+ * keeping no more than 1e-12 of its diagonal is dropped (that unknown is 0),
+ * the same rule as the GPU solver.  Returns the number of dropped pivots, or
+ * -1 on a non-finite pivot. */
 int orc_solve_chol(int n, int k, const double *A, const double *B, double *X)
 {
     double *L = (double *) calloc((size_t) n * n, sizeof(double));
+    int ndrop = 0;
     for (int j = 0; j < n; j++) {
         double d = A[(size_t) j * n + j];
         for (int p = 0; p < j; p++)
             d -= L[(size_t) j * n + p] * L[(size_t) j * n + p];
-        if (!(d > 0.0)) {
+        if (!isfinite(d)) {
             free(L);
             return -1;
+        }
+        if (!(d > 1e-12 * A[(size_t) j * n + j])) {
+            ndrop++;
+            L[(size_t) j * n + j] = 0.0;
+            continue; /* column j below the diagonal stays 0 */
         }
         d = sqrt(d);
         L[(size_t) j * n + j] = d;
@@ -361,18 +370,20 @@ int orc_solve_chol(int n, int k, const double *A, const double *B, double *X)
             double v = B[(size_t) i * k + c];
             for (int p = 0; p < i; p++)
                 v -= L[(size_t) i * n + p] * z[p];
-            z[i] = v / L[(size_t) i * n + i];
+            double lii = L[(size_t) i * n + i];
+            z[i] = (lii != 0.0) ? v / lii : 0.0;
         }
         for (int i = n - 1; i >= 0; i--) {
             double v = z[i];
             for (int p = i + 1; p < n; p++)
                 v -= L[(size_t) p * n + i] * X[(size_t) p * k + c];
-            X[(size_t) i * k + c] = v / L[(size_t) i * n + i];
+            double lii = L[(size_t) i * n + i];
+            X[(size_t) i * k + c] = (lii != 0.0) ? v / lii : 0.0;
         }
     }
     free(z);
     free(L);
-    return 0;
+    return ndrop;
 }
 
 /* dagtm/dagtm.cxx:1769: Y = FI W (gsl_blas_dgemm NoTrans/NoTrans). */
@@ -751,7 +762,7 @@ double orc_ctemp(int N, int D, const double *T)
 static int solve_w(int solver, int M1, int D, const double *A, const double *B, double *W)
 {
     if (solver == 1)
-        return orc_solve_chol(M1, D, A, B, W);
+        return orc_solve_chol(M1, D, A, B, W) < 0 ? -1 : 0;
     return orc_solve2(M1, D, A, B, W);
 }
 

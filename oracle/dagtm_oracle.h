@@ -51,7 +51,8 @@ void orc_mstep_stats(int K, int N, int D, int M1, const double *R,
 /* comm/comm.c:1299-1348 dagtm_solve2: A X = B by SVD (n x n A, n x k B). */
 int orc_solve2(int n, int k, const double *A, const double *B, double *X);
 
-/* FP64 Cholesky solve of the same system (the GPU's default solver). */
+/* FP64 Cholesky solve of the same system (the GPU's default solver); pivots
+ * keeping <= 1e-12 of their diagonal are dropped.  Returns the number dropped. */
 int orc_solve_chol(int n, int k, const double *A, const double *B, double *X);
 
 /* Y = FI W  (dagtm/dagtm.cxx:1769) */

@@ -145,8 +145,8 @@ def solve_chol(A, B):
     A, B = _c(A), _c(B)
     n, k = B.shape
     X = np.empty((n, k))
-    if lib().orc_solve_chol(n, k, _p(A), _p(B), _p(X)) != 0:
-        raise np.linalg.LinAlgError("matrix not positive definite")
+    if lib().orc_solve_chol(n, k, _p(A), _p(B), _p(X)) < 0:
+        raise np.linalg.LinAlgError("non-finite pivot")
     return X
 
 

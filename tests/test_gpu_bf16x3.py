@@ -1,0 +1,129 @@
+"""Split-BF16 tensor-core form against the FP64 oracle, through the C ABI.
+
+The distances are formed from BF16 hi/lo pieces of Y (and of T unless T is
+exactly representable in BF16) with FP32 accumulation; column statistics,
+reductions, the solve and beta are FP64.  Stated tolerances (relative):
+qualities (free energy, log-likelihood) 1e-5, beta / G / R T / centres 1e-4,
+responsibilities 1e-4 absolute (R is in [0, 1]).
+"""
+import importlib
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    a, b = np.asarray(a, float), np.asarray(b, float)
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def sub(pkg, name):
+    return importlib.import_module(pkg.__name__ + "." + name)
+
+
+def oracle_step(orc, T, FI, Y, beta, isDA, temp):
+    Dm = orc.dist(Y, T)
+    R, vgc, vgc2 = orc.resp(Dm, beta, isDA, temp)
+    N, D = T.shape
+    K = Y.shape[0]
+    llh = orc.qual(N, K, D, beta, vgc, 0, temp)
+    nfree = orc.qual(N, K, D, beta, vgc2, 1, temp) if isDA else -llh
+    G, A, B = orc.mstep_stats(R, FI, T)
+    Yn = orc.fiw(FI, orc.solve_chol(A, B))
+    bn, _, _ = orc.beta_update(Yn, T, R)
+    return dict(R=R, llh=llh, nfree=nfree, G=G, RT=R @ T, Y=Yn, beta=bn)
+
+
+def fingerprint_problem(pkg, N, K, M, L=3, s=1.0, seed=3):
+    ds = sub(pkg, "datasets")
+    st = sub(pkg, "gtm_setup")
+    T = ds.fingerprints(N, 166, 20, seed=seed)
+    X, FI = st.setup_grid(L, K, M, s)
+    rng = np.random.default_rng(seed)
+    Y = T[rng.integers(0, N, K)] * 0.7 + 0.15 + 0.05 * rng.standard_normal((K, 166))
+    return T, X, FI, Y
+
+
+@pytest.mark.parametrize("N,K,M,temp,isDA", [
+    (2048, 512, 27, 1.6, 1),   # multiples of the tiles
+    (1000, 343, 27, 2.3, 1),   # ragged points and centres
+    (777, 125, 8, 1.0, 1),     # temp = 1: one exponential per element
+    (1500, 216, 27, 1.0, 0),   # plain EM
+])
+def test_em_step_matches_oracle(pkg, orc, N, K, M, temp, isDA):
+    T, X, FI, Y = fingerprint_problem(pkg, N, K, M)
+    beta = 4.0
+    ref = oracle_step(orc, T, FI, Y, beta, isDA, temp)
+    with pkg.Context(T, FI, "bf16x3") as c:
+        c.set_Y(Y)
+        llh, nfree = c.estep(beta, isDA, temp)
+        Rg = c.R_block(0, K, 0, min(N, 300))
+        b, W, Yn = c.mstep(want_Y=True)
+        G, RT = c.get_stats()
+    assert llh == pytest.approx(ref["llh"], rel=1e-5)
+    assert nfree == pytest.approx(ref["nfree"], rel=1e-5)
+    assert np.max(np.abs(Rg - ref["R"][:, :Rg.shape[1]])) <= 1e-4
+    assert rel(G, ref["G"]) <= 1e-4
+    assert rel(RT, ref["RT"]) <= 1e-4
+    assert rel(Yn, ref["Y"]) <= 1e-4
+    assert b == pytest.approx(ref["beta"], rel=1e-4)
+
+
+def test_non_bf16_data_uses_split_T(pkg, orc, golden):
+    # the oil data are not exact in BF16: T is split into hi/lo as well
+    T, Y, FI, beta = golden["T"], golden["Y"], golden["FI"], golden["beta"][0]
+    ref = oracle_step(orc, T, FI, Y, beta, 1, 1.3)
+    with pkg.Context(T, FI, "bf16x3") as c:
+        c.set_Y(Y)
+        llh, nfree = c.estep(beta, 1, 1.3)
+        b, W, Yn = c.mstep(want_Y=True)
+        G, RT = c.get_stats()
+    assert llh == pytest.approx(ref["llh"], rel=1e-5)
+    assert nfree == pytest.approx(ref["nfree"], rel=1e-5)
+    assert rel(G, ref["G"]) <= 1e-4
+    assert rel(RT, ref["RT"]) <= 1e-4
+    assert b == pytest.approx(ref["beta"], rel=1e-4)
+
+
+def test_zero_column_fallback_bf16x3(pkg, orc):
+    T, X, FI, Y = fingerprint_problem(pkg, 640, 216, 27)
+    T = T.copy()
+    T[5] = 40.0  # every exp(-beta d / 2) underflows for this point
+    beta, temp = 4.0, 2.0
+    ref = oracle_step(orc, T, FI, Y, beta, 1, temp)
+    with pkg.Context(T, FI, "bf16x3") as c:
+        c.set_Y(Y)
+        llh, nfree = c.estep(beta, 1, temp)
+        R = c.R_block(0, 216, 0, 16)
+    assert llh == -np.inf == ref["llh"]
+    assert nfree == pytest.approx(ref["nfree"], rel=1e-5)
+    assert np.allclose(R[:, 5], 1.0 / 216, rtol=1e-12)
+
+
+def test_trajectory_against_fp64_form(pkg):
+    T, X, FI, Y = fingerprint_problem(pkg, 4096, 512, 27, seed=9)
+    kw = dict(isDA=1, alpha=0.9, eps=1e-7, maxloop=12)
+    out = {}
+    for form in ("fp64", "bf16x3"):
+        with pkg.Context(T, FI, form) as c:
+            c.set_Y(Y)
+            out[form] = pkg.anneal(c, 2.0, 3.0, **kw)
+    a, b = out["bf16x3"], out["fp64"]
+    assert len(a.nfree_trace) == len(b.nfree_trace)
+    assert rel(a.nfree_trace, b.nfree_trace) <= 1e-4
+    assert rel(a.beta_trace, b.beta_trace) <= 1e-4
+
+
+def test_reruns_are_bit_identical_bf16x3(pkg):
+    T, X, FI, Y = fingerprint_problem(pkg, 1024, 216, 27)
+    outs = []
+    for _ in range(2):
+        with pkg.Context(T, FI, "bf16x3") as c:
+            c.set_Y(Y)
+            q = c.estep(3.0, 1, 1.7)
+            b, W, Yn = c.mstep(want_Y=True)
+            outs.append((q, b, Yn))
+    assert outs[0][0] == outs[1][0] and outs[0][1] == outs[1][1]
+    assert np.array_equal(outs[0][2], outs[1][2])

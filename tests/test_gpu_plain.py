@@ -1,10 +1,12 @@
 """Parity of the plain forms (FP64, FP32) through the C ABI against the oracle.
 
-Tolerances: FP64 form 1e-9 relative for the qualities, beta, G, RT and the
-centres Y (the reference's own precision target); W is compared through Y
-because A = FI^T diag(G) FI is ill-conditioned (cond ~ 6e9 on the oil data:
-two correct FP64 solvers differ in W at ~1e-6 relative).  FP32 form: 1e-5
-relative on the qualities, 1e-4 on beta / Y.
+Tolerances: FP64 form 1e-12 relative for the qualities, G and RT, and 1e-9
+for beta, the centres Y = FI W and the free-energy / beta traces on a
+well-conditioned basis (cond(FI^T FI) ~ 6e6).  On the reference's oil data
+A = FI^T diag(G) FI has cond ~ 6e9, so two correct FP64 solvers (and two
+summation orders of B) already differ in Y by ~cond x eps; there Y, beta and
+the traces are compared at 1e-6.  W itself is compared through Y.  FP32 form:
+1e-5 relative on the qualities, 1e-4 on beta / Y.
 """
 import numpy as np
 import pytest
@@ -55,10 +57,23 @@ def test_map_and_R_block_reproduce_reference_output(pkg, oil):
     assert np.max(np.abs(R.sum(0) - 1.0)) <= 1e-13
 
 
+def gmm_problem(pkg):
+    ds = pkg_mod(pkg, "datasets")
+    st = pkg_mod(pkg, "gtm_setup")
+    T = ds.make("gmm_n1k", seed=0)
+    X, FI, W, beta = st.random_init(T, 2, 400, 16, 1.0, seed=1)
+    return T, FI, FI @ W, beta, st.start_temp(T, 0.99)
+
+
 @pytest.mark.parametrize("solver", ["cholesky", "svd"])
-def test_mstep_fp64(pkg, orc, oil, solver):
-    T, Y, FI, beta = oil["T"], oil["Y"], oil["FI"], oil["beta"][0]
-    temp = 1.7
+@pytest.mark.parametrize("data", ["oil", "gmm"])
+def test_mstep_fp64(pkg, orc, oil, solver, data):
+    if data == "oil":
+        T, Y, FI, beta = oil["T"], oil["Y"], oil["FI"], oil["beta"][0]
+        temp, tol = 1.7, 1e-6
+    else:
+        T, FI, Y, beta, temp = gmm_problem(pkg)
+        tol = 1e-9
     R, _, _ = oracle_estep(orc, T, Y, beta, 1, temp)
     G, A, B = orc.mstep_stats(R, FI, T)
     Wo = orc.solve_chol(A, B) if solver == "cholesky" else orc.solve2(A, B)
@@ -71,9 +86,9 @@ def test_mstep_fp64(pkg, orc, oil, solver):
         Gg, RT = c.get_stats()
     assert rel(Gg, G) <= 1e-12
     assert rel(RT, R @ T) <= 1e-12
-    assert rel(Yn, Yo) <= 1e-9
-    assert rel(FI @ W, Yo) <= 1e-9
-    assert b == pytest.approx(bo, rel=1e-9)
+    assert rel(Yn, Yo) <= tol
+    assert rel(FI @ W, Yo) <= tol
+    assert b == pytest.approx(bo, rel=tol)
 
 
 def test_trajectory_matches_oracle_fp64(pkg, orc, oil):
@@ -84,28 +99,25 @@ def test_trajectory_matches_oracle_fp64(pkg, orc, oil):
         c.set_Y(oil["Y"])
         out = pkg.anneal(c, oil["beta"][0], 1.5, **kw)
         Yg = c.get_Y()
+    # oil: cond(A) ~ 6e9 (see the module docstring)
     assert len(out.nfree_trace) == ref["n"]
     assert np.array_equal(out.temp_trace, ref["temp_trace"])
-    assert rel(out.nfree_trace, ref["nfree_trace"]) <= 1e-9
-    assert rel(out.llh_trace, ref["llh_trace"]) <= 1e-9
-    assert rel(out.beta_trace, ref["beta_trace"]) <= 1e-9
-    assert out.beta == pytest.approx(ref["beta"], rel=1e-9)
-    assert rel(Yg, ref["Y"]) <= 1e-8
+    assert rel(out.nfree_trace, ref["nfree_trace"]) <= 1e-6
+    assert rel(out.llh_trace, ref["llh_trace"]) <= 1e-6
+    assert rel(out.beta_trace, ref["beta_trace"]) <= 1e-6
+    assert out.beta == pytest.approx(ref["beta"], rel=1e-6)
+    assert rel(Yg, ref["Y"]) <= 1e-6
 
 
 def test_gmm_config_trajectory_fp64(pkg, orc):
-    ds = pkg_mod(pkg, "datasets")
-    st = pkg_mod(pkg, "gtm_setup")
-    T = ds.make("gmm_n1k", seed=0)
-    X, FI, W, beta = st.random_init(T, 2, 400, 16, 1.0, seed=1)
-    Y0 = FI @ W
-    temp0 = st.start_temp(T, 0.99)
+    T, FI, Y0, beta, temp0 = gmm_problem(pkg)
     kw = dict(isDA=1, alpha=0.95, eps=1e-6, maxloop=20)
     ref = orc.run(T, FI, Y0, beta, temp0, solver=1, **kw)
     with pkg.Context(T, FI, "fp64") as c:
         c.set_Y(Y0)
         out = pkg.anneal(c, beta, temp0, **kw)
     assert rel(out.nfree_trace, ref["nfree_trace"]) <= 1e-9
+    assert rel(out.llh_trace, ref["llh_trace"]) <= 1e-9
     assert rel(out.beta_trace, ref["beta_trace"]) <= 1e-9
 
 
@@ -114,7 +126,7 @@ def pkg_mod(pkg, name):
     return importlib.import_module(pkg.__name__ + "." + name)
 
 
-@pytest.mark.parametrize("N,D,K,M1", [(517, 37, 203, 10), (64, 16, 64, 5), (1, 3, 1, 1),
+@pytest.mark.parametrize("N,D,K,M1", [(517, 37, 203, 10), (64, 16, 64, 5), (2, 3, 1, 1),
                                       (130, 256, 70, 7)])
 def test_ragged_shapes_fp64(pkg, orc, N, D, K, M1):
     rng = np.random.default_rng(N + D + K)
@@ -132,8 +144,8 @@ def test_ragged_shapes_fp64(pkg, orc, N, D, K, M1):
         assert np.max(np.abs(Rg - R)) <= 1e-13
         try:
             c.mstep()
-        except pkg.DgtmError as e:  # tiny random problems may be singular
-            assert e.code == 3
+        except pkg.DgtmError as e:  # a degenerate exact fit gives beta = inf
+            assert e.code == 4
             return
         G, RT = c.get_stats()
     assert rel(G, R.sum(1)) <= 1e-12

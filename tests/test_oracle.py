@@ -100,8 +100,9 @@ def test_svd_solve_drops_exact_zero_singular_values(orc):
     b = np.array([[1.0], [2.0], [0.0]])
     x = orc.solve2(A, b)
     assert np.allclose(A @ x, b, atol=1e-12)
-    with pytest.raises(np.linalg.LinAlgError):
-        orc.solve_chol(A, b)
+    # the Cholesky solver drops the dependent pivots instead of failing
+    xc = orc.solve_chol(A, b)
+    assert np.allclose(A @ xc, b, atol=1e-12)
 
 
 def test_mt19937_matches_published_stream(orc):
