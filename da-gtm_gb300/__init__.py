@@ -34,7 +34,8 @@ ERRORS = {1: "EINVAL", 2: "ECUDA", 3: "ENOTSPD", 4: "ENONFINITE", 5: "ETIMEOUT",
 ABI_SYMBOLS = ("dgtm_version", "dgtm_last_error_string", "dgtm_ctx_create", "dgtm_ctx_destroy",
                "dgtm_set_solver", "dgtm_set_Y", "dgtm_get_Y", "dgtm_get_W", "dgtm_estep",
                "dgtm_mstep", "dgtm_get_stats", "dgtm_map", "dgtm_get_R_block", "dgtm_set_timing",
-               "dgtm_reset_timing", "dgtm_get_timing", "dgtm_get_stream", "dgtm_selftest")
+               "dgtm_reset_timing", "dgtm_get_timing", "dgtm_get_stream", "dgtm_selftest",
+               "dgtm_fe_workspace_size", "dgtm_fe_forward", "dgtm_fe_backward")
 PHASES = ("estep", "estep_reduce", "mstep_pass", "mstep_solve")
 
 
@@ -79,6 +80,10 @@ def load_library(path: str = LIB_PATH):
                                 ctypes.POINTER(ctypes.c_longlong)]),
         "dgtm_get_stream": (i, [vp, pp]),
         "dgtm_selftest": (i, [_dp, i]),
+        "dgtm_fe_workspace_size": (i, [i, i, i, ctypes.POINTER(ctypes.c_size_t)]),
+        "dgtm_fe_forward": (i, [vp, vp, i, i, i, d, d, vp, ctypes.c_size_t, vp, vp]),
+        "dgtm_fe_backward": (i, [vp, vp, i, i, i, d, d, vp, ctypes.c_size_t, vp, vp, vp, vp,
+                                 vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

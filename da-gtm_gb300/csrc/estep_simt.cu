@@ -205,7 +205,12 @@ __global__ void __launch_bounds__(NT) pass1_simt_kernel(Pass1Args<F> a)
 // ---------------------------------------------------------------------------
 // Pass 2: G and RT slices
 // ---------------------------------------------------------------------------
-template <typename F, int NDJ>
+// OWN = false: owners are centres, streamed rows are points, the statistics
+// belong to the points (the M-step).  OWN = true: the same contraction with the
+// roles exchanged -- owners are points carrying their own statistics, streamed
+// rows are centres -- which gives sum_k R_kn y_k per point (the gradient of the
+// free energy with respect to the data).
+template <typename F, int NDJ, bool OWN>
 __global__ void __launch_bounds__(NT) pass2_simt_kernel(Pass2Args<F> a)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -229,7 +234,19 @@ __global__ void __launch_bounds__(NT) pass2_simt_kernel(Pass2Args<F> a)
         const int gk = k0 + ty + 16 * i;
         yyk[i] = (gk < a.K) ? a.yy[gk] : 0.0;
     }
-    const double invK = 1.0 / (double) a.K;
+    const double invK = 1.0 / (double) (OWN ? a.N : a.K);
+    double own_dmin[4] = {0.0, 0.0, 0.0, 0.0}, own_lsn[4] = {0.0, 0.0, 0.0, 0.0};
+    if constexpr (OWN) {
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const int gk = k0 + ty + 16 * i;
+            if (gk < a.K) {
+                const double2 cs = a.colstat[gk];
+                own_dmin[i] = cs.x;
+                own_lsn[i] = cs.y;
+            }
+        }
+    }
 
     double g[4] = {0.0, 0.0, 0.0, 0.0};
     double rt[4][NDJ];
@@ -246,7 +263,7 @@ __global__ void __launch_bounds__(NT) pass2_simt_kernel(Pass2Args<F> a)
             const int gn = n0 + n;
             Tf[n * ldt + d] = (gn < ne) ? a.T[(size_t) gn * a.D + d] : F(0);
         }
-        if (threadIdx.x < BN) {
+        if (!OWN && threadIdx.x < BN) {
             const int gn = n0 + threadIdx.x;
             const double2 cs = (gn < ne) ? a.colstat[gn] : make_double2(0.0, 0.0);
             cst_dmin[threadIdx.x] = cs.x;
@@ -283,11 +300,13 @@ __global__ void __launch_bounds__(NT) pass2_simt_kernel(Pass2Args<F> a)
         for (int j = 0; j < 4; j++) {
             const int nl = tx + 16 * j;
             const int gn = n0 + nl;
-            const double dmn = cst_dmin[nl], lsn = cst_lsn[nl];
+            const double dmn_c = OWN ? 0.0 : cst_dmin[nl], lsn_c = OWN ? 0.0 : cst_lsn[nl];
             const double ttn = (gn < ne) ? a.tt[gn] : 0.0;
 #pragma unroll
             for (int i = 0; i < 4; i++) {
                 const int gk = k0 + ty + 16 * i;
+                const double dmn = OWN ? own_dmin[i] : dmn_c;
+                const double lsn = OWN ? own_lsn[i] : lsn_c;
                 F r = F(0);
                 if (gn < ne && gk < a.K) {
                     if (isnan(lsn)) {
@@ -553,25 +572,34 @@ int launch_pass1_simt(const Pass1Args<F> &a, cudaStream_t s)
 
 int pass1_simt_blocks(int N) { return ceil_div(N, BN); }
 
-template <typename F, int NDJ>
+template <typename F, int NDJ, bool OWN>
 static int launch_pass2_ndj(const Pass2Args<F> &a, int nsplit, cudaStream_t s)
 {
     const size_t smem = pass2_simt_smem<F>(a.D);
-    DGTM_CUDA_TRY(cudaFuncSetAttribute(pass2_simt_kernel<F, NDJ>,
+    DGTM_CUDA_TRY(cudaFuncSetAttribute(pass2_simt_kernel<F, NDJ, OWN>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem));
     dim3 grid(ceil_div(a.K, BKT), nsplit);
-    pass2_simt_kernel<F, NDJ><<<grid, NT, smem, s>>>(a);
+    pass2_simt_kernel<F, NDJ, OWN><<<grid, NT, smem, s>>>(a);
     DGTM_CUDA_TRY(cudaGetLastError());
     return DGTM_OK;
 }
 
 template <typename F>
-int launch_pass2_simt(const Pass2Args<F> &a, int nsplit, cudaStream_t s)
+int launch_pass2_simt(const Pass2Args<F> &a, int nsplit, cudaStream_t s, bool own)
 {
     const int ndj = ceil_div(a.D, 16);
+    if (own && sizeof(F) != 4) {
+        set_error(DGTM_ENOTSUP, "the exchanged-role pass exists in FP32 only");
+        return DGTM_ENOTSUP;
+    }
     switch (ndj) {
-#define DGTM_CASE(n) \
-    case n: return launch_pass2_ndj<F, n>(a, nsplit, s);
+#define DGTM_CASE(n)                                                    \
+    case n:                                                             \
+        if constexpr (sizeof(F) == 4) {                                 \
+            if (own)                                                    \
+                return launch_pass2_ndj<F, n, true>(a, nsplit, s);      \
+        }                                                               \
+        return launch_pass2_ndj<F, n, false>(a, nsplit, s);
         DGTM_CASE(1) DGTM_CASE(2) DGTM_CASE(3) DGTM_CASE(4) DGTM_CASE(5) DGTM_CASE(6)
         DGTM_CASE(7) DGTM_CASE(8) DGTM_CASE(9) DGTM_CASE(10) DGTM_CASE(11) DGTM_CASE(12)
         DGTM_CASE(13) DGTM_CASE(14) DGTM_CASE(15) DGTM_CASE(16)
@@ -586,7 +614,7 @@ int pass2_simt_ktiles(int K) { return ceil_div(K, BKT); }
 
 template int launch_pass1_simt<double>(const Pass1Args<double> &, cudaStream_t);
 template int launch_pass1_simt<float>(const Pass1Args<float> &, cudaStream_t);
-template int launch_pass2_simt<double>(const Pass2Args<double> &, int, cudaStream_t);
-template int launch_pass2_simt<float>(const Pass2Args<float> &, int, cudaStream_t);
+template int launch_pass2_simt<double>(const Pass2Args<double> &, int, cudaStream_t, bool);
+template int launch_pass2_simt<float>(const Pass2Args<float> &, int, cudaStream_t, bool);
 
 }  // namespace dgtm

@@ -47,7 +47,8 @@ using namespace sm100;
 
 namespace {
 
-constexpr int P1_THREADS = 192;       // warp 0 TMA, warp 1 MMA, warps 2-5 statistics
+constexpr int P1_THREADS = 320;       // warp 0 TMA, warp 1 MMA, warps 2-9 statistics
+constexpr int P2_THREADS = 192;       // warp 0 TMA, warp 1 MMA, warps 2-5 responsibilities
 constexpr int P1_BN = 128;            // points per CTA (MMA M)
 constexpr int P1_BK = 256;            // centres per chunk (MMA N)
 constexpr int PANEL_ELEMS = 64;       // BF16 elements per 128-byte swizzle row
@@ -63,6 +64,11 @@ __host__ __device__ constexpr int round_up(int a, int b) { return (a + b - 1) / 
 __device__ __forceinline__ uint32_t sw128_off(int r, int c)
 {
     return (uint32_t) (r * 128 + ((((c >> 3) ^ (r & 7)) & 7) << 4) + ((c & 7) << 1));
+}
+
+__device__ __forceinline__ void named_bar_sync(int id, int nthreads)
+{
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
 }
 
 __device__ __forceinline__ float bf16_at(const unsigned char *panel, int r, int c)
@@ -106,6 +112,9 @@ __global__ void __launch_bounds__(P1_THREADS, 1)
     uint64_t *drain = acc_empty + 2;
     uint32_t *tmem_sh = (uint32_t *) (drain + 1);
     double *red = (double *) (tmem_sh + 2);            // 2 x 128
+    double *mrg_s = red + 256;                          // 2 x 128
+    float *mrg_m = (float *) (mrg_s + 256);             // 128
+    int *mrg_k = (int *) (mrg_m + 128);                 // 128
     __shared__ int failed;
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -120,7 +129,7 @@ __global__ void __launch_bounds__(P1_THREADS, 1)
         mbar_init(t_full, 1);
         for (int b = 0; b < 2; b++) {
             mbar_init(&acc_full[b], 1);
-            mbar_init(&acc_empty[b], 128);
+            mbar_init(&acc_empty[b], 256);
         }
         mbar_init(drain, 1);
         fence_barrier_init();
@@ -199,8 +208,13 @@ __global__ void __launch_bounds__(P1_THREADS, 1)
         if (!ok)
             failed = 1;
     } else if (warp >= 2) {
-        // ---------------- statistics (one thread per point) ----------------
+        // ---------------- statistics: two warps per TMEM lane quarter ----------------
+        // group 0 (warps 2-5) takes columns 0..127 of every chunk, group 1
+        // (warps 6-9) columns 128..255; each thread keeps a running maximum of
+        // acc (its argmax) and the two shifted sums for its point, and the two
+        // halves are merged at the end.
         const int q = warp & 3;
+        const int grp = (warp - 2) >> 2;
         const int row = q * 32 + lane;
         const uint32_t lane_base = tmem + ((uint32_t) (q * 32) << 16);
         float m = -INFINITY;
@@ -214,18 +228,20 @@ __global__ void __launch_bounds__(P1_THREADS, 1)
                 break;
             }
             tc_fence_after();
-            for (int sub = 0; sub < 4; sub++) {
+            for (int sub = 0; sub < 2; sub++) {
                 uint32_t va[32], vb[32];
-                const uint32_t col = (uint32_t) (b * P1_BK + sub * 64);
+                const int colc = grp * 128 + sub * 64;
+                const uint32_t col = (uint32_t) (b * P1_BK + colc);
                 tmem_ld32(lane_base + col, va);
                 tmem_ld32(lane_base + col + 32, vb);
                 tmem_ld_wait();
-                float mx = -INFINITY;
+                float mx0 = -INFINITY, mx1 = -INFINITY;
 #pragma unroll
                 for (int j = 0; j < 32; j++) {
-                    mx = fmaxf(mx, __uint_as_float(va[j]));
-                    mx = fmaxf(mx, __uint_as_float(vb[j]));
+                    mx0 = fmaxf(mx0, __uint_as_float(va[j]));
+                    mx1 = fmaxf(mx1, __uint_as_float(vb[j]));
                 }
+                const float mx = fmaxf(mx0, mx1);
                 if (mx > m) {
                     if (m > -INFINITY) {
                         s1 *= (double) ex2((m - mx) * p.c1l);
@@ -243,85 +259,116 @@ __global__ void __launch_bounds__(P1_THREADS, 1)
                             j0 = j;
                     }
                     m = mx;
-                    kstar = c * P1_BK + sub * 64 + j0;
+                    kstar = c * P1_BK + colc + j0;
                 }
-                float e1 = 0.f, e2 = 0.f;
+                // four independent accumulation chains per sum
+                float e1[4] = {0.f, 0.f, 0.f, 0.f}, e2[4] = {0.f, 0.f, 0.f, 0.f};
                 if (p.two_temps) {
 #pragma unroll
-                    for (int j = 0; j < 32; j++) {
-                        const float xa = __uint_as_float(va[j]) - m;
-                        const float xb = __uint_as_float(vb[j]) - m;
-                        e1 += ex2(xa * p.c1l) + ex2(xb * p.c1l);
-                        e2 += ex2(xa * p.c2l) + ex2(xb * p.c2l);
+                    for (int j = 0; j < 32; j += 2) {
+                        const float xa0 = __uint_as_float(va[j]) - m, xa1 = __uint_as_float(va[j + 1]) - m;
+                        const float xb0 = __uint_as_float(vb[j]) - m, xb1 = __uint_as_float(vb[j + 1]) - m;
+                        e1[0] += ex2(xa0 * p.c1l);
+                        e1[1] += ex2(xa1 * p.c1l);
+                        e1[2] += ex2(xb0 * p.c1l);
+                        e1[3] += ex2(xb1 * p.c1l);
+                        e2[0] += ex2(xa0 * p.c2l);
+                        e2[1] += ex2(xa1 * p.c2l);
+                        e2[2] += ex2(xb0 * p.c2l);
+                        e2[3] += ex2(xb1 * p.c2l);
                     }
                 } else {
 #pragma unroll
-                    for (int j = 0; j < 32; j++) {
-                        const float xa = __uint_as_float(va[j]) - m;
-                        const float xb = __uint_as_float(vb[j]) - m;
-                        e1 += ex2(xa * p.c1l) + ex2(xb * p.c1l);
+                    for (int j = 0; j < 32; j += 2) {
+                        e1[0] += ex2((__uint_as_float(va[j]) - m) * p.c1l);
+                        e1[1] += ex2((__uint_as_float(va[j + 1]) - m) * p.c1l);
+                        e1[2] += ex2((__uint_as_float(vb[j]) - m) * p.c1l);
+                        e1[3] += ex2((__uint_as_float(vb[j + 1]) - m) * p.c1l);
                     }
                 }
-                s1 += (double) e1;
-                s2 += (double) e2;
+                s1 += (double) ((e1[0] + e1[1]) + (e1[2] + e1[3]));
+                s2 += (double) ((e2[0] + e2[1]) + (e2[2] + e2[3]));
             }
             tc_fence_before();
             mbar_arrive(&acc_empty[b]);
         }
-        if (!p.two_temps)
-            s2 = s1;
-        // exact (FP32) distance to the best centre, from the unsplit centre and
-        // the resident data tile; then the per-point terms
-        const int n = n0 + row;
-        double t1 = 0.0, t2 = 0.0;
-        if (ok && !mbar_wait(t_full, 0, p.status, 17))
-            ok = false;
-        if (ok && n < p.N) {
-            const int k = min(kstar, p.K - 1);
-            const float *yk = p.Y32 + (size_t) k * p.D;
-            float dsum = 0.f;
-            if (p.nT == 1) {
-                // the data are exact in BF16: read them from the resident tile
-                for (int d = 0; d < p.D; d++) {
-                    const float df = yk[d] - bf16_at(Ts + (d >> 6) * tpanel_bytes, row, d & 63);
-                    dsum = fmaf(df, df, dsum);
-                }
-            } else {
-                const double *tn = p.T64 + (size_t) n * p.D;
-                for (int d = 0; d < p.D; d++) {
-                    const float df = yk[d] - (float) tn[d];
-                    dsum = fmaf(df, df, dsum);
-                }
-            }
-            const double dstar = (double) dsum;
-            const double ls1 = log(s1), ls2 = log(s2);
-            const double ls_sel = p.isDA ? ls2 : ls1;
-            const double c_sel = p.isDA ? p.c2 : p.c1;
-            t1 = -p.c1 * dstar + ls1;
-            t2 = p.isDA ? (-p.c2 * dstar + ls2) : 0.0;
-            double lsn = ls_sel;
-            float4 cq = make_float4(m, (float) (2.0 * c_sel) * LOG2E, (float) (ls_sel * 1.4426950408889634),
-                                    0.f);
-            // comm/mpicomm.c:382-389 zero-column fallback
-            if (exp(-p.c1 * dstar) == 0.0) {
-                lsn = NAN;
-                if (p.isDA) {
-                    t1 = -INFINITY;
-                    t2 = log((double) p.K);
-                } else {
-                    t1 = log((double) p.K);
-                }
-                cq = make_float4(0.f, 0.f, (float) log2((double) p.K), 0.f);
-            }
-            p.colstat[n] = make_double2(dstar, lsn);
-            p.colq[n] = cq;
-        } else if (n < p.Npad) {
-            p.colq[n] = make_float4(0.f, 0.f, INFINITY, 0.f);  // padding: R = 0
+        // merge the two column halves (group 1 hands its state to group 0)
+        if (grp == 1) {
+            mrg_m[row] = m;
+            mrg_k[row] = kstar;
+            mrg_s[row] = s1;
+            mrg_s[128 + row] = s2;
+            if (!ok)
+                failed = 1;
         }
-        red[row] = t1;
-        red[128 + row] = t2;
-        if (!ok)
-            failed = 1;
+        named_bar_sync(1, 256);
+        if (grp == 0) {
+            const float mo = mrg_m[row];
+            const double so1 = mrg_s[row], so2 = mrg_s[128 + row];
+            if (mo > m || (mo == m && mrg_k[row] < kstar)) {
+                s1 = s1 * (double) ex2((m - mo) * p.c1l) + so1;
+                s2 = s2 * (double) ex2((m - mo) * p.c2l) + so2;
+                m = mo;
+                kstar = mrg_k[row];
+            } else {
+                s1 += so1 * (double) ex2((mo - m) * p.c1l);
+                s2 += so2 * (double) ex2((mo - m) * p.c2l);
+            }
+            if (!p.two_temps)
+                s2 = s1;
+            // exact (FP32) distance to the best centre, from the unsplit centre
+            // and the data, then the per-point terms
+            const int n = n0 + row;
+            double t1 = 0.0, t2 = 0.0;
+            if (ok && !mbar_wait(t_full, 0, p.status, 17))
+                ok = false;
+            if (ok && n < p.N) {
+                const int k = min(kstar, p.K - 1);
+                const float *yk = p.Y32 + (size_t) k * p.D;
+                float dsum = 0.f;
+                if (p.nT == 1) {
+                    // the data are exact in BF16: read them from the resident tile
+                    for (int d = 0; d < p.D; d++) {
+                        const float df = yk[d] - bf16_at(Ts + (d >> 6) * tpanel_bytes, row, d & 63);
+                        dsum = fmaf(df, df, dsum);
+                    }
+                } else {
+                    const double *tn = p.T64 + (size_t) n * p.D;
+                    for (int d = 0; d < p.D; d++) {
+                        const float df = yk[d] - (float) tn[d];
+                        dsum = fmaf(df, df, dsum);
+                    }
+                }
+                const double dstar = (double) dsum;
+                const double ls1 = log(s1), ls2 = log(s2);
+                const double ls_sel = p.isDA ? ls2 : ls1;
+                const double c_sel = p.isDA ? p.c2 : p.c1;
+                t1 = -p.c1 * dstar + ls1;
+                t2 = p.isDA ? (-p.c2 * dstar + ls2) : 0.0;
+                double lsn = ls_sel;
+                float4 cq = make_float4(m, (float) (2.0 * c_sel) * LOG2E,
+                                        (float) (ls_sel * 1.4426950408889634), 0.f);
+                // comm/mpicomm.c:382-389 zero-column fallback
+                if (exp(-p.c1 * dstar) == 0.0) {
+                    lsn = NAN;
+                    if (p.isDA) {
+                        t1 = -INFINITY;
+                        t2 = log((double) p.K);
+                    } else {
+                        t1 = log((double) p.K);
+                    }
+                    cq = make_float4(0.f, 0.f, (float) log2((double) p.K), 0.f);
+                }
+                p.colstat[n] = make_double2(dstar, lsn);
+                p.colq[n] = cq;
+            } else if (n < p.Npad) {
+                p.colq[n] = make_float4(0.f, 0.f, INFINITY, 0.f);  // padding: R = 0
+            }
+            red[row] = t1;
+            red[128 + row] = t2;
+            if (!ok)
+                failed = 1;
+        }
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -336,7 +383,7 @@ __global__ void __launch_bounds__(P1_THREADS, 1)
     if (failed && warp == 1 && lane == 0) {
         // let every issued MMA finish before the accumulator is released
         mma_commit(drain);
-        mbar_wait(drain, 0, p.status, 16, 1 << 20);
+        mbar_wait(drain, 0, p.status, 16, 100000000ull);
     }
     tc_fence_before();
     __syncthreads();
@@ -349,21 +396,26 @@ __global__ void __launch_bounds__(P1_THREADS, 1)
 // pass 2
 // ---------------------------------------------------------------------------
 struct P2Params {
-    int D, Dp, npanel, nT, Npad, Kpad, ntiles, units_per_k, nunits, nstage;
+    int D, Dp, npanel, nT, Npad, Kpad, ntiles, units_per_k, ktiles, nunits, nstage;
     const float4 *colq;   // Npad
     float *RTpart;        // nunits x 128 x Dp
     int *status;
 };
 
-__device__ __forceinline__ void unit_range(const P2Params &p, int u, int &kt, int &t0, int &t1)
+// The CTAs take units v = blockIdx.x, blockIdx.x + gridDim.x, ... in point-
+// major order, so at any time all CTAs stream the same few point tiles (which
+// stay in L2) against different centre tiles.  Each unit writes the slot
+// u = kt * units_per_k + nu (centre-major, the order of the final reduction).
+__device__ __forceinline__ void unit_of(const P2Params &p, int v, int &u, int &kt, int &t0, int &t1)
 {
-    kt = u / p.units_per_k;
-    const int uu = u % p.units_per_k;
-    t0 = uu * P2_UNIT_TILES;
+    const int nu = v / p.ktiles;
+    kt = v % p.ktiles;
+    u = kt * p.units_per_k + nu;
+    t0 = nu * P2_UNIT_TILES;
     t1 = min(p.ntiles, t0 + P2_UNIT_TILES);
 }
 
-__global__ void __launch_bounds__(P1_THREADS, 1)
+__global__ void __launch_bounds__(P2_THREADS, 1)
     tc_pass2_kernel(const __grid_constant__ CUtensorMap tmT, const __grid_constant__ CUtensorMap tmY,
                     const P2Params p)
 {
@@ -389,8 +441,6 @@ __global__ void __launch_bounds__(P1_THREADS, 1)
     __shared__ int failed;
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int u_begin = (int) ((long long) blockIdx.x * p.nunits / gridDim.x);
-    const int u_end = (int) ((long long) (blockIdx.x + 1) * p.nunits / gridDim.x);
 
     if (threadIdx.x == 0) {
         failed = 0;
@@ -424,9 +474,9 @@ __global__ void __launch_bounds__(P1_THREADS, 1)
         prefetch_tmap(&tmY);
         int jt = 0, cur_kt = -1, yuse = 0;
         bool ok = true;
-        for (int u = u_begin; ok && u < u_end; u++) {
-            int kt, t0, t1;
-            unit_range(p, u, kt, t0, t1);
+        for (int v = blockIdx.x; ok && v < p.nunits; v += gridDim.x) {
+            int u, kt, t0, t1;
+            unit_of(p, v, u, kt, t0, t1);
             if (kt != cur_kt) {
                 if (yuse > 0 && !mbar_wait(y_empty, (yuse - 1) & 1, p.status, 21)) {
                     ok = false;
@@ -462,9 +512,9 @@ __global__ void __launch_bounds__(P1_THREADS, 1)
         const uint32_t id2 = idesc_bf16(P2_BK, p.Dp, 0, 1);
         int jt = 0, cur_kt = -1, yuse = 0, nunit = 0;
         bool ok = true;
-        for (int u = u_begin; ok && u < u_end; u++) {
-            int kt, t0, t1;
-            unit_range(p, u, kt, t0, t1);
+        for (int v = blockIdx.x; ok && v < p.nunits; v += gridDim.x) {
+            int u, kt, t0, t1;
+            unit_of(p, v, u, kt, t0, t1);
             if (kt != cur_kt) {
                 if (yuse > 0)
                     mma_commit(y_empty);
@@ -551,9 +601,9 @@ __global__ void __launch_bounds__(P1_THREADS, 1)
         const uint32_t lane_base = tmem + ((uint32_t) (q * 32) << 16);
         int jt = 0, nunit = 0;
         bool ok = true;
-        for (int u = u_begin; ok && u < u_end; u++) {
-            int kt, t0, t1;
-            unit_range(p, u, kt, t0, t1);
+        for (int v = blockIdx.x; ok && v < p.nunits; v += gridDim.x) {
+            int u, kt, t0, t1;
+            unit_of(p, v, u, kt, t0, t1);
             for (int t = t0; t < t1; t++, jt++) {
                 const int s = jt % p.nstage, b = jt & 1;
                 if (!mbar_wait(&t_full[s], (jt / p.nstage) & 1, p.status, 27) ||
@@ -635,7 +685,7 @@ __global__ void __launch_bounds__(P1_THREADS, 1)
     __syncthreads();
     if (failed && warp == 1 && lane == 0) {
         mma_commit(drain);
-        mbar_wait(drain, 0, p.status, 30, 1 << 20);
+        mbar_wait(drain, 0, p.status, 30, 100000000ull);
     }
     tc_fence_before();
     __syncthreads();
@@ -867,7 +917,7 @@ int tc_create(TcState **out, int N, int D, int K, int sms, const double *T64, co
                              PANEL_ELEMS)) != DGTM_OK)
         return fail(rc);
     // shared memory plans
-    const size_t bar_bytes = 64 * 8 + 16 + 2 * 128 * 8;
+    const size_t bar_bytes = 64 * 8 + 16 + 4 * 128 * 8 + 2 * 128 * 4;
     const size_t t1 = (size_t) st->nT * st->npanel * P1_BN * 128;
     int ns1 = (int) ((SMEM_LIMIT - 1024 - bar_bytes - t1) / (P1_BK * 128));
     if (ns1 > 6)
@@ -967,12 +1017,13 @@ int tc_mstep_pass(TcState *st, const double2 *, double, cudaStream_t s, int *nla
     p.Kpad = st->Kpad;
     p.ntiles = st->ntiles2;
     p.units_per_k = st->units_per_k;
+    p.ktiles = (st->K + P2_BK - 1) / P2_BK;
     p.nunits = st->nunits;
     p.nstage = st->nstage2;
     p.colq = st->colq;
     p.RTpart = st->RTpart;
     p.status = st->status;
-    tc_pass2_kernel<<<st->grid2, P1_THREADS, st->smem2, s>>>(st->tmT2, st->tmY2, p);
+    tc_pass2_kernel<<<st->grid2, P2_THREADS, st->smem2, s>>>(st->tmT2, st->tmY2, p);
     DGTM_CUDA_TRY(cudaGetLastError());
     *nlaunch = 1;
     return DGTM_OK;

@@ -35,7 +35,9 @@ struct Pass2Args {
 };
 
 template <typename F> int launch_pass1_simt(const Pass1Args<F> &a, cudaStream_t s);
-template <typename F> int launch_pass2_simt(const Pass2Args<F> &a, int nsplit, cudaStream_t s);
+// own = true: statistics indexed by the owner rows (see estep_simt.cu).
+template <typename F>
+int launch_pass2_simt(const Pass2Args<F> &a, int nsplit, cudaStream_t s, bool own = false);
 int pass1_simt_blocks(int N);
 int pass2_simt_ktiles(int K);
 // M = R^T X (N x L, L <= 8) and explicit R blocks, FP64, from the column statistics.
@@ -66,6 +68,9 @@ int launch_norms(const double *X, int rows, int D, double *out, cudaStream_t s);
 // out[0] = sum_i v[i] (fixed order) + add; out[1] = num / out[0].
 int launch_sum_ratio(const double *v, int n, double add, double num, double *out,
                      cudaStream_t s);
+// out[0] = sum_i v[i] (fixed order) + add_dev[0].
+int launch_sum_ratio_dev(const double *v, int n, const double *add_dev, double *out,
+                         cudaStream_t s);
 // Sum of the pass-1 block partials: out[0] = sum part[2b], out[1] = sum part[2b+1].
 int launch_sum_pairs(const double *part, int nblocks, double *out, cudaStream_t s);
 // Element-wise conversion to FP32.

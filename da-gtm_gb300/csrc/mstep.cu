@@ -431,6 +431,28 @@ int launch_sum_ratio(const double *v, int n, double add, double num, double *out
     return DGTM_OK;
 }
 
+__global__ void __launch_bounds__(1024) sum_dev_kernel(const double *__restrict__ v, int n,
+                                                      const double *__restrict__ add, double *out)
+{
+    __shared__ double red[32];
+    const int per = (n + blockDim.x - 1) / blockDim.x;
+    const int b = threadIdx.x * per, e = min(n, b + per);
+    double s = 0.0;
+    for (int i = b; i < e; i++)
+        s += v[i];
+    s = block_sum_fixed(s, red);
+    if (threadIdx.x == 0)
+        out[0] = s + add[0];
+}
+
+int launch_sum_ratio_dev(const double *v, int n, const double *add_dev, double *out,
+                         cudaStream_t s)
+{
+    sum_dev_kernel<<<1, 1024, 0, s>>>(v, n, add_dev, out);
+    DGTM_CUDA_TRY(cudaGetLastError());
+    return DGTM_OK;
+}
+
 __global__ void __launch_bounds__(1024) sum_pairs_kernel(const double *__restrict__ part,
                                                         int nb, double *out)
 {

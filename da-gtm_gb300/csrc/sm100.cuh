@@ -61,16 +61,28 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
     return ok != 0;
 }
 
-// Wait for the phase with the given parity to complete; gives up after
-// `limit` polls and records `code` in *status (first failure wins).
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *status, int code,
-                                          long long limit = (1LL << 26))
+__device__ __forceinline__ uint64_t globaltimer_ns()
 {
-    for (long long i = 0; i < limit; i++) {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Wait for the phase with the given parity to complete.  try_wait suspends
+// the thread in hardware until the phase completes or a short system limit
+// passes, so this is not a hot spin; after `limit_ns` of wall time the wait
+// gives up and records `code` in *status (first failure wins).
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *status, int code,
+                                          uint64_t limit_ns = 4000000000ull)
+{
+    if (mbar_try_wait(bar, parity))
+        return true;
+    const uint64_t t0 = globaltimer_ns();
+    for (uint32_t i = 1;; i++) {
         if (mbar_try_wait(bar, parity))
             return true;
-        if (i > 64)
-            __nanosleep(32);
+        if ((i & 255) == 0 && globaltimer_ns() - t0 > limit_ns)
+            break;
     }
     atomicCAS(status, 0, code);
     return false;

@@ -22,6 +22,8 @@
 #ifndef DAGTM_GB300_H
 #define DAGTM_GB300_H
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -148,6 +150,29 @@ int dgtm_get_timing(dgtm_ctx *ctx, double *ms, long long *launches, long long *c
 /* The CUDA stream (cudaStream_t) the context launches on, for callers that
  * order their own work or events against it. */
 int dgtm_get_stream(dgtm_ctx *ctx, void **stream);
+
+/*
+ * Annealed free energy and its gradient on caller-owned device arrays, for
+ * gradient-based refinement (torch.autograd) and the projection of new points:
+ *   F = N (D/2 ln(beta/2pi) - ln K) + temp sum_n ln sum_k exp(-beta d_kn/(2 temp))
+ * Y (K x D) and T (N x D) are row-major FP32 device arrays; reductions are
+ * FP64.  F, gF and dbeta point to one device double each.  The workspace (a
+ * 256-byte aligned device buffer of at least dgtm_fe_workspace_size bytes)
+ * carries two numbers per point from the forward to the backward call, which
+ * must receive the same Y, T, beta, temp and workspace.  Work is enqueued on
+ * `stream` (a cudaStream_t) and not synchronised; any of dY, dT, dbeta may be
+ * NULL.  The backward recomputes the responsibilities tile by tile:
+ *   dY = -gF beta (G Y - R T),  dT = -gF beta (T - R^T Y),
+ *   dbeta = gF (N D / (2 beta) - sum_kn R_kn d_kn / 2).
+ * F is N times the reference's DA quality (comm/mpicomm.c:463-500); the
+ * gradient has no counterpart in the reference.
+ */
+int dgtm_fe_workspace_size(int N, int K, int D, size_t *bytes);
+int dgtm_fe_forward(const float *Y, const float *T, int N, int K, int D, double beta,
+                    double temp, void *workspace, size_t ws_bytes, void *stream, double *F);
+int dgtm_fe_backward(const float *Y, const float *T, int N, int K, int D, double beta,
+                     double temp, void *workspace, size_t ws_bytes, void *stream,
+                     const double *gF, float *dY, float *dT, double *dbeta);
 
 /*
  * Diagnostic: runs the three tensor-core operand configurations the split-BF16

@@ -72,7 +72,10 @@ def test_em_step_matches_oracle(pkg, orc, N, K, M, temp, isDA):
 
 
 def test_non_bf16_data_uses_split_T(pkg, orc, golden):
-    # the oil data are not exact in BF16: T is split into hi/lo as well
+    # The oil data are not exact in BF16: T is split into hi/lo as well, which
+    # represents it to ~16 bits; with beta = 31 the per-point qualities
+    # (|llh| ~ 0.17) then carry ~3e-6 absolute error: the stated 1e-4
+    # relative bound of the split form applies here.
     T, Y, FI, beta = golden["T"], golden["Y"], golden["FI"], golden["beta"][0]
     ref = oracle_step(orc, T, FI, Y, beta, 1, 1.3)
     with pkg.Context(T, FI, "bf16x3") as c:
@@ -80,8 +83,8 @@ def test_non_bf16_data_uses_split_T(pkg, orc, golden):
         llh, nfree = c.estep(beta, 1, 1.3)
         b, W, Yn = c.mstep(want_Y=True)
         G, RT = c.get_stats()
-    assert llh == pytest.approx(ref["llh"], rel=1e-5)
-    assert nfree == pytest.approx(ref["nfree"], rel=1e-5)
+    assert llh == pytest.approx(ref["llh"], rel=1e-4)
+    assert nfree == pytest.approx(ref["nfree"], rel=1e-4)
     assert rel(G, ref["G"]) <= 1e-4
     assert rel(RT, ref["RT"]) <= 1e-4
     assert b == pytest.approx(ref["beta"], rel=1e-4)
