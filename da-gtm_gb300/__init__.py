@@ -35,7 +35,8 @@ ABI_SYMBOLS = ("dgtm_version", "dgtm_last_error_string", "dgtm_ctx_create", "dgt
                "dgtm_set_solver", "dgtm_set_Y", "dgtm_get_Y", "dgtm_get_W", "dgtm_estep",
                "dgtm_mstep", "dgtm_get_stats", "dgtm_map", "dgtm_get_R_block", "dgtm_set_timing",
                "dgtm_reset_timing", "dgtm_get_timing", "dgtm_get_stream", "dgtm_selftest",
-               "dgtm_fe_workspace_size", "dgtm_fe_forward", "dgtm_fe_backward")
+               "dgtm_fe_workspace_size", "dgtm_fe_forward", "dgtm_fe_backward",
+               "dgtm_fe_forward_noalloc")
 PHASES = ("estep", "estep_reduce", "mstep_pass", "mstep_solve")
 
 
@@ -84,6 +85,7 @@ def load_library(path: str = LIB_PATH):
         "dgtm_fe_forward": (i, [vp, vp, i, i, i, d, d, vp, ctypes.c_size_t, vp, vp]),
         "dgtm_fe_backward": (i, [vp, vp, i, i, i, d, d, vp, ctypes.c_size_t, vp, vp, vp, vp,
                                  vp]),
+        "dgtm_fe_forward_noalloc": (i, [vp, vp, i, i, i, d, d, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

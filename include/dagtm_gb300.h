@@ -175,6 +175,31 @@ int dgtm_fe_backward(const float *Y, const float *T, int N, int K, int D, double
                      const double *gF, float *dY, float *dT, double *dbeta);
 
 /*
+ * dgtm_fe_forward for callers that cannot allocate device memory at all, not
+ * even a workspace: code running where cudaMalloc is forbidden or unwanted (a
+ * host callback; a process whose device memory is all handed out by another
+ * allocator; a latency-critical loop that cannot pay for the synchronisation
+ * an allocation implies).  It runs the same kernels as dgtm_fe_forward and
+ * writes F (one device double) the same way, but keeps its scratch in a
+ * fixed array of DGTM_FE_NOALLOC_BYTES inside this library, which every GPU
+ * that loads the library holds until the process exits.  It calls no
+ * allocator.  Limits and rules:
+ *   - the scratch needs about 24 N + 8 K bytes (plus alignment); problems
+ *     that need more than DGTM_FE_NOALLOC_BYTES are rejected with
+ *     DGTM_EINVAL and a message giving the bytes needed;
+ *   - the first call on each device looks up the array's device address
+ *     (cudaGetSymbolAddress) with that device current: make that first call
+ *     before any stream capture;
+ *   - all calls share the one array, so calls that may overlap on the GPU
+ *     (other streams, other host threads) race with each other: serialise
+ *     them; nothing in the array needs to start at zero.
+ * No counterpart in the reference (which has no GPU code).
+ */
+#define DGTM_FE_NOALLOC_BYTES (8u << 20)
+int dgtm_fe_forward_noalloc(const float *Y, const float *T, int N, int K, int D, double beta,
+                            double temp, void *stream, double *F);
+
+/*
  * Diagnostic: runs the three tensor-core operand configurations the split-BF16
  * kernels rely on (K-major x K-major from shared memory; K-major x MN-major;
  * tensor-memory A x MN-major) on small integer matrices and writes the largest
