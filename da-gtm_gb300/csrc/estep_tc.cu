@@ -48,13 +48,13 @@ using namespace sm100;
 namespace {
 
 constexpr int P1_THREADS = 320;       // warp 0 TMA, warp 1 MMA, warps 2-9 statistics
-constexpr int P2_THREADS = 192;       // warp 0 TMA, warp 1 MMA, warps 2-5 responsibilities
-constexpr int P1_BN = 128;            // points per CTA (MMA M)
-constexpr int P1_BK = 256;            // centres per chunk (MMA N)
+constexpr int P2_THREADS = 320;       // warp 0 TMA, warp 1 MMA, warps 2-9 responsibilities
+constexpr int P1_TILE = 128;          // points per tile (MMA M); a CTA holds 1 or 2 tiles
+constexpr int P1_BK = 128;            // centres per chunk (MMA N)
 constexpr int PANEL_ELEMS = 64;       // BF16 elements per 128-byte swizzle row
 constexpr int P2_BK = 128;            // centres per CTA (MMA M)
-constexpr int P2_BN = 64;             // points per streamed tile
-constexpr int P2_UNIT_TILES = 64;     // tiles per output slot (4096 points)
+constexpr int P2_UNIT_POINTS = 16384; // points per output slot
+constexpr int NPAD_ALIGN = 256;       // point padding (two pass-1 tiles)
 constexpr float LOG2E = 1.4426950408889634f;
 constexpr int SMEM_LIMIT = 227 * 1024;
 
@@ -66,11 +66,6 @@ __device__ __forceinline__ uint32_t sw128_off(int r, int c)
     return (uint32_t) (r * 128 + ((((c >> 3) ^ (r & 7)) & 7) << 4) + ((c & 7) << 1));
 }
 
-__device__ __forceinline__ void named_bar_sync(int id, int nthreads)
-{
-    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
-}
-
 __device__ __forceinline__ float bf16_at(const unsigned char *panel, int r, int c)
 {
     const uint16_t v = *(const uint16_t *) (panel + sw128_off(r, c));
@@ -78,7 +73,7 @@ __device__ __forceinline__ float bf16_at(const unsigned char *panel, int r, int 
 }
 
 struct P1Params {
-    int N, D, Dp, npanel, nT, Npad, Kpad, K, nchunk, nstage;
+    int N, D, Dp, npanel, nT, Npad, Kpad, K, nchunk, nstage, ntile;
     float c1l, c2l;       // beta log2(e), beta/temp log2(e)
     double c1, c2;        // beta/2, beta/(2 temp)
     int isDA, two_temps;  // two_temps: isDA and temp != 1
@@ -91,34 +86,31 @@ struct P1Params {
 };
 
 // ---------------------------------------------------------------------------
-// pass 1
+// pass 1: one CTA per ntile x 128 points (ntile = 2 when T is exact in BF16)
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(P1_THREADS, 1)
     tc_pass1_kernel(const __grid_constant__ CUtensorMap tmT, const __grid_constant__ CUtensorMap tmY,
                     const P1Params p)
 {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    unsigned char *base = (unsigned char *) (((uintptr_t) smem_raw + 1023) & ~(uintptr_t) 1023);
-    const int tpanel_bytes = P1_BN * 128;             // 16 KB
-    const int ystage_bytes = P1_BK * 128;             // 32 KB
-    unsigned char *Ts = base;                          // nT x npanel panels
-    unsigned char *Ystage = base + p.nT * p.npanel * tpanel_bytes;
+    unsigned char *base = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
+    const int tpanel_bytes = P1_TILE * 128;           // 16 KB
+    const int ystage_bytes = P1_BK * 128;             // 16 KB
+    unsigned char *Ts = base;                          // ntile x nT x npanel panels
+    unsigned char *Ystage = base + p.ntile * p.nT * p.npanel * tpanel_bytes;
     uint64_t *bars = (uint64_t *) (Ystage + p.nstage * ystage_bytes);
     uint64_t *y_full = bars;
     uint64_t *y_empty = bars + p.nstage;
     uint64_t *t_full = bars + 2 * p.nstage;
-    uint64_t *acc_full = t_full + 1;
-    uint64_t *acc_empty = acc_full + 2;
-    uint64_t *drain = acc_empty + 2;
+    uint64_t *acc_full = t_full + 1;    // [tile * 2 + buffer]
+    uint64_t *acc_empty = acc_full + 4;
+    uint64_t *drain = acc_empty + 4;
     uint32_t *tmem_sh = (uint32_t *) (drain + 1);
-    double *red = (double *) (tmem_sh + 2);            // 2 x 128
-    double *mrg_s = red + 256;                          // 2 x 128
-    float *mrg_m = (float *) (mrg_s + 256);             // 128
-    int *mrg_k = (int *) (mrg_m + 128);                 // 128
+    double *red = (double *) (tmem_sh + 2);            // 2 x 256
     __shared__ int failed;
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int n0 = blockIdx.x * P1_BN;
+    const int n0 = blockIdx.x * p.ntile * P1_TILE;
 
     if (threadIdx.x == 0) {
         failed = 0;
@@ -127,9 +119,9 @@ __global__ void __launch_bounds__(P1_THREADS, 1)
             mbar_init(&y_empty[s], 1);
         }
         mbar_init(t_full, 1);
-        for (int b = 0; b < 2; b++) {
+        for (int b = 0; b < 4; b++) {
             mbar_init(&acc_full[b], 1);
-            mbar_init(&acc_empty[b], 256);
+            mbar_init(&acc_empty[b], 128);
         }
         mbar_init(drain, 1);
         fence_barrier_init();
@@ -148,11 +140,12 @@ __global__ void __launch_bounds__(P1_THREADS, 1)
         // ---------------- producer ----------------
         prefetch_tmap(&tmT);
         prefetch_tmap(&tmY);
-        mbar_expect_tx(t_full, (uint32_t) (p.nT * p.npanel * tpanel_bytes));
-        for (int tp = 0; tp < p.nT; tp++)
-            for (int pn = 0; pn < p.npanel; pn++)
-                tma_load_2d(Ts + (tp * p.npanel + pn) * tpanel_bytes, &tmT, t_full,
-                            PANEL_ELEMS * pn, tp * p.Npad + n0);
+        mbar_expect_tx(t_full, (uint32_t) (p.ntile * p.nT * p.npanel * tpanel_bytes));
+        for (int i = 0; i < p.ntile; i++)
+            for (int tp = 0; tp < p.nT; tp++)
+                for (int pn = 0; pn < p.npanel; pn++)
+                    tma_load_2d(Ts + ((i * p.nT + tp) * p.npanel + pn) * tpanel_bytes, &tmT, t_full,
+                                PANEL_ELEMS * pn, tp * p.Npad + n0 + i * P1_TILE);
         for (int it = 0; it < total_loads; it++) {
             const int s = it % p.nstage, use = it / p.nstage;
             if (use > 0 && !mbar_wait(&y_empty[s], (use - 1) & 1, p.status, 11)) {
@@ -167,18 +160,20 @@ __global__ void __launch_bounds__(P1_THREADS, 1)
         }
     } else if (warp == 1 && lane == 0) {
         // ---------------- MMA issuer ----------------
-        const uint32_t idesc = idesc_bf16(P1_BN, P1_BK, 0, 0);
+        const uint32_t idesc = idesc_bf16(P1_TILE, P1_BK, 0, 0);
         bool ok = mbar_wait(t_full, 0, p.status, 12);
         int it = 0;
         for (int c = 0; ok && c < p.nchunk; c++) {
             const int b = c & 1, use = c >> 1;
-            if (use > 0 && !mbar_wait(&acc_empty[b], (use - 1) & 1, p.status, 13)) {
-                ok = false;
+            for (int i = 0; i < p.ntile && use > 0; i++)
+                if (!mbar_wait(&acc_empty[i * 2 + b], (use - 1) & 1, p.status, 13)) {
+                    ok = false;
+                    break;
+                }
+            if (!ok)
                 break;
-            }
             tc_fence_after();
-            const uint32_t d_tmem = tmem + (uint32_t) (b * P1_BK);
-            uint32_t acc = 0;
+            uint32_t acc0 = 0, acc1 = 0;
             for (int r = 0; r < per_chunk; r++, it++) {
                 const int s = it % p.nstage;
                 if (!mbar_wait(&y_full[s], (it / p.nstage) & 1, p.status, 14)) {
@@ -187,139 +182,120 @@ __global__ void __launch_bounds__(P1_THREADS, 1)
                 }
                 tc_fence_after();
                 const int piece = r / p.npanel, pn = r % p.npanel;
-                const uint32_t ys = smem_u32(Ystage + s * ystage_bytes);
+                const uint64_t bd0 = sdesc_sw128(smem_u32(Ystage + s * ystage_bytes), 16, 1024);
                 // Y_hi pairs with T_hi (and T_lo when T is split); Y_lo with T_hi
                 const int ntp = (piece == 0) ? p.nT : 1;
-                for (int kk = 0; kk < 4; kk++) {
-                    const uint64_t bd = sdesc_sw128(ys + kk * 32, 16, 1024);
+                for (int i = 0; i < p.ntile; i++) {
+                    const uint32_t d_tmem = tmem + (uint32_t) ((i * 2 + b) * P1_BK);
+                    uint32_t &acc = (i == 0) ? acc0 : acc1;
                     for (int tp = 0; tp < ntp; tp++) {
-                        const uint32_t ta =
-                            smem_u32(Ts + (tp * p.npanel + pn) * tpanel_bytes) + kk * 32;
-                        mma_ss(d_tmem, sdesc_sw128(ta, 16, 1024), bd, idesc, acc);
-                        acc = 1;
+                        const uint64_t ad0 = sdesc_sw128(
+                            smem_u32(Ts + ((i * p.nT + tp) * p.npanel + pn) * tpanel_bytes), 16, 1024);
+#pragma unroll
+                        for (int kk = 0; kk < 4; kk++) {
+                            mma_ss(d_tmem, ad0 + 2 * kk, bd0 + 2 * kk, idesc, acc);
+                            acc = 1;
+                        }
                     }
                 }
                 mma_commit(&y_empty[s]);
             }
             if (!ok)
                 break;
-            mma_commit(&acc_full[b]);
+            for (int i = 0; i < p.ntile; i++)
+                mma_commit(&acc_full[i * 2 + b]);
         }
         if (!ok)
             failed = 1;
     } else if (warp >= 2) {
-        // ---------------- statistics: two warps per TMEM lane quarter ----------------
-        // group 0 (warps 2-5) takes columns 0..127 of every chunk, group 1
-        // (warps 6-9) columns 128..255; each thread keeps a running maximum of
-        // acc (its argmax) and the two shifted sums for its point, and the two
-        // halves are merged at the end.
+        // ---------------- statistics: one 4-warp group per point tile ----------------
         const int q = warp & 3;
-        const int grp = (warp - 2) >> 2;
+        const int g = (warp - 2) >> 2;
         const int row = q * 32 + lane;
         const uint32_t lane_base = tmem + ((uint32_t) (q * 32) << 16);
-        float m = -INFINITY;
-        int kstar = 0;
-        double s1 = 0.0, s2 = 0.0;
+        double t1 = 0.0, t2 = 0.0;
         bool ok = true;
-        for (int c = 0; c < p.nchunk; c++) {
-            const int b = c & 1;
-            if (!mbar_wait(&acc_full[b], (c >> 1) & 1, p.status, 15)) {
-                ok = false;
-                break;
-            }
-            tc_fence_after();
-            for (int sub = 0; sub < 2; sub++) {
-                uint32_t va[32], vb[32];
-                const int colc = grp * 128 + sub * 64;
-                const uint32_t col = (uint32_t) (b * P1_BK + colc);
-                tmem_ld32(lane_base + col, va);
-                tmem_ld32(lane_base + col + 32, vb);
-                tmem_ld_wait();
-                float mx0 = -INFINITY, mx1 = -INFINITY;
-#pragma unroll
-                for (int j = 0; j < 32; j++) {
-                    mx0 = fmaxf(mx0, __uint_as_float(va[j]));
-                    mx1 = fmaxf(mx1, __uint_as_float(vb[j]));
+        if (g < p.ntile) {
+            float m = -INFINITY;
+            int kstar = 0;
+            double s1 = 0.0, s2 = 0.0;
+            for (int c = 0; c < p.nchunk; c++) {
+                const int b = c & 1;
+                if (!mbar_wait(&acc_full[g * 2 + b], (c >> 1) & 1, p.status, 15)) {
+                    ok = false;
+                    break;
                 }
-                const float mx = fmaxf(mx0, mx1);
-                if (mx > m) {
-                    if (m > -INFINITY) {
-                        s1 *= (double) ex2((m - mx) * p.c1l);
-                        s2 *= (double) ex2((m - mx) * p.c2l);
-                    }
-                    int j0 = 64;
+                tc_fence_after();
+#pragma unroll 1
+                for (int sub = 0; sub < 2; sub++) {
+                    uint32_t va[32], vb[32];
+                    const uint32_t col = (uint32_t) ((g * 2 + b) * P1_BK + sub * 64);
+                    tmem_ld32(lane_base + col, va);
+                    tmem_ld32(lane_base + col + 32, vb);
+                    tmem_ld_wait();
+                    float mx0 = -INFINITY, mx1 = -INFINITY;
 #pragma unroll
-                    for (int j = 31; j >= 0; j--) {
-                        if (__uint_as_float(vb[j]) == mx)
-                            j0 = 32 + j;
+                    for (int j = 0; j < 32; j++) {
+                        mx0 = fmaxf(mx0, __uint_as_float(va[j]));
+                        mx1 = fmaxf(mx1, __uint_as_float(vb[j]));
                     }
+                    const float mx = fmaxf(mx0, mx1);
+                    if (mx > m) {
+                        if (m > -INFINITY) {
+                            s1 *= (double) ex2((m - mx) * p.c1l);
+                            s2 *= (double) ex2((m - mx) * p.c2l);
+                        }
+                        int j0 = 64;
 #pragma unroll
-                    for (int j = 31; j >= 0; j--) {
-                        if (__uint_as_float(va[j]) == mx)
-                            j0 = j;
+                        for (int j = 31; j >= 0; j--) {
+                            if (__uint_as_float(vb[j]) == mx)
+                                j0 = 32 + j;
+                        }
+#pragma unroll
+                        for (int j = 31; j >= 0; j--) {
+                            if (__uint_as_float(va[j]) == mx)
+                                j0 = j;
+                        }
+                        m = mx;
+                        kstar = c * P1_BK + sub * 64 + j0;
                     }
-                    m = mx;
-                    kstar = c * P1_BK + colc + j0;
+                    // four independent accumulation chains per sum
+                    float e1[4] = {0.f, 0.f, 0.f, 0.f}, e2[4] = {0.f, 0.f, 0.f, 0.f};
+                    if (p.two_temps) {
+#pragma unroll
+                        for (int j = 0; j < 32; j += 2) {
+                            const float xa0 = __uint_as_float(va[j]) - m, xa1 = __uint_as_float(va[j + 1]) - m;
+                            const float xb0 = __uint_as_float(vb[j]) - m, xb1 = __uint_as_float(vb[j + 1]) - m;
+                            e1[0] += ex2(xa0 * p.c1l);
+                            e1[1] += ex2(xa1 * p.c1l);
+                            e1[2] += ex2(xb0 * p.c1l);
+                            e1[3] += ex2(xb1 * p.c1l);
+                            e2[0] += ex2(xa0 * p.c2l);
+                            e2[1] += ex2(xa1 * p.c2l);
+                            e2[2] += ex2(xb0 * p.c2l);
+                            e2[3] += ex2(xb1 * p.c2l);
+                        }
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < 32; j += 2) {
+                            e1[0] += ex2((__uint_as_float(va[j]) - m) * p.c1l);
+                            e1[1] += ex2((__uint_as_float(va[j + 1]) - m) * p.c1l);
+                            e1[2] += ex2((__uint_as_float(vb[j]) - m) * p.c1l);
+                            e1[3] += ex2((__uint_as_float(vb[j + 1]) - m) * p.c1l);
+                        }
+                    }
+                    s1 += (double) ((e1[0] + e1[1]) + (e1[2] + e1[3]));
+                    s2 += (double) ((e2[0] + e2[1]) + (e2[2] + e2[3]));
                 }
-                // four independent accumulation chains per sum
-                float e1[4] = {0.f, 0.f, 0.f, 0.f}, e2[4] = {0.f, 0.f, 0.f, 0.f};
-                if (p.two_temps) {
-#pragma unroll
-                    for (int j = 0; j < 32; j += 2) {
-                        const float xa0 = __uint_as_float(va[j]) - m, xa1 = __uint_as_float(va[j + 1]) - m;
-                        const float xb0 = __uint_as_float(vb[j]) - m, xb1 = __uint_as_float(vb[j + 1]) - m;
-                        e1[0] += ex2(xa0 * p.c1l);
-                        e1[1] += ex2(xa1 * p.c1l);
-                        e1[2] += ex2(xb0 * p.c1l);
-                        e1[3] += ex2(xb1 * p.c1l);
-                        e2[0] += ex2(xa0 * p.c2l);
-                        e2[1] += ex2(xa1 * p.c2l);
-                        e2[2] += ex2(xb0 * p.c2l);
-                        e2[3] += ex2(xb1 * p.c2l);
-                    }
-                } else {
-#pragma unroll
-                    for (int j = 0; j < 32; j += 2) {
-                        e1[0] += ex2((__uint_as_float(va[j]) - m) * p.c1l);
-                        e1[1] += ex2((__uint_as_float(va[j + 1]) - m) * p.c1l);
-                        e1[2] += ex2((__uint_as_float(vb[j]) - m) * p.c1l);
-                        e1[3] += ex2((__uint_as_float(vb[j + 1]) - m) * p.c1l);
-                    }
-                }
-                s1 += (double) ((e1[0] + e1[1]) + (e1[2] + e1[3]));
-                s2 += (double) ((e2[0] + e2[1]) + (e2[2] + e2[3]));
-            }
-            tc_fence_before();
-            mbar_arrive(&acc_empty[b]);
-        }
-        // merge the two column halves (group 1 hands its state to group 0)
-        if (grp == 1) {
-            mrg_m[row] = m;
-            mrg_k[row] = kstar;
-            mrg_s[row] = s1;
-            mrg_s[128 + row] = s2;
-            if (!ok)
-                failed = 1;
-        }
-        named_bar_sync(1, 256);
-        if (grp == 0) {
-            const float mo = mrg_m[row];
-            const double so1 = mrg_s[row], so2 = mrg_s[128 + row];
-            if (mo > m || (mo == m && mrg_k[row] < kstar)) {
-                s1 = s1 * (double) ex2((m - mo) * p.c1l) + so1;
-                s2 = s2 * (double) ex2((m - mo) * p.c2l) + so2;
-                m = mo;
-                kstar = mrg_k[row];
-            } else {
-                s1 += so1 * (double) ex2((mo - m) * p.c1l);
-                s2 += so2 * (double) ex2((mo - m) * p.c2l);
+                tc_fence_before();
+                mbar_arrive(&acc_empty[g * 2 + b]);
             }
             if (!p.two_temps)
                 s2 = s1;
             // exact (FP32) distance to the best centre, from the unsplit centre
             // and the data, then the per-point terms
-            const int n = n0 + row;
-            double t1 = 0.0, t2 = 0.0;
+            const int prow = g * P1_TILE + row;
+            const int n = n0 + prow;
             if (ok && !mbar_wait(t_full, 0, p.status, 17))
                 ok = false;
             if (ok && n < p.N) {
@@ -328,8 +304,9 @@ __global__ void __launch_bounds__(P1_THREADS, 1)
                 float dsum = 0.f;
                 if (p.nT == 1) {
                     // the data are exact in BF16: read them from the resident tile
+                    const unsigned char *tile = Ts + g * p.npanel * tpanel_bytes;
                     for (int d = 0; d < p.D; d++) {
-                        const float df = yk[d] - bf16_at(Ts + (d >> 6) * tpanel_bytes, row, d & 63);
+                        const float df = yk[d] - bf16_at(tile + (d >> 6) * tpanel_bytes, row, d & 63);
                         dsum = fmaf(df, df, dsum);
                     }
                 } else {
@@ -364,24 +341,24 @@ __global__ void __launch_bounds__(P1_THREADS, 1)
             } else if (n < p.Npad) {
                 p.colq[n] = make_float4(0.f, 0.f, INFINITY, 0.f);  // padding: R = 0
             }
-            red[row] = t1;
-            red[128 + row] = t2;
             if (!ok)
                 failed = 1;
         }
+        red[g * P1_TILE + row] = t1;
+        red[256 + g * P1_TILE + row] = t2;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
         double a = 0.0, b2 = 0.0;
-        for (int i = 0; i < 128; i++) {
+        for (int i = 0; i < p.ntile * P1_TILE; i++) {
             a += red[i];
-            b2 += red[128 + i];
+            b2 += red[256 + i];
         }
         p.part[2 * blockIdx.x] = a;
         p.part[2 * blockIdx.x + 1] = b2;
     }
     if (failed && warp == 1 && lane == 0) {
-        // let every issued MMA finish before the accumulator is released
+        // let every issued MMA finish before the accumulators are released
         mma_commit(drain);
         mbar_wait(drain, 0, p.status, 16, 100000000ull);
     }
@@ -396,7 +373,7 @@ __global__ void __launch_bounds__(P1_THREADS, 1)
 // pass 2
 // ---------------------------------------------------------------------------
 struct P2Params {
-    int D, Dp, npanel, nT, Npad, Kpad, ntiles, units_per_k, ktiles, nunits, nstage;
+    int D, Dp, npanel, nT, Npad, Kpad, bn, ntiles, units_per_k, ktiles, nunits, nstage;
     const float4 *colq;   // Npad
     float *RTpart;        // nunits x 128 x Dp
     int *status;
@@ -411,8 +388,9 @@ __device__ __forceinline__ void unit_of(const P2Params &p, int v, int &u, int &k
     const int nu = v / p.ktiles;
     kt = v % p.ktiles;
     u = kt * p.units_per_k + nu;
-    t0 = nu * P2_UNIT_TILES;
-    t1 = min(p.ntiles, t0 + P2_UNIT_TILES);
+    const int per_unit = P2_UNIT_POINTS / p.bn;
+    t0 = nu * per_unit;
+    t1 = min(p.ntiles, t0 + per_unit);
 }
 
 __global__ void __launch_bounds__(P2_THREADS, 1)
@@ -420,14 +398,16 @@ __global__ void __launch_bounds__(P2_THREADS, 1)
                     const P2Params p)
 {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    unsigned char *base = (unsigned char *) (((uintptr_t) smem_raw + 1023) & ~(uintptr_t) 1023);
+    unsigned char *base = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
+    const int bn = p.bn;                                   // points per tile: 64 or 128
+    const int ng = bn / 64;                                // active responsibility groups
     const int ypanel_bytes = P2_BK * 128;                  // 16 KB
-    const int tpanel_bytes = P2_BN * 128;                  // 8 KB
+    const int tpanel_bytes = bn * 128;
     const int tstage_bytes = p.nT * p.npanel * tpanel_bytes;
     unsigned char *Ys = base;                               // 2 x npanel panels
     unsigned char *Tst = base + 2 * p.npanel * ypanel_bytes;
-    float4 *cq = (float4 *) (Tst + p.nstage * tstage_bytes); // nstage x 64
-    uint64_t *bars = (uint64_t *) (cq + p.nstage * P2_BN);
+    float4 *cq = (float4 *) (Tst + p.nstage * tstage_bytes); // nstage x bn
+    uint64_t *bars = (uint64_t *) (cq + p.nstage * bn);
     uint64_t *t_full = bars;
     uint64_t *t_empty = bars + p.nstage;
     uint64_t *y_full = bars + 2 * p.nstage;
@@ -452,10 +432,10 @@ __global__ void __launch_bounds__(P2_THREADS, 1)
         mbar_init(y_empty, 1);
         for (int b = 0; b < 2; b++) {
             mbar_init(&s_full[b], 1);
-            mbar_init(&p_full[b], 128);
+            mbar_init(&p_full[b], 128 * ng);
         }
         mbar_init(rt_full, 1);
-        mbar_init(rt_empty, 128);
+        mbar_init(rt_empty, 128 * ng);
         mbar_init(drain, 1);
         fence_barrier_init();
     }
@@ -496,19 +476,19 @@ __global__ void __launch_bounds__(P2_THREADS, 1)
                     ok = false;
                     break;
                 }
-                mbar_expect_tx(&t_full[s], (uint32_t) (tstage_bytes + P2_BN * 16));
+                mbar_expect_tx(&t_full[s], (uint32_t) (tstage_bytes + bn * 16));
                 for (int tp = 0; tp < p.nT; tp++)
                     for (int pn = 0; pn < p.npanel; pn++)
                         tma_load_2d(Tst + s * tstage_bytes + (tp * p.npanel + pn) * tpanel_bytes,
-                                    &tmT, &t_full[s], PANEL_ELEMS * pn, tp * p.Npad + t * P2_BN);
-                bulk_load(cq + s * P2_BN, p.colq + (size_t) t * P2_BN, P2_BN * 16, &t_full[s]);
+                                    &tmT, &t_full[s], PANEL_ELEMS * pn, tp * p.Npad + t * bn);
+                bulk_load(cq + s * bn, p.colq + (size_t) t * bn, (uint32_t) (bn * 16), &t_full[s]);
             }
         }
         if (!ok)
             failed = 1;
     } else if (warp == 1 && lane == 0) {
         // ---------------- MMA issuer ----------------
-        const uint32_t id1 = idesc_bf16(P2_BK, P2_BN, 0, 0);
+        const uint32_t id1 = idesc_bf16(P2_BK, bn, 0, 0);
         const uint32_t id2 = idesc_bf16(P2_BK, p.Dp, 0, 1);
         int jt = 0, cur_kt = -1, yuse = 0, nunit = 0;
         bool ok = true;
@@ -529,25 +509,27 @@ __global__ void __launch_bounds__(P2_THREADS, 1)
             const int first_j = jt;
             for (int t = t0; t <= t1 && ok; t++) {
                 if (t < t1) {
-                    // distances of tile jt
+                    // distances of tile jt: M = 128 centres, N = bn points
                     const int s = jt % p.nstage, b = jt & 1;
                     if (!mbar_wait(&t_full[s], (jt / p.nstage) & 1, p.status, 24)) {
                         ok = false;
                         break;
                     }
                     tc_fence_after();
-                    const uint32_t d = tmem + (uint32_t) (b * P2_BN);
+                    const uint32_t d = tmem + (uint32_t) (b * bn);
                     const uint32_t tst = smem_u32(Tst + s * tstage_bytes);
                     uint32_t acc = 0;
                     for (int piece = 0; piece < 2; piece++) {
                         const int ntp = (piece == 0) ? p.nT : 1;
                         for (int pn = 0; pn < p.npanel; pn++) {
-                            const uint32_t ya = smem_u32(Ys + (piece * p.npanel + pn) * ypanel_bytes);
-                            for (int kk = 0; kk < 4; kk++) {
-                                const uint64_t ad = sdesc_sw128(ya + kk * 32, 16, 1024);
-                                for (int tp = 0; tp < ntp; tp++) {
-                                    const uint32_t tb = tst + (tp * p.npanel + pn) * tpanel_bytes + kk * 32;
-                                    mma_ss(d, ad, sdesc_sw128(tb, 16, 1024), id1, acc);
+                            const uint64_t ad0 = sdesc_sw128(
+                                smem_u32(Ys + (piece * p.npanel + pn) * ypanel_bytes), 16, 1024);
+                            for (int tp = 0; tp < ntp; tp++) {
+                                const uint64_t bd0 = sdesc_sw128(
+                                    tst + (tp * p.npanel + pn) * tpanel_bytes, 16, 1024);
+#pragma unroll
+                                for (int kk = 0; kk < 4; kk++) {
+                                    mma_ss(d, ad0 + 2 * kk, bd0 + 2 * kk, id1, acc);
                                     acc = 1;
                                 }
                             }
@@ -556,8 +538,8 @@ __global__ void __launch_bounds__(P2_THREADS, 1)
                     mma_commit(&s_full[b]);
                 }
                 if (t > t0) {
-                    // R T of the previous tile
-                    const int j = (t < t1) ? jt - 1 : jt - 1;
+                    // R T of the previous tile: A = R (TMEM), B = the same T tile, MN-major
+                    const int j = jt - 1;
                     const int s = j % p.nstage, b = j & 1;
                     if (j == first_j && nunit > 0 &&
                         !mbar_wait(rt_empty, (nunit - 1) & 1, p.status, 25)) {
@@ -572,12 +554,13 @@ __global__ void __launch_bounds__(P2_THREADS, 1)
                     const uint32_t tst = smem_u32(Tst + s * tstage_bytes);
                     for (int rp = 0; rp < 2; rp++) {
                         const int ntp = (rp == 0) ? p.nT : 1;
-                        for (int kk = 0; kk < P2_BN / 16; kk++) {
-                            const uint32_t a = tmem + (uint32_t) (b * P2_BN + rp * 32 + kk * 8);
-                            for (int tp = 0; tp < ntp; tp++) {
-                                const uint64_t bd = sdesc_sw128(
-                                    tst + tp * p.npanel * tpanel_bytes + kk * 2048, tpanel_bytes, 1024);
-                                mma_ts(rt_tmem, a, bd, id2, rt_acc);
+                        for (int tp = 0; tp < ntp; tp++) {
+                            const uint64_t bd0 =
+                                sdesc_sw128(tst + tp * p.npanel * tpanel_bytes, tpanel_bytes, 1024);
+                            for (int kk = 0; kk < bn / 16; kk++) {
+                                const uint32_t a = tmem + (uint32_t) (b * bn + (kk >> 2) * 64 +
+                                                                      rp * 32 + (kk & 3) * 8);
+                                mma_ts(rt_tmem, a, bd0 + (uint64_t) (kk * (2048 >> 4)), id2, rt_acc);
                                 rt_acc = 1;
                             }
                         }
@@ -596,91 +579,98 @@ __global__ void __launch_bounds__(P2_THREADS, 1)
             failed = 1;
     } else if (warp >= 2) {
         // ---------------- responsibilities and the R T drain ----------------
+        // group g (warps 2-5 / 6-9) handles points 64 g .. 64 g + 63 of each tile
         const int q = warp & 3;
+        const int g = (warp - 2) >> 2;
         const int row = q * 32 + lane;  // centre within the tile
         const uint32_t lane_base = tmem + ((uint32_t) (q * 32) << 16);
-        int jt = 0, nunit = 0;
-        bool ok = true;
-        for (int v = blockIdx.x; ok && v < p.nunits; v += gridDim.x) {
-            int u, kt, t0, t1;
-            unit_of(p, v, u, kt, t0, t1);
-            for (int t = t0; t < t1; t++, jt++) {
-                const int s = jt % p.nstage, b = jt & 1;
-                if (!mbar_wait(&t_full[s], (jt / p.nstage) & 1, p.status, 27) ||
-                    !mbar_wait(&s_full[b], (jt >> 1) & 1, p.status, 28)) {
+        if (g < ng) {
+            int jt = 0, nunit = 0;
+            bool ok = true;
+            for (int v = blockIdx.x; ok && v < p.nunits; v += gridDim.x) {
+                int u, kt, t0, t1;
+                unit_of(p, v, u, kt, t0, t1);
+                for (int t = t0; t < t1; t++, jt++) {
+                    const int s = jt % p.nstage, b = jt & 1;
+                    if (!mbar_wait(&t_full[s], (jt / p.nstage) & 1, p.status, 27) ||
+                        !mbar_wait(&s_full[b], (jt >> 1) & 1, p.status, 28)) {
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t col0 = (uint32_t) (b * bn + g * 64);
+                    uint32_t va[32], vb[32];
+                    tmem_ld32(lane_base + col0, va);
+                    tmem_ld32(lane_base + col0 + 32, vb);
+                    tmem_ld_wait();
+                    const float4 *cqs = cq + s * bn + g * 64;
+                    uint32_t hi[32], lo[32];
+#pragma unroll
+                    for (int j = 0; j < 16; j++) {
+                        float r[4];
+#pragma unroll
+                        for (int e = 0; e < 4; e++) {
+                            const int n = 4 * j + e;  // point within the sub-block
+                            const float a = (n < 32) ? __uint_as_float(va[n]) : __uint_as_float(vb[n - 32]);
+                            const float4 c = cqs[n];
+                            r[e] = ex2(fmaf(a - c.x, c.y, -c.z));
+                        }
+#pragma unroll
+                        for (int e = 0; e < 4; e += 2) {
+                            const uint32_t h = pack_bf16(r[e], r[e + 1]);
+                            const float rl0 = r[e] - bf16lo_to_f32(h);
+                            const float rl1 = r[e + 1] - bf16hi_to_f32(h);
+                            hi[2 * j + e / 2] = h;
+                            lo[2 * j + e / 2] = pack_bf16(rl0, rl1);
+                        }
+                    }
+                    // R_hi over the first half of the sub-block, R_lo over the second
+                    uint32_t h16[16], l16[16];
+#pragma unroll
+                    for (int i = 0; i < 16; i++) {
+                        h16[i] = hi[i];
+                        l16[i] = lo[i];
+                    }
+                    tmem_st16(lane_base + col0, h16);
+                    tmem_st16(lane_base + col0 + 32, l16);
+#pragma unroll
+                    for (int i = 0; i < 16; i++) {
+                        h16[i] = hi[16 + i];
+                        l16[i] = lo[16 + i];
+                    }
+                    tmem_st16(lane_base + col0 + 16, h16);
+                    tmem_st16(lane_base + col0 + 48, l16);
+                    tmem_st_wait();
+                    tc_fence_before();
+                    mbar_arrive(&p_full[b]);
+                }
+                if (!ok)
+                    break;
+                // drain this unit's R T (FP32) to its slot; the groups split the columns
+                if (!mbar_wait(rt_full, nunit & 1, p.status, 29)) {
                     ok = false;
                     break;
                 }
                 tc_fence_after();
-                uint32_t va[32], vb[32];
-                tmem_ld32(lane_base + (uint32_t) (b * P2_BN), va);
-                tmem_ld32(lane_base + (uint32_t) (b * P2_BN + 32), vb);
-                tmem_ld_wait();
-                const float4 *cqs = cq + s * P2_BN;
-                uint32_t hi[32], lo[32];
+                float *dst = p.RTpart + ((size_t) u * P2_BK + row) * p.Dp;
+                const int cw = p.Dp / ng;
+                for (int c0 = g * cw; c0 < (g + 1) * cw; c0 += 32) {
+                    uint32_t vv[32];
+                    tmem_ld32(lane_base + 256 + (uint32_t) c0, vv);
+                    tmem_ld_wait();
 #pragma unroll
-                for (int j = 0; j < 16; j++) {
-                    float r[4];
-#pragma unroll
-                    for (int e = 0; e < 4; e++) {
-                        const int n = 4 * j + e;  // point within the tile
-                        const float a = (n < 32) ? __uint_as_float(va[n]) : __uint_as_float(vb[n - 32]);
-                        const float4 c = cqs[n];
-                        r[e] = ex2(fmaf(a - c.x, c.y, -c.z));
-                    }
-#pragma unroll
-                    for (int e = 0; e < 4; e += 2) {
-                        const uint32_t h = pack_bf16(r[e], r[e + 1]);
-                        const float rl0 = r[e] - bf16lo_to_f32(h);
-                        const float rl1 = r[e + 1] - bf16hi_to_f32(h);
-                        hi[2 * j + e / 2] = h;
-                        lo[2 * j + e / 2] = pack_bf16(rl0, rl1);
-                    }
+                    for (int j = 0; j < 32; j += 4)
+                        *(float4 *) (dst + c0 + j) =
+                            make_float4(__uint_as_float(vv[j]), __uint_as_float(vv[j + 1]),
+                                        __uint_as_float(vv[j + 2]), __uint_as_float(vv[j + 3]));
                 }
-                // R_hi over the first half of the buffer, R_lo over the second
-                uint32_t h16[16], l16[16];
-#pragma unroll
-                for (int i = 0; i < 16; i++) {
-                    h16[i] = hi[i];
-                    l16[i] = lo[i];
-                }
-                tmem_st16(lane_base + (uint32_t) (b * P2_BN), h16);
-                tmem_st16(lane_base + (uint32_t) (b * P2_BN + 32), l16);
-#pragma unroll
-                for (int i = 0; i < 16; i++) {
-                    h16[i] = hi[16 + i];
-                    l16[i] = lo[16 + i];
-                }
-                tmem_st16(lane_base + (uint32_t) (b * P2_BN + 16), h16);
-                tmem_st16(lane_base + (uint32_t) (b * P2_BN + 48), l16);
-                tmem_st_wait();
                 tc_fence_before();
-                mbar_arrive(&p_full[b]);
+                mbar_arrive(rt_empty);
+                nunit++;
             }
             if (!ok)
-                break;
-            // drain this unit's R T (FP32) to its slot
-            if (!mbar_wait(rt_full, nunit & 1, p.status, 29)) {
-                ok = false;
-                break;
-            }
-            tc_fence_after();
-            float *dst = p.RTpart + ((size_t) u * P2_BK + row) * p.Dp;
-            for (int c0 = 0; c0 < p.Dp; c0 += 32) {
-                uint32_t v[32];
-                tmem_ld32(lane_base + 256 + (uint32_t) c0, v);
-                tmem_ld_wait();
-#pragma unroll
-                for (int j = 0; j < 32; j += 4)
-                    *(float4 *) (dst + c0 + j) = make_float4(__uint_as_float(v[j]), __uint_as_float(v[j + 1]),
-                                                             __uint_as_float(v[j + 2]), __uint_as_float(v[j + 3]));
-            }
-            tc_fence_before();
-            mbar_arrive(rt_empty);
-            nunit++;
+                failed = 1;
         }
-        if (!ok)
-            failed = 1;
     }
     __syncthreads();
     if (failed && warp == 1 && lane == 0) {
@@ -806,7 +796,7 @@ __global__ void slot_reduce_kernel(const float *__restrict__ RTpart, int K, int 
 struct TcState {
     int N, D, K, sms;
     int Dp, npanel, Npad, Kpad, nT;
-    int nchunk, nstage1, nstage2;
+    int nchunk, nstage1, nstage2, ntile1, bn2;
     int ntiles2, units_per_k, nunits, grid2;
     size_t smem1, smem2;
     __nv_bfloat16 *Tb, *Yb;
@@ -852,7 +842,7 @@ int tc_create(TcState **out, int N, int D, int K, int sms, const double *T64, co
     st->T64 = T64;
     st->Dp = round_up(D + 3, PANEL_ELEMS);
     st->npanel = st->Dp / PANEL_ELEMS;
-    st->Npad = round_up(N, P1_BN);
+    st->Npad = round_up(N, NPAD_ALIGN);
     st->Kpad = round_up(K, P1_BK);
     st->nchunk = st->Kpad / P1_BK;
     int rc = DGTM_OK;
@@ -878,11 +868,15 @@ int tc_create(TcState **out, int N, int D, int K, int sms, const double *T64, co
         return fail(DGTM_ECUDA);
     }
     st->nT = (*st->hstatus) ? 2 : 1;
+    // exact 0/1 data: two 128-point tiles per pass-1 CTA and 128-point pass-2
+    // tiles; split data (two T pieces) halve both to fit shared memory
+    st->ntile1 = (st->nT == 1) ? 2 : 1;
+    st->bn2 = (st->nT == 1) ? 128 : 64;
 
     const size_t tpl = (size_t) st->Npad * st->Dp, ypl = (size_t) st->Kpad * st->Dp;
     // pass 2 work units
-    st->ntiles2 = st->Npad / P2_BN;
-    st->units_per_k = (st->ntiles2 + P2_UNIT_TILES - 1) / P2_UNIT_TILES;
+    st->ntiles2 = st->Npad / st->bn2;
+    st->units_per_k = (st->Npad + P2_UNIT_POINTS - 1) / P2_UNIT_POINTS;
     const int ktiles2 = (K + P2_BK - 1) / P2_BK;
     st->nunits = ktiles2 * st->units_per_k;
     st->grid2 = st->nunits < sms ? st->nunits : sms;
@@ -908,26 +902,26 @@ int tc_create(TcState **out, int N, int D, int K, int sms, const double *T64, co
     }
     // tensor maps: T pieces stacked by rows, Y pieces stacked by rows
     if ((rc = make_tmap_bf16(&st->tmT1, st->Tb, (uint64_t) st->nT * st->Npad, st->Dp, st->Dp,
-                             P1_BN, PANEL_ELEMS)) != DGTM_OK ||
+                             P1_TILE, PANEL_ELEMS)) != DGTM_OK ||
         (rc = make_tmap_bf16(&st->tmT2, st->Tb, (uint64_t) st->nT * st->Npad, st->Dp, st->Dp,
-                             P2_BN, PANEL_ELEMS)) != DGTM_OK ||
+                             st->bn2, PANEL_ELEMS)) != DGTM_OK ||
         (rc = make_tmap_bf16(&st->tmY1, st->Yb, 2 * (uint64_t) st->Kpad, st->Dp, st->Dp, P1_BK,
                              PANEL_ELEMS)) != DGTM_OK ||
         (rc = make_tmap_bf16(&st->tmY2, st->Yb, 2 * (uint64_t) st->Kpad, st->Dp, st->Dp, P2_BK,
                              PANEL_ELEMS)) != DGTM_OK)
         return fail(rc);
     // shared memory plans
-    const size_t bar_bytes = 64 * 8 + 16 + 4 * 128 * 8 + 2 * 128 * 4;
-    const size_t t1 = (size_t) st->nT * st->npanel * P1_BN * 128;
+    const size_t bar_bytes = 64 * 8 + 16 + 2 * 256 * 8;
+    const size_t t1 = (size_t) st->ntile1 * st->nT * st->npanel * P1_TILE * 128;
     int ns1 = (int) ((SMEM_LIMIT - 1024 - bar_bytes - t1) / (P1_BK * 128));
-    if (ns1 > 6)
-        ns1 = 6;
+    if (ns1 > 8)
+        ns1 = 8;
     const size_t y2 = (size_t) 2 * st->npanel * P2_BK * 128;
-    const size_t ts2 = (size_t) st->nT * st->npanel * P2_BN * 128 + P2_BN * 16;
+    const size_t ts2 = (size_t) st->nT * st->npanel * st->bn2 * 128 + st->bn2 * 16;
     int ns2 = (int) ((SMEM_LIMIT - 1024 - bar_bytes - y2) / ts2);
     if (ns2 > 4)
         ns2 = 4;
-    if (ns1 < 2 || ns2 < 2) {
+    if (ns1 < 3 || ns2 < 2) {
         set_error(DGTM_ENOTSUP, "the split-BF16 form does not fit shared memory (D = %d)", D);
         return fail(DGTM_ENOTSUP);
     }
@@ -971,7 +965,7 @@ int tc_prepare_y(TcState *st, const double *Y64, cudaStream_t s)
     return DGTM_OK;
 }
 
-int tc_pass1_blocks(const TcState *st) { return st->Npad / P1_BN; }
+int tc_pass1_blocks(const TcState *st) { return st->Npad / (st->ntile1 * P1_TILE); }
 
 int tc_estep(TcState *st, const double *, double c1, double c2, int isDA, double2 *colstat,
              double *part, cudaStream_t s, int *nlaunch)
@@ -987,6 +981,7 @@ int tc_estep(TcState *st, const double *, double c1, double c2, int isDA, double
     p.K = st->K;
     p.nchunk = st->nchunk;
     p.nstage = st->nstage1;
+    p.ntile = st->ntile1;
     p.c1 = c1;
     p.c2 = c2;
     p.c1l = (float) (2.0 * c1 * 1.4426950408889634);
@@ -1000,7 +995,7 @@ int tc_estep(TcState *st, const double *, double c1, double c2, int isDA, double
     p.part = part;
     p.status = st->status;
     DGTM_CUDA_TRY(cudaMemsetAsync(st->status, 0, sizeof(int), s));
-    tc_pass1_kernel<<<st->Npad / P1_BN, P1_THREADS, st->smem1, s>>>(st->tmT1, st->tmY1, p);
+    tc_pass1_kernel<<<tc_pass1_blocks(st), P1_THREADS, st->smem1, s>>>(st->tmT1, st->tmY1, p);
     DGTM_CUDA_TRY(cudaGetLastError());
     *nlaunch = 1;
     return DGTM_OK;
@@ -1015,6 +1010,7 @@ int tc_mstep_pass(TcState *st, const double2 *, double, cudaStream_t s, int *nla
     p.nT = st->nT;
     p.Npad = st->Npad;
     p.Kpad = st->Kpad;
+    p.bn = st->bn2;
     p.ntiles = st->ntiles2;
     p.units_per_k = st->units_per_k;
     p.ktiles = (st->K + P2_BK - 1) / P2_BK;

@@ -33,7 +33,7 @@ __global__ void __launch_bounds__(128) selftest_kernel(const __grid_constant__ C
 {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     // 1024-byte aligned operand region
-    unsigned char *base = (unsigned char *) (((uintptr_t) smem_raw + 1023) & ~(uintptr_t) 1023);
+    unsigned char *base = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
     unsigned char *As = base;            // up to 2 panels x 128 rows x 128 B = 32 KB
     unsigned char *Bs = base + 32768;    // up to 64 KB
     __shared__ uint64_t bar_tma, bar_mma;
