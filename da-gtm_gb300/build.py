@@ -18,6 +18,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libdagtm_gb300.so")
+DRIVER = os.path.join(HERE, "dagtm")
+DRIVER_SRC = os.path.join(HERE, "driver")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -80,7 +82,24 @@ def build(force: bool = False, verbose: bool = False) -> str:
         if res.returncode != 0:
             raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
         os.replace(LIB + ".tmp", LIB)
+    build_driver()
     return LIB
+
+
+def build_driver() -> str:
+    """The `dagtm` command (C++17, links the C ABI library)."""
+    srcs = sorted(glob.glob(os.path.join(DRIVER_SRC, "*.cc")))
+    deps = srcs + sorted(glob.glob(os.path.join(DRIVER_SRC, "*.h"))) + [LIB]
+    if not _stale(DRIVER, deps):
+        return DRIVER
+    cxx = shutil.which("g++") or "g++"
+    cmd = [cxx, "-O2", "-std=c++17", "-Wall", "-I" + INCLUDE] + srcs + [
+        "-L" + HERE, "-ldagtm_gb300", "-Wl,-rpath,$ORIGIN", "-o", DRIVER + ".tmp"]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"driver build failed:\n{res.stdout}\n{res.stderr}")
+    os.replace(DRIVER + ".tmp", DRIVER)
+    return DRIVER
 
 
 if __name__ == "__main__":

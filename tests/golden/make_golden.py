@@ -4,7 +4,8 @@ Reads ``data/Oil.h5`` (the input the reference ships) and ``data/Oil.out.h5``
 (an output file the reference wrote for it: a converged DA-GTM state with
 K = 125 (5^3, L = 3), M = 8 (2^3) RBF centres plus bias, N = 1000, D = 12)
 from a jychoi-hpc/da-gtm checkout and stores the arrays the parity tests
-need in ``oil_golden.npz``.  The reference tree is not available where the
+need in ``oil_golden.npz``; ``oil_input.h5`` is a byte copy of the input
+file, for the command-line driver's HDF5 reader.  The reference tree is not available where the
 GPU tests run, so only the .npz travels; this script is kept beside it so
 the fixture can be regenerated:
 
@@ -18,6 +19,7 @@ contiguous datasets (Oil.h5) and deflate-compressed chunked datasets
 from __future__ import annotations
 
 import os
+import shutil
 import struct
 import sys
 import zlib
@@ -170,6 +172,9 @@ def main(data_dir):
     g["R_rowsum"] = R.sum(axis=1)
     here = os.path.dirname(os.path.abspath(__file__))
     np.savez_compressed(os.path.join(here, "oil_golden.npz"), **g)
+    # the input file itself (written by the HDF5 library the reference links),
+    # the fixture of the command-line driver's reader
+    shutil.copyfile(os.path.join(data_dir, "Oil.h5"), os.path.join(here, "oil_input.h5"))
     for k, v in g.items():
         print(k, v.shape, v.dtype)
 

@@ -1,0 +1,100 @@
+"""The `dagtm` command end to end on the reference's oil input: the options,
+the `:::` trace, checkpoints, restart, interpolation and the output layout of
+dagtm/dagtm.cxx, with the EM step on the GPU."""
+import os
+import re
+import signal
+import subprocess
+import sys
+import time
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+from make_golden import H5File  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+DRIVER = os.path.join(ROOT, "da-gtm_gb300", "dagtm")
+OIL_IN = os.path.join(ROOT, "tests", "golden", "oil_input.h5")
+TRACE = re.compile(r"^:::\s+(\d+)\s+(\d+)\s+(\d+)\s+(\S+)\s+(\S+)\s+(\S+)\s+(\S+)")
+
+
+def run(args, cwd):
+    out = subprocess.run([DRIVER] + args, cwd=cwd, capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr
+    return out.stdout
+
+
+def trace(stdout):
+    rows = [TRACE.match(ln) for ln in stdout.splitlines()]
+    return np.array([[float(x) for x in m.groups()] for m in rows if m])
+
+
+def test_run_trace_and_output(tmp_path, pkg, golden):
+    # -e 0: every iteration stays at the start temperature, so the comparison
+    # below does not hinge on where |diff| first drops under eps
+    out = run(["-i", OIL_IN, "-o", "out.h5", "-K", "125", "-L", "3", "-M", "8", "-s", "7",
+               "-j", "40", "-n", "-p", "-a", "0.95", "-e", "0", "-F", "fp64"], tmp_path)
+    tr = trace(out)
+    assert len(tr) == 40 and tr[0][0] == 1 and tr[-1][0] == 40
+    assert "SUMMARY" in out and "Num. of Iterations" in out
+    f = H5File(str(tmp_path / "out.h5"))
+    for name in ("T", "M", "X", "FI", "Y", "W", "beta", "temp", "iter", "seed", "qual", "id", "lb",
+                 "Temp", "LLH", "NFree"):
+        assert name in f.datasets, name
+    assert np.array_equal(f.read("T"), golden["T_in"].astype(np.float64))
+    assert np.array_equal(f.read("lb"), golden["lb_in"])
+    X, FI, Y, W = f.read("X"), f.read("FI"), f.read("Y"), f.read("W")
+    assert X.shape == (125, 3) and FI.shape == (125, 9) and W.shape == (9, 12)
+    assert np.array_equal(X, golden["X"]) and np.max(np.abs(FI - golden["FI"])) < 1e-15
+    assert np.max(np.abs(FI @ W - Y)) < 1e-6 * np.max(np.abs(Y))
+    M = f.read("M")
+    assert M.shape == (1000, 3) and np.all(np.abs(M) <= 1.0 + 1e-12)
+    assert int(f.read("iter")[0]) == 40 and int(f.read("seed")[0]) == 7
+    assert np.allclose(f.read("NFree"), tr[:, 4], rtol=1e-6)
+    # the driver's trace agrees with the package's own loop from the same set-up
+    st = __import__("importlib").import_module(pkg.__name__ + ".gtm_setup")
+    T = golden["T_in"].astype(np.float64)
+    _, FI0, W0, beta0 = st.random_init(T, 3, 125, 8, 2.0, seed=7)
+    with pkg.Context(T, FI0, "fp64", solver="svd") as c:
+        c.set_Y(FI0 @ W0)
+        ref = pkg.anneal(c, beta0, st.start_temp(T, 0.95), alpha=0.95, eps=0.0, maxloop=40)
+    assert np.allclose(tr[:, 4], ref.nfree_trace, rtol=1e-5, atol=1e-6)
+
+
+def test_checkpoint_restart_and_interpolation(tmp_path):
+    # -e 0 keeps the whole run at one temperature, where a restart resumes exactly
+    common = ["-i", OIL_IN, "-K", "125", "-L", "3", "-M", "8", "-s", "3", "-a", "0.9", "-e", "0"]
+    full = trace(run(common + ["-j", "16", "-n"], tmp_path))
+    run(common + ["-j", "10", "-P", "5", "-w", "ck."], tmp_path)
+    assert (tmp_path / "ck.5.h5").exists() and (tmp_path / "ck.10.h5").exists()
+    ck = H5File(str(tmp_path / "ck.10.h5"))
+    for name in ("X", "FI", "Y", "beta", "temp", "iter", "seed", "qual"):
+        assert name in ck.datasets
+    assert int(ck.read("iter")[0]) == 10
+    rest = trace(run(common + ["-r", "ck.10.h5", "-j", "6", "-n"], tmp_path))
+    assert rest[0][0] == 11 and len(rest) == 6
+    # the restarted run repeats iterations 11..16 of the uninterrupted one
+    assert np.allclose(rest[:, 4], full[10:16, 4], rtol=1e-12)
+    assert np.allclose(rest[:, 5], full[10:16, 5], rtol=1e-12)
+    run(["-i", OIL_IN, "-I", "-r", "ck.10.h5", "-o", "interp.h5"], tmp_path)
+    M = H5File(str(tmp_path / "interp.h5")).read("M")
+    assert M.shape == (1000, 3) and np.all(np.isfinite(M))
+
+
+def test_signal_forces_a_checkpoint_and_exit(tmp_path):
+    p = subprocess.Popen([DRIVER, "-i", OIL_IN, "-K", "125", "-L", "3", "-M", "8", "-s", "5",
+                          "-e", "0", "-j", "1000000", "-n", "-w", "sig."], cwd=tmp_path,
+                         stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True)
+    time.sleep(3.0)
+    p.send_signal(signal.SIGCHLD)
+    out, err = p.communicate(timeout=120)
+    assert p.returncode == 0, err
+    files = list(tmp_path.glob("sig.*.h5"))
+    assert len(files) == 1
+    n = int(H5File(str(files[0])).read("iter")[0])
+    assert str(files[0]).endswith(f"sig.{n}.h5")
