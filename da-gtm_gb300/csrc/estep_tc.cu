@@ -16,13 +16,16 @@
 // (the term that dominates its log-sum-exp) is recomputed in FP32 from the
 // unsplit centre.
 //
-// Pass 1 (one CTA per 128 points): warp 0 streams 256-centre x 64-depth
-// BF16 panels of Y through a TMA ring, warp 1 issues tcgen05.mma
-// (M = 128 points, N = 256 centres, K = 16) into one of two TMEM
-// accumulators, warps 2-5 (one thread per point = one TMEM lane) run the
+// Pass 1 (one CTA per two 128-point tiles, or one tile when the data are
+// split): the data tiles are copied once into tensor memory as the MMA A
+// operand; warp 0 streams 128-centre x 64-depth BF16 panels of Y through a
+// TMA ring, warp 1 issues tcgen05.mma (M = 128 points, N = 128 centres,
+// K = 16, A from tensor memory) into one 128-column accumulator per tile,
+// warps 2-9 (one 4-warp group per tile, one thread per point = one TMEM lane)
+// copy each finished chunk to registers, release the accumulator and run the
 // online log-sum-exp over k at temperature 1 and at `temp`.
 //
-// Pass 2 (persistent, units of (128 centres) x (64 x 64 points)): the CTA
+// Pass 2 (persistent, units of (128 centres) x 16384 points): the CTA
 // keeps its 128 centres resident, streams 64-point T tiles, recomputes
 // acc (M = 128 centres, N = 64 points), turns it into R_kn with the pass-1
 // statistics, writes R as BF16 hi/lo back into tensor memory and multiplies
@@ -60,66 +63,74 @@ constexpr int SMEM_LIMIT = 227 * 1024;
 
 __host__ __device__ constexpr int round_up(int a, int b) { return (a + b - 1) / b * b; }
 
-// Byte offset of element (row r, column c) inside one 128-byte-swizzled panel.
-__device__ __forceinline__ uint32_t sw128_off(int r, int c)
-{
-    return (uint32_t) (r * 128 + ((((c >> 3) ^ (r & 7)) & 7) << 4) + ((c & 7) << 1));
-}
-
-__device__ __forceinline__ float bf16_at(const unsigned char *panel, int r, int c)
-{
-    const uint16_t v = *(const uint16_t *) (panel + sw128_off(r, c));
-    return __uint_as_float((uint32_t) v << 16);
-}
-
 struct P1Params {
     int N, D, Dp, npanel, nT, Npad, Kpad, K, nchunk, nstage, ntile;
+    int ksteps;           // 16-deep MMA steps covering the D + 3 used columns
     float c1l, c2l;       // beta log2(e), beta/temp log2(e)
     double c1, c2;        // beta/2, beta/(2 temp)
     int isDA, two_temps;  // two_temps: isDA and temp != 1
     const float *Y32;     // K x D
     const double *T64;    // N x D (exact data, read when T is split in two pieces)
+    const uint32_t *Tb;   // nT x Npad x Dp BF16 (as BF16 pairs)
     double2 *colstat;     // N
     float4 *colq;         // Npad
     double *part;         // 2 per CTA
     int *status;
 };
 
+// TMEM map of pass 1: the point tiles (MMA operand A, BF16 pairs) from column
+// 0, the two 128-column accumulators at columns 256 and 384.
+constexpr int P1_ACC_COL = 256;
+
 // ---------------------------------------------------------------------------
-// pass 1: one CTA per ntile x 128 points (ntile = 2 when T is exact in BF16)
+// pass 1: one CTA per NTILE x 128 points.  The data tiles live in tensor
+// memory as the A operand; shared memory holds only the Y ring.  NTILE = 2
+// (data exact in BF16): each tile owns one accumulator and the two tiles
+// ping-pong, so the tensor pipe works on one tile while the statistics warps
+// read the other.  NTILE = 1 (data split in two BF16 pieces): one tile
+// double-buffers the two accumulators.
+//
+// The kernel is a template on the operand shape -- NP 64-deep panels, KL
+// 16-deep steps used in the last one, NT data pieces -- so that the MMA
+// sequence of a chunk is straight-line code with constant operand offsets.
+// One warp issues; a loop that recomputes descriptors per MMA cannot keep
+// the tensor pipe busy at N = 128.  The Y ring is in slots of one piece
+// (hi or lo) of a 128-centre chunk, NP panels of 16 KB each.
 // ---------------------------------------------------------------------------
+template <int NP, int KL, int NT>
 __global__ void __launch_bounds__(P1_THREADS, 1)
-    tc_pass1_kernel(const __grid_constant__ CUtensorMap tmT, const __grid_constant__ CUtensorMap tmY,
-                    const P1Params p)
+    tc_pass1_kernel(const __grid_constant__ CUtensorMap tmY, const P1Params p)
 {
+    constexpr int NTILE = (NT == 1) ? 2 : 1;
+    constexpr int ACOL = NP * 32;                      // TMEM columns of one data piece
+    constexpr int PANEL_BYTES = P1_BK * 128;           // 16 KB
+    constexpr int SLOT_BYTES = NP * PANEL_BYTES;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char *base = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
-    const int tpanel_bytes = P1_TILE * 128;           // 16 KB
-    const int ystage_bytes = P1_BK * 128;             // 16 KB
-    unsigned char *Ts = base;                          // ntile x nT x npanel panels
-    unsigned char *Ystage = base + p.ntile * p.nT * p.npanel * tpanel_bytes;
-    uint64_t *bars = (uint64_t *) (Ystage + p.nstage * ystage_bytes);
+    const int nslot = p.nstage;
+    unsigned char *Yslot = base;
+    uint64_t *bars = (uint64_t *) (Yslot + nslot * SLOT_BYTES);
     uint64_t *y_full = bars;
-    uint64_t *y_empty = bars + p.nstage;
-    uint64_t *t_full = bars + 2 * p.nstage;
-    uint64_t *acc_full = t_full + 1;    // [tile * 2 + buffer]
-    uint64_t *acc_empty = acc_full + 4;
-    uint64_t *drain = acc_empty + 4;
+    uint64_t *y_empty = bars + nslot;
+    uint64_t *a_ready = bars + 2 * nslot;
+    uint64_t *acc_full = a_ready + 1;   // [region]
+    uint64_t *acc_empty = acc_full + 2;
+    uint64_t *drain = acc_empty + 2;
     uint32_t *tmem_sh = (uint32_t *) (drain + 1);
     double *red = (double *) (tmem_sh + 2);            // 2 x 256
     __shared__ int failed;
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int n0 = blockIdx.x * p.ntile * P1_TILE;
+    const int n0 = blockIdx.x * NTILE * P1_TILE;
 
     if (threadIdx.x == 0) {
         failed = 0;
-        for (int s = 0; s < p.nstage; s++) {
+        for (int s = 0; s < nslot; s++) {
             mbar_init(&y_full[s], 1);
             mbar_init(&y_empty[s], 1);
         }
-        mbar_init(t_full, 1);
-        for (int b = 0; b < 4; b++) {
+        mbar_init(a_ready, 128 * NTILE);
+        for (int b = 0; b < 2; b++) {
             mbar_init(&acc_full[b], 1);
             mbar_init(&acc_empty[b], 128);
         }
@@ -132,78 +143,89 @@ __global__ void __launch_bounds__(P1_THREADS, 1)
     }
     __syncthreads();
     tc_fence_after();
-    const uint32_t tmem = *tmem_sh;
-    const int per_chunk = 2 * p.npanel;  // Y hi/lo x depth panels
-    const int total_loads = p.nchunk * per_chunk;
+    const uint32_t tmem = __shfl_sync(0xffffffffu, *tmem_sh, 0);
+    // accumulator region and its use count for (tile g, chunk c)
+    auto region = [&](int g, int c) { return NTILE == 2 ? g : (c & 1); };
+    auto ruse = [&](int c) { return NTILE == 2 ? c : (c >> 1); };
 
     if (warp == 0 && lane == 0) {
-        // ---------------- producer ----------------
-        prefetch_tmap(&tmT);
+        // ---------------- producer: the Y ring, one piece of a chunk per slot ----------------
         prefetch_tmap(&tmY);
-        mbar_expect_tx(t_full, (uint32_t) (p.ntile * p.nT * p.npanel * tpanel_bytes));
-        for (int i = 0; i < p.ntile; i++)
-            for (int tp = 0; tp < p.nT; tp++)
-                for (int pn = 0; pn < p.npanel; pn++)
-                    tma_load_2d(Ts + ((i * p.nT + tp) * p.npanel + pn) * tpanel_bytes, &tmT, t_full,
-                                PANEL_ELEMS * pn, tp * p.Npad + n0 + i * P1_TILE);
-        for (int it = 0; it < total_loads; it++) {
-            const int s = it % p.nstage, use = it / p.nstage;
-            if (use > 0 && !mbar_wait(&y_empty[s], (use - 1) & 1, p.status, 11)) {
+        int q = 0;
+        uint32_t ph = 0;
+        for (int it = 0; it < 2 * p.nchunk; it++) {
+            if (it >= nslot && !mbar_wait(&y_empty[q], ph ^ 1u, p.status, 11)) {
                 failed = 1;
                 break;
             }
-            const int c = it / per_chunk, r = it % per_chunk;
-            const int piece = r / p.npanel, pn = r % p.npanel;
-            mbar_expect_tx(&y_full[s], (uint32_t) ystage_bytes);
-            tma_load_2d(Ystage + s * ystage_bytes, &tmY, &y_full[s], PANEL_ELEMS * pn,
-                        piece * p.Kpad + c * P1_BK);
+            const int c = it >> 1, piece = it & 1;
+            mbar_expect_tx(&y_full[q], (uint32_t) SLOT_BYTES);
+#pragma unroll
+            for (int pn = 0; pn < NP; pn++)
+                tma_load_2d(Yslot + q * SLOT_BYTES + pn * PANEL_BYTES, &tmY, &y_full[q],
+                            PANEL_ELEMS * pn, piece * p.Kpad + c * P1_BK);
+            if (++q == nslot) {
+                q = 0;
+                ph ^= 1u;
+            }
         }
-    } else if (warp == 1 && lane == 0) {
-        // ---------------- MMA issuer ----------------
+    } else if (warp == 1) {
+        // ---------------- MMA issuer (whole warp; one elected lane issues) ----------------
         const uint32_t idesc = idesc_bf16(P1_TILE, P1_BK, 0, 0);
-        bool ok = mbar_wait(t_full, 0, p.status, 12);
-        int it = 0;
+        const uint64_t ydesc0 = sdesc_sw128(smem_u32(Yslot), 16, 1024);
+        bool ok = mbar_wait_w(a_ready, 0, p.status, 12);
+        int q0 = 0;
+        uint32_t ph0 = 0;
         for (int c = 0; ok && c < p.nchunk; c++) {
-            const int b = c & 1, use = c >> 1;
-            for (int i = 0; i < p.ntile && use > 0; i++)
-                if (!mbar_wait(&acc_empty[i * 2 + b], (use - 1) & 1, p.status, 13)) {
-                    ok = false;
-                    break;
-                }
-            if (!ok)
-                break;
-            tc_fence_after();
-            uint32_t acc0 = 0, acc1 = 0;
-            for (int r = 0; r < per_chunk; r++, it++) {
-                const int s = it % p.nstage;
-                if (!mbar_wait(&y_full[s], (it / p.nstage) & 1, p.status, 14)) {
+            int q = q0;
+            uint32_t ph = ph0;
+#pragma unroll
+            for (int g = 0; g < NTILE; g++) {
+                const int rg = region(g, c), use = ruse(c);
+                if (use > 0 && !mbar_wait_w(&acc_empty[rg], (use - 1) & 1, p.status, 13)) {
                     ok = false;
                     break;
                 }
                 tc_fence_after();
-                const int piece = r / p.npanel, pn = r % p.npanel;
-                const uint64_t bd0 = sdesc_sw128(smem_u32(Ystage + s * ystage_bytes), 16, 1024);
-                // Y_hi pairs with T_hi (and T_lo when T is split); Y_lo with T_hi
-                const int ntp = (piece == 0) ? p.nT : 1;
-                for (int i = 0; i < p.ntile; i++) {
-                    const uint32_t d_tmem = tmem + (uint32_t) ((i * 2 + b) * P1_BK);
-                    uint32_t &acc = (i == 0) ? acc0 : acc1;
-                    for (int tp = 0; tp < ntp; tp++) {
-                        const uint64_t ad0 = sdesc_sw128(
-                            smem_u32(Ts + ((i * p.nT + tp) * p.npanel + pn) * tpanel_bytes), 16, 1024);
+                const uint32_t d_tmem = tmem + (uint32_t) (P1_ACC_COL + rg * P1_BK);
+                const uint32_t a_tile = tmem + (uint32_t) (g * NT * ACOL);
+                q = q0;
+                ph = ph0;
 #pragma unroll
-                        for (int kk = 0; kk < 4; kk++) {
-                            mma_ss(d_tmem, ad0 + 2 * kk, bd0 + 2 * kk, idesc, acc);
-                            acc = 1;
+                for (int piece = 0; piece < 2; piece++) {
+                    if (g == 0) {
+                        if (!mbar_wait_w(&y_full[q], ph, p.status, 14)) {
+                            ok = false;
+                            break;
+                        }
+                        tc_fence_after();
+                    }
+                    const uint64_t bd = ydesc0 + (uint64_t) (q * (SLOT_BYTES >> 4));
+                    // Y_hi pairs with T_hi (and T_lo when T is split); Y_lo with T_hi
+#pragma unroll
+                    for (int pn = 0; pn < NP; pn++) {
+#pragma unroll
+                        for (int tp = 0; tp < (piece == 0 ? NT : 1); tp++) {
+#pragma unroll
+                            for (int kk = 0; kk < (pn == NP - 1 ? KL : 4); kk++)
+                                mma_ts_w(d_tmem, a_tile + (uint32_t) (tp * ACOL + pn * 32 + kk * 8),
+                                         bd + (uint64_t) (pn * (PANEL_BYTES >> 4) + 2 * kk), idesc,
+                                         (piece | pn | tp | kk) ? 1u : 0u);
                         }
                     }
+                    if (g == NTILE - 1)
+                        mma_commit_w(&y_empty[q]);
+                    if (++q == nslot) {
+                        q = 0;
+                        ph ^= 1u;
+                    }
                 }
-                mma_commit(&y_empty[s]);
+                if (!ok)
+                    break;
+                mma_commit_w(&acc_full[rg]);
             }
-            if (!ok)
-                break;
-            for (int i = 0; i < p.ntile; i++)
-                mma_commit(&acc_full[i * 2 + b]);
+            q0 = q;
+            ph0 = ph;
         }
         if (!ok)
             failed = 1;
@@ -213,101 +235,120 @@ __global__ void __launch_bounds__(P1_THREADS, 1)
         const int g = (warp - 2) >> 2;
         const int row = q * 32 + lane;
         const uint32_t lane_base = tmem + ((uint32_t) (q * 32) << 16);
+        const int prow = g * P1_TILE + row;
+        const int n = n0 + prow;
         double t1 = 0.0, t2 = 0.0;
         bool ok = true;
-        if (g < p.ntile) {
+        if (g < NTILE) {
+            // this thread's data row into tensor memory (A operand): column j of
+            // piece tp holds depths 2j (low half) and 2j + 1
+            for (int tp = 0; tp < NT; tp++) {
+                const uint4 *src = (const uint4 *) (p.Tb + ((size_t) tp * p.Npad + n) * ACOL);
+                for (int c0 = 0; c0 < ACOL; c0 += 16) {
+                    uint32_t v[16];
+#pragma unroll
+                    for (int j = 0; j < 4; j++) {
+                        const uint4 w = src[c0 / 4 + j];
+                        v[4 * j] = w.x;
+                        v[4 * j + 1] = w.y;
+                        v[4 * j + 2] = w.z;
+                        v[4 * j + 3] = w.w;
+                    }
+                    tmem_st16(lane_base + (uint32_t) ((g * NT + tp) * ACOL + c0), v);
+                }
+            }
+            tmem_st_wait();
+            tc_fence_before();
+            mbar_arrive(a_ready);
+
             float m = -INFINITY;
             int kstar = 0;
             double s1 = 0.0, s2 = 0.0;
             for (int c = 0; c < p.nchunk; c++) {
-                const int b = c & 1;
-                if (!mbar_wait(&acc_full[g * 2 + b], (c >> 1) & 1, p.status, 15)) {
+                const int rg = region(g, c);
+                if (!mbar_wait(&acc_full[rg], ruse(c) & 1, p.status, 15)) {
                     ok = false;
                     break;
                 }
                 tc_fence_after();
-#pragma unroll 1
-                for (int sub = 0; sub < 2; sub++) {
-                    uint32_t va[32], vb[32];
-                    const uint32_t col = (uint32_t) ((g * 2 + b) * P1_BK + sub * 64);
-                    tmem_ld32(lane_base + col, va);
-                    tmem_ld32(lane_base + col + 32, vb);
+                // copy the whole chunk out and hand the accumulator back at
+                // once, so the next chunk's MMAs overlap this arithmetic
+                uint32_t v[P1_BK];
+                {
+                    const uint32_t col = lane_base + (uint32_t) (P1_ACC_COL + rg * P1_BK);
+                    tmem_ld32p(col, v);
+                    tmem_ld32p(col + 32, v + 32);
+                    tmem_ld32p(col + 64, v + 64);
+                    tmem_ld32p(col + 96, v + 96);
                     tmem_ld_wait();
-                    float mx0 = -INFINITY, mx1 = -INFINITY;
-#pragma unroll
-                    for (int j = 0; j < 32; j++) {
-                        mx0 = fmaxf(mx0, __uint_as_float(va[j]));
-                        mx1 = fmaxf(mx1, __uint_as_float(vb[j]));
-                    }
-                    const float mx = fmaxf(mx0, mx1);
-                    if (mx > m) {
-                        if (m > -INFINITY) {
-                            s1 *= (double) ex2((m - mx) * p.c1l);
-                            s2 *= (double) ex2((m - mx) * p.c2l);
-                        }
-                        int j0 = 64;
-#pragma unroll
-                        for (int j = 31; j >= 0; j--) {
-                            if (__uint_as_float(vb[j]) == mx)
-                                j0 = 32 + j;
-                        }
-#pragma unroll
-                        for (int j = 31; j >= 0; j--) {
-                            if (__uint_as_float(va[j]) == mx)
-                                j0 = j;
-                        }
-                        m = mx;
-                        kstar = c * P1_BK + sub * 64 + j0;
-                    }
-                    // four independent accumulation chains per sum
-                    float e1[4] = {0.f, 0.f, 0.f, 0.f}, e2[4] = {0.f, 0.f, 0.f, 0.f};
-                    if (p.two_temps) {
-#pragma unroll
-                        for (int j = 0; j < 32; j += 2) {
-                            const float xa0 = __uint_as_float(va[j]) - m, xa1 = __uint_as_float(va[j + 1]) - m;
-                            const float xb0 = __uint_as_float(vb[j]) - m, xb1 = __uint_as_float(vb[j + 1]) - m;
-                            e1[0] += ex2(xa0 * p.c1l);
-                            e1[1] += ex2(xa1 * p.c1l);
-                            e1[2] += ex2(xb0 * p.c1l);
-                            e1[3] += ex2(xb1 * p.c1l);
-                            e2[0] += ex2(xa0 * p.c2l);
-                            e2[1] += ex2(xa1 * p.c2l);
-                            e2[2] += ex2(xb0 * p.c2l);
-                            e2[3] += ex2(xb1 * p.c2l);
-                        }
-                    } else {
-#pragma unroll
-                        for (int j = 0; j < 32; j += 2) {
-                            e1[0] += ex2((__uint_as_float(va[j]) - m) * p.c1l);
-                            e1[1] += ex2((__uint_as_float(va[j + 1]) - m) * p.c1l);
-                            e1[2] += ex2((__uint_as_float(vb[j]) - m) * p.c1l);
-                            e1[3] += ex2((__uint_as_float(vb[j + 1]) - m) * p.c1l);
-                        }
-                    }
-                    s1 += (double) ((e1[0] + e1[1]) + (e1[2] + e1[3]));
-                    s2 += (double) ((e2[0] + e2[1]) + (e2[2] + e2[3]));
                 }
                 tc_fence_before();
-                mbar_arrive(&acc_empty[g * 2 + b]);
+                mbar_arrive(&acc_empty[rg]);
+                float mxq[4] = {-INFINITY, -INFINITY, -INFINITY, -INFINITY};
+#pragma unroll
+                for (int j = 0; j < P1_BK; j += 4) {
+                    mxq[0] = fmaxf(mxq[0], __uint_as_float(v[j]));
+                    mxq[1] = fmaxf(mxq[1], __uint_as_float(v[j + 1]));
+                    mxq[2] = fmaxf(mxq[2], __uint_as_float(v[j + 2]));
+                    mxq[3] = fmaxf(mxq[3], __uint_as_float(v[j + 3]));
+                }
+                const float mx = fmaxf(fmaxf(mxq[0], mxq[1]), fmaxf(mxq[2], mxq[3]));
+                if (mx > m) {
+                    if (m > -INFINITY) {
+                        s1 *= (double) ex2((m - mx) * p.c1l);
+                        s2 *= (double) ex2((m - mx) * p.c2l);
+                    }
+                    int j0 = P1_BK;
+#pragma unroll
+                    for (int j = P1_BK - 1; j >= 0; j--) {
+                        if (__uint_as_float(v[j]) == mx)
+                            j0 = j;
+                    }
+                    m = mx;
+                    kstar = c * P1_BK + j0;
+                }
+                // four independent accumulation chains per sum
+                float e1[4] = {0.f, 0.f, 0.f, 0.f}, e2[4] = {0.f, 0.f, 0.f, 0.f};
+                if (p.two_temps) {
+#pragma unroll
+                    for (int j = 0; j < P1_BK; j += 4) {
+#pragma unroll
+                        for (int u = 0; u < 4; u++) {
+                            const float x = __uint_as_float(v[j + u]) - m;
+                            e1[u] += ex2(x * p.c1l);
+                            e2[u] += ex2(x * p.c2l);
+                        }
+                    }
+                } else {
+#pragma unroll
+                    for (int j = 0; j < P1_BK; j += 4) {
+#pragma unroll
+                        for (int u = 0; u < 4; u++)
+                            e1[u] += ex2((__uint_as_float(v[j + u]) - m) * p.c1l);
+                    }
+                }
+                s1 += (double) ((e1[0] + e1[1]) + (e1[2] + e1[3]));
+                s2 += (double) ((e2[0] + e2[1]) + (e2[2] + e2[3]));
             }
             if (!p.two_temps)
                 s2 = s1;
             // exact (FP32) distance to the best centre, from the unsplit centre
             // and the data, then the per-point terms
-            const int prow = g * P1_TILE + row;
-            const int n = n0 + prow;
-            if (ok && !mbar_wait(t_full, 0, p.status, 17))
-                ok = false;
             if (ok && n < p.N) {
                 const int k = min(kstar, p.K - 1);
                 const float *yk = p.Y32 + (size_t) k * p.D;
                 float dsum = 0.f;
-                if (p.nT == 1) {
-                    // the data are exact in BF16: read them from the resident tile
-                    const unsigned char *tile = Ts + g * p.npanel * tpanel_bytes;
-                    for (int d = 0; d < p.D; d++) {
-                        const float df = yk[d] - bf16_at(tile + (d >> 6) * tpanel_bytes, row, d & 63);
-                        dsum = fmaf(df, df, dsum);
+                if (NT == 1) {
+                    // the data are exact in BF16
+                    const uint32_t *tr = p.Tb + (size_t) n * ACOL;
+                    for (int d = 0; d < p.D; d += 2) {
+                        const uint32_t w = tr[d / 2];
+                        const float df0 = yk[d] - __uint_as_float(w << 16);
+                        dsum = fmaf(df0, df0, dsum);
+                        if (d + 1 < p.D) {
+                            const float df1 = yk[d + 1] - __uint_as_float(w & 0xFFFF0000u);
+                            dsum = fmaf(df1, df1, dsum);
+                        }
                     }
                 } else {
                     const double *tn = p.T64 + (size_t) n * p.D;
@@ -350,17 +391,17 @@ __global__ void __launch_bounds__(P1_THREADS, 1)
     __syncthreads();
     if (threadIdx.x == 0) {
         double a = 0.0, b2 = 0.0;
-        for (int i = 0; i < p.ntile * P1_TILE; i++) {
+        for (int i = 0; i < NTILE * P1_TILE; i++) {
             a += red[i];
             b2 += red[256 + i];
         }
         p.part[2 * blockIdx.x] = a;
         p.part[2 * blockIdx.x + 1] = b2;
     }
-    if (failed && warp == 1 && lane == 0) {
+    if (failed && warp == 1) {
         // let every issued MMA finish before the accumulators are released
-        mma_commit(drain);
-        mbar_wait(drain, 0, p.status, 16, 100000000ull);
+        mma_commit_w(drain);
+        mbar_wait_w(drain, 0, p.status, 16, 100000000ull);
     }
     tc_fence_before();
     __syncthreads();
@@ -374,6 +415,7 @@ __global__ void __launch_bounds__(P1_THREADS, 1)
 // ---------------------------------------------------------------------------
 struct P2Params {
     int D, Dp, npanel, nT, Npad, Kpad, bn, ntiles, units_per_k, ktiles, nunits, nstage;
+    int ksteps;           // 16-deep steps of the distance product (D + 3 used columns)
     const float4 *colq;   // Npad
     float *RTpart;        // nunits x 128 x Dp
     int *status;
@@ -486,7 +528,7 @@ __global__ void __launch_bounds__(P2_THREADS, 1)
         }
         if (!ok)
             failed = 1;
-    } else if (warp == 1 && lane == 0) {
+    } else if (warp == 1) {
         // ---------------- MMA issuer ----------------
         const uint32_t id1 = idesc_bf16(P2_BK, bn, 0, 0);
         const uint32_t id2 = idesc_bf16(P2_BK, p.Dp, 0, 1);
@@ -497,8 +539,8 @@ __global__ void __launch_bounds__(P2_THREADS, 1)
             unit_of(p, v, u, kt, t0, t1);
             if (kt != cur_kt) {
                 if (yuse > 0)
-                    mma_commit(y_empty);
-                if (!mbar_wait(y_full, yuse & 1, p.status, 23)) {
+                    mma_commit_w(y_empty);
+                if (!mbar_wait_w(y_full, yuse & 1, p.status, 23)) {
                     ok = false;
                     break;
                 }
@@ -511,7 +553,7 @@ __global__ void __launch_bounds__(P2_THREADS, 1)
                 if (t < t1) {
                     // distances of tile jt: M = 128 centres, N = bn points
                     const int s = jt % p.nstage, b = jt & 1;
-                    if (!mbar_wait(&t_full[s], (jt / p.nstage) & 1, p.status, 24)) {
+                    if (!mbar_wait_w(&t_full[s], (jt / p.nstage) & 1, p.status, 24)) {
                         ok = false;
                         break;
                     }
@@ -524,29 +566,32 @@ __global__ void __launch_bounds__(P2_THREADS, 1)
                         for (int pn = 0; pn < p.npanel; pn++) {
                             const uint64_t ad0 = sdesc_sw128(
                                 smem_u32(Ys + (piece * p.npanel + pn) * ypanel_bytes), 16, 1024);
+                            const int kmax = min(4, p.ksteps - 4 * pn);  // skip all-zero steps
                             for (int tp = 0; tp < ntp; tp++) {
                                 const uint64_t bd0 = sdesc_sw128(
                                     tst + (tp * p.npanel + pn) * tpanel_bytes, 16, 1024);
 #pragma unroll
                                 for (int kk = 0; kk < 4; kk++) {
-                                    mma_ss(d, ad0 + 2 * kk, bd0 + 2 * kk, id1, acc);
-                                    acc = 1;
+                                    if (kk < kmax) {
+                                        mma_ss_w(d, ad0 + 2 * kk, bd0 + 2 * kk, id1, acc);
+                                        acc = 1;
+                                    }
                                 }
                             }
                         }
                     }
-                    mma_commit(&s_full[b]);
+                    mma_commit_w(&s_full[b]);
                 }
                 if (t > t0) {
                     // R T of the previous tile: A = R (TMEM), B = the same T tile, MN-major
                     const int j = jt - 1;
                     const int s = j % p.nstage, b = j & 1;
                     if (j == first_j && nunit > 0 &&
-                        !mbar_wait(rt_empty, (nunit - 1) & 1, p.status, 25)) {
+                        !mbar_wait_w(rt_empty, (nunit - 1) & 1, p.status, 25)) {
                         ok = false;
                         break;
                     }
-                    if (!mbar_wait(&p_full[b], (j >> 1) & 1, p.status, 26)) {
+                    if (!mbar_wait_w(&p_full[b], (j >> 1) & 1, p.status, 26)) {
                         ok = false;
                         break;
                     }
@@ -560,19 +605,19 @@ __global__ void __launch_bounds__(P2_THREADS, 1)
                             for (int kk = 0; kk < bn / 16; kk++) {
                                 const uint32_t a = tmem + (uint32_t) (b * bn + (kk >> 2) * 64 +
                                                                       rp * 32 + (kk & 3) * 8);
-                                mma_ts(rt_tmem, a, bd0 + (uint64_t) (kk * (2048 >> 4)), id2, rt_acc);
+                                mma_ts_w(rt_tmem, a, bd0 + (uint64_t) (kk * (2048 >> 4)), id2, rt_acc);
                                 rt_acc = 1;
                             }
                         }
                     }
-                    mma_commit(&t_empty[s]);
+                    mma_commit_w(&t_empty[s]);
                 }
                 if (t < t1)
                     jt++;
             }
             if (!ok)
                 break;
-            mma_commit(rt_full);
+            mma_commit_w(rt_full);
             nunit++;
         }
         if (!ok)
@@ -673,9 +718,9 @@ __global__ void __launch_bounds__(P2_THREADS, 1)
         }
     }
     __syncthreads();
-    if (failed && warp == 1 && lane == 0) {
-        mma_commit(drain);
-        mbar_wait(drain, 0, p.status, 30, 100000000ull);
+    if (failed && warp == 1) {
+        mma_commit_w(drain);
+        mbar_wait_w(drain, 0, p.status, 30, 100000000ull);
     }
     tc_fence_before();
     __syncthreads();
@@ -791,14 +836,30 @@ __global__ void slot_reduce_kernel(const float *__restrict__ RTpart, int K, int 
     }
 }
 
+using P1Kernel = void (*)(const CUtensorMap, const P1Params);
+
+// the pass-1 instantiation for a shape (NP panels, KL steps in the last, NT pieces)
+P1Kernel pass1_for(int np, int kl, int nt)
+{
+#define DGTM_P1(NP_, KL_, NT_) \
+    if (np == NP_ && kl == KL_ && nt == NT_) return tc_pass1_kernel<NP_, KL_, NT_>;
+#define DGTM_P1_KL(NP_, NT_) DGTM_P1(NP_, 1, NT_) DGTM_P1(NP_, 2, NT_) DGTM_P1(NP_, 3, NT_) DGTM_P1(NP_, 4, NT_)
+    DGTM_P1_KL(1, 1) DGTM_P1_KL(1, 2) DGTM_P1_KL(2, 1) DGTM_P1_KL(2, 2)
+    DGTM_P1_KL(3, 1) DGTM_P1_KL(3, 2) DGTM_P1_KL(4, 1) DGTM_P1_KL(4, 2)
+#undef DGTM_P1_KL
+#undef DGTM_P1
+    return nullptr;
+}
+
 }  // namespace
 
 struct TcState {
     int N, D, K, sms;
-    int Dp, npanel, Npad, Kpad, nT;
+    int Dp, npanel, Npad, Kpad, nT, ksteps;
     int nchunk, nstage1, nstage2, ntile1, bn2;
     int ntiles2, units_per_k, nunits, grid2;
     size_t smem1, smem2;
+    P1Kernel pass1;
     __nv_bfloat16 *Tb, *Yb;
     float *Y32;
     float4 *colq;
@@ -842,6 +903,7 @@ int tc_create(TcState **out, int N, int D, int K, int sms, const double *T64, co
     st->T64 = T64;
     st->Dp = round_up(D + 3, PANEL_ELEMS);
     st->npanel = st->Dp / PANEL_ELEMS;
+    st->ksteps = (D + 3 + 15) / 16;  // columns D + 3 .. Dp - 1 are zero in both operands
     st->Npad = round_up(N, NPAD_ALIGN);
     st->Kpad = round_up(K, P1_BK);
     st->nchunk = st->Kpad / P1_BK;
@@ -912,24 +974,27 @@ int tc_create(TcState **out, int N, int D, int K, int sms, const double *T64, co
         return fail(rc);
     // shared memory plans
     const size_t bar_bytes = 64 * 8 + 16 + 2 * 256 * 8;
-    const size_t t1 = (size_t) st->ntile1 * st->nT * st->npanel * P1_TILE * 128;
-    int ns1 = (int) ((SMEM_LIMIT - 1024 - bar_bytes - t1) / (P1_BK * 128));
-    if (ns1 > 8)
-        ns1 = 8;
+    // pass 1: Y slots of one chunk piece (npanel panels of 16 KB); the data
+    // tiles live in tensor memory
+    const size_t slot1 = (size_t) st->npanel * P1_BK * 128;
+    int ns1 = (int) ((SMEM_LIMIT - 1024 - bar_bytes) / slot1);
+    if (ns1 > 12)
+        ns1 = 12;
+    st->pass1 = pass1_for(st->npanel, st->ksteps - 4 * (st->npanel - 1), st->nT);
     const size_t y2 = (size_t) 2 * st->npanel * P2_BK * 128;
     const size_t ts2 = (size_t) st->nT * st->npanel * st->bn2 * 128 + st->bn2 * 16;
     int ns2 = (int) ((SMEM_LIMIT - 1024 - bar_bytes - y2) / ts2);
     if (ns2 > 4)
         ns2 = 4;
-    if (ns1 < 3 || ns2 < 2) {
+    if (ns1 < 2 || ns2 < 2 || !st->pass1) {
         set_error(DGTM_ENOTSUP, "the split-BF16 form does not fit shared memory (D = %d)", D);
         return fail(DGTM_ENOTSUP);
     }
     st->nstage1 = ns1;
     st->nstage2 = ns2;
-    st->smem1 = 1024 + t1 + (size_t) ns1 * P1_BK * 128 + bar_bytes;
+    st->smem1 = 1024 + (size_t) ns1 * slot1 + bar_bytes;
     st->smem2 = 1024 + y2 + (size_t) ns2 * ts2 + bar_bytes;
-    e = cudaFuncSetAttribute(tc_pass1_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    e = cudaFuncSetAttribute(st->pass1, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int) st->smem1);
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(tc_pass2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -982,6 +1047,7 @@ int tc_estep(TcState *st, const double *, double c1, double c2, int isDA, double
     p.nchunk = st->nchunk;
     p.nstage = st->nstage1;
     p.ntile = st->ntile1;
+    p.ksteps = st->ksteps;
     p.c1 = c1;
     p.c2 = c2;
     p.c1l = (float) (2.0 * c1 * 1.4426950408889634);
@@ -990,12 +1056,13 @@ int tc_estep(TcState *st, const double *, double c1, double c2, int isDA, double
     p.two_temps = isDA && (c1 != c2);
     p.Y32 = st->Y32;
     p.T64 = st->T64;
+    p.Tb = (const uint32_t *) st->Tb;
     p.colstat = colstat;
     p.colq = st->colq;
     p.part = part;
     p.status = st->status;
     DGTM_CUDA_TRY(cudaMemsetAsync(st->status, 0, sizeof(int), s));
-    tc_pass1_kernel<<<tc_pass1_blocks(st), P1_THREADS, st->smem1, s>>>(st->tmT1, st->tmY1, p);
+    st->pass1<<<tc_pass1_blocks(st), P1_THREADS, st->smem1, s>>>(st->tmY1, p);
     DGTM_CUDA_TRY(cudaGetLastError());
     *nlaunch = 1;
     return DGTM_OK;
@@ -1016,6 +1083,7 @@ int tc_mstep_pass(TcState *st, const double2 *, double, cudaStream_t s, int *nla
     p.ktiles = (st->K + P2_BK - 1) / P2_BK;
     p.nunits = st->nunits;
     p.nstage = st->nstage2;
+    p.ksteps = st->ksteps;
     p.colq = st->colq;
     p.RTpart = st->RTpart;
     p.status = st->status;
