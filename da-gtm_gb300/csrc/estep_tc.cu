@@ -414,12 +414,14 @@ __global__ void __launch_bounds__(P1_THREADS, 1)
 // pass 2
 // ---------------------------------------------------------------------------
 struct P2Params {
-    int D, Dp, npanel, nT, Npad, Kpad, bn, ntiles, units_per_k, ktiles, nunits, nstage;
-    int ksteps;           // 16-deep steps of the distance product (D + 3 used columns)
+    int D, Dp, Npad, Kpad, ntiles, units_per_k, ktiles, nunits, nstage;
+    const uint32_t *Yb;   // 2 x Kpad x Dp BF16 (as BF16 pairs): the centre pieces
     const float4 *colq;   // Npad
     float *RTpart;        // nunits x 128 x Dp
     int *status;
 };
+
+constexpr int P2_TILE = 64;  // points per tile (MMA N of the distance product)
 
 // The CTAs take units v = blockIdx.x, blockIdx.x + gridDim.x, ... in point-
 // major order, so at any time all CTAs stream the same few point tiles (which
@@ -430,35 +432,46 @@ __device__ __forceinline__ void unit_of(const P2Params &p, int v, int &u, int &k
     const int nu = v / p.ktiles;
     kt = v % p.ktiles;
     u = kt * p.units_per_k + nu;
-    const int per_unit = P2_UNIT_POINTS / p.bn;
+    constexpr int per_unit = P2_UNIT_POINTS / P2_TILE;
     t0 = nu * per_unit;
     t1 = min(p.ntiles, t0 + per_unit);
 }
 
+// Pass 2, a template on the operand shape like pass 1.  Tensor memory holds
+// the unit's R T accumulator (columns 0 .. Dp-1), two 64-point buffers in
+// which the distance accumulator S is turned into R (BF16 hi/lo), and the
+// unit's 128 centres (Y hi, Y lo) as the A operand of the distance product,
+// so shared memory is left to a deep ring of point tiles.  Per 64-point tile:
+// MMA 1 (A = Y from tensor memory, B = T tile, N = 64) gives S; eight warps
+// (two 32-point groups x four lane quarters) form R and write it over S; MMA 2
+// (A = R from tensor memory, B = the same T tile read MN-major, N = Dp)
+// accumulates R T.  At a unit boundary the same warps drain R T to the
+// unit's slot and load the next unit's centres into tensor memory.
+template <int NP, int KL, int NT>
 __global__ void __launch_bounds__(P2_THREADS, 1)
-    tc_pass2_kernel(const __grid_constant__ CUtensorMap tmT, const __grid_constant__ CUtensorMap tmY,
-                    const P2Params p)
+    tc_pass2_kernel(const __grid_constant__ CUtensorMap tmT, const P2Params p)
 {
+    constexpr int KS = 4 * (NP - 1) + KL;               // 16-deep steps of the distance product
+    constexpr int DP = NP * PANEL_ELEMS;
+    constexpr int YCOLS = (KS * 8 + 15) / 16 * 16;      // TMEM columns of one Y piece
+    constexpr int SP_COL = DP;                          // S / P buffers: 2 x 64 columns
+    constexpr int Y_COL = DP + 2 * P2_TILE;             // Y hi, then Y lo
+    static_assert(Y_COL + 2 * YCOLS <= 512, "pass 2 tensor memory plan");
+    constexpr int TPANEL_BYTES = P2_TILE * 128;         // 8 KB
+    constexpr int TSTAGE_BYTES = NT * NP * TPANEL_BYTES;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char *base = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
-    const int bn = p.bn;                                   // points per tile: 64 or 128
-    const int ng = bn / 64;                                // active responsibility groups
-    const int ypanel_bytes = P2_BK * 128;                  // 16 KB
-    const int tpanel_bytes = bn * 128;
-    const int tstage_bytes = p.nT * p.npanel * tpanel_bytes;
-    unsigned char *Ys = base;                               // 2 x npanel panels
-    unsigned char *Tst = base + 2 * p.npanel * ypanel_bytes;
-    float4 *cq = (float4 *) (Tst + p.nstage * tstage_bytes); // nstage x bn
-    uint64_t *bars = (uint64_t *) (cq + p.nstage * bn);
+    const int nstage = p.nstage;
+    unsigned char *Tst = base;
+    float4 *cq = (float4 *) (Tst + nstage * TSTAGE_BYTES);  // nstage x 64
+    uint64_t *bars = (uint64_t *) (cq + nstage * P2_TILE);
     uint64_t *t_full = bars;
-    uint64_t *t_empty = bars + p.nstage;
-    uint64_t *y_full = bars + 2 * p.nstage;
-    uint64_t *y_empty = y_full + 1;
-    uint64_t *s_full = y_empty + 1;   // 2
-    uint64_t *p_full = s_full + 2;    // 2
+    uint64_t *t_empty = bars + nstage;
+    uint64_t *s_full = bars + 2 * nstage;  // 2
+    uint64_t *p_full = s_full + 2;         // 2
     uint64_t *rt_full = p_full + 2;
-    uint64_t *rt_empty = rt_full + 1;
-    uint64_t *drain = rt_empty + 1;
+    uint64_t *y_ready = rt_full + 1;       // centres loaded and R T drained
+    uint64_t *drain = y_ready + 1;
     uint32_t *tmem_sh = (uint32_t *) (drain + 1);
     __shared__ int failed;
 
@@ -466,18 +479,16 @@ __global__ void __launch_bounds__(P2_THREADS, 1)
 
     if (threadIdx.x == 0) {
         failed = 0;
-        for (int s = 0; s < p.nstage; s++) {
+        for (int s = 0; s < nstage; s++) {
             mbar_init(&t_full[s], 1);
             mbar_init(&t_empty[s], 1);
         }
-        mbar_init(y_full, 1);
-        mbar_init(y_empty, 1);
         for (int b = 0; b < 2; b++) {
             mbar_init(&s_full[b], 1);
-            mbar_init(&p_full[b], 128 * ng);
+            mbar_init(&p_full[b], 256);
         }
         mbar_init(rt_full, 1);
-        mbar_init(rt_empty, 128 * ng);
+        mbar_init(y_ready, 256);
         mbar_init(drain, 1);
         fence_barrier_init();
     }
@@ -487,133 +498,119 @@ __global__ void __launch_bounds__(P2_THREADS, 1)
     }
     __syncthreads();
     tc_fence_after();
-    const uint32_t tmem = *tmem_sh;
-    const uint32_t rt_tmem = tmem + 256;
+    const uint32_t tmem = __shfl_sync(0xffffffffu, *tmem_sh, 0);
 
     if (warp == 0 && lane == 0) {
-        // ---------------- producer ----------------
+        // ---------------- producer: point tiles and their column statistics ----------------
         prefetch_tmap(&tmT);
-        prefetch_tmap(&tmY);
-        int jt = 0, cur_kt = -1, yuse = 0;
+        int s = 0;
+        uint32_t ph = 0;
+        int jt = 0;
         bool ok = true;
         for (int v = blockIdx.x; ok && v < p.nunits; v += gridDim.x) {
             int u, kt, t0, t1;
             unit_of(p, v, u, kt, t0, t1);
-            if (kt != cur_kt) {
-                if (yuse > 0 && !mbar_wait(y_empty, (yuse - 1) & 1, p.status, 21)) {
-                    ok = false;
-                    break;
-                }
-                mbar_expect_tx(y_full, (uint32_t) (2 * p.npanel * ypanel_bytes));
-                for (int piece = 0; piece < 2; piece++)
-                    for (int pn = 0; pn < p.npanel; pn++)
-                        tma_load_2d(Ys + (piece * p.npanel + pn) * ypanel_bytes, &tmY, y_full,
-                                    PANEL_ELEMS * pn, piece * p.Kpad + kt * P2_BK);
-                yuse++;
-                cur_kt = kt;
-            }
             for (int t = t0; t < t1; t++, jt++) {
-                const int s = jt % p.nstage, use = jt / p.nstage;
-                if (use > 0 && !mbar_wait(&t_empty[s], (use - 1) & 1, p.status, 22)) {
+                if (jt >= nstage && !mbar_wait(&t_empty[s], ph ^ 1u, p.status, 22)) {
                     ok = false;
                     break;
                 }
-                mbar_expect_tx(&t_full[s], (uint32_t) (tstage_bytes + bn * 16));
-                for (int tp = 0; tp < p.nT; tp++)
-                    for (int pn = 0; pn < p.npanel; pn++)
-                        tma_load_2d(Tst + s * tstage_bytes + (tp * p.npanel + pn) * tpanel_bytes,
-                                    &tmT, &t_full[s], PANEL_ELEMS * pn, tp * p.Npad + t * bn);
-                bulk_load(cq + s * bn, p.colq + (size_t) t * bn, (uint32_t) (bn * 16), &t_full[s]);
+                mbar_expect_tx(&t_full[s], (uint32_t) (TSTAGE_BYTES + P2_TILE * 16));
+#pragma unroll
+                for (int tp = 0; tp < NT; tp++)
+#pragma unroll
+                    for (int pn = 0; pn < NP; pn++)
+                        tma_load_2d(Tst + s * TSTAGE_BYTES + (tp * NP + pn) * TPANEL_BYTES, &tmT,
+                                    &t_full[s], PANEL_ELEMS * pn, tp * p.Npad + t * P2_TILE);
+                bulk_load(cq + s * P2_TILE, p.colq + (size_t) t * P2_TILE, (uint32_t) (P2_TILE * 16),
+                          &t_full[s]);
+                if (++s == nstage) {
+                    s = 0;
+                    ph ^= 1u;
+                }
             }
         }
         if (!ok)
             failed = 1;
     } else if (warp == 1) {
-        // ---------------- MMA issuer ----------------
-        const uint32_t id1 = idesc_bf16(P2_BK, bn, 0, 0);
-        const uint32_t id2 = idesc_bf16(P2_BK, p.Dp, 0, 1);
-        int jt = 0, cur_kt = -1, yuse = 0, nunit = 0;
+        // ---------------- MMA issuer (whole warp; one elected lane issues) ----------------
+        const uint32_t id1 = idesc_bf16(P2_BK, P2_TILE, 0, 0);
+        const uint32_t id2 = idesc_bf16(P2_BK, DP, 0, 1);
+        const uint64_t tdesc_k = sdesc_sw128(smem_u32(Tst), 16, 1024);            // K-major (MMA 1)
+        const uint64_t tdesc_mn = sdesc_sw128(smem_u32(Tst), TPANEL_BYTES, 1024); // MN-major (MMA 2)
+        const uint32_t rt_tmem = tmem;
+        int jt = 0, s = 0, nunit = 0;
+        uint32_t ph = 0;
+        int sp = 0;  // stage of the tile awaiting MMA 2
         bool ok = true;
         for (int v = blockIdx.x; ok && v < p.nunits; v += gridDim.x) {
             int u, kt, t0, t1;
             unit_of(p, v, u, kt, t0, t1);
-            if (kt != cur_kt) {
-                if (yuse > 0)
-                    mma_commit_w(y_empty);
-                if (!mbar_wait_w(y_full, yuse & 1, p.status, 23)) {
-                    ok = false;
-                    break;
-                }
-                yuse++;
-                cur_kt = kt;
+            // the unit's centres are in tensor memory and the R T accumulator is free
+            if (!mbar_wait_w(y_ready, nunit & 1, p.status, 23)) {
+                ok = false;
+                break;
             }
-            uint32_t rt_acc = 0;
-            const int first_j = jt;
-            for (int t = t0; t <= t1 && ok; t++) {
+            tc_fence_after();
+            for (int t = t0; t <= t1; t++) {
                 if (t < t1) {
-                    // distances of tile jt: M = 128 centres, N = bn points
-                    const int s = jt % p.nstage, b = jt & 1;
-                    if (!mbar_wait_w(&t_full[s], (jt / p.nstage) & 1, p.status, 24)) {
+                    // S = Y T^T for tile jt: M = 128 centres, N = 64 points
+                    const int b = jt & 1;
+                    if (!mbar_wait_w(&t_full[s], ph, p.status, 24)) {
                         ok = false;
                         break;
                     }
                     tc_fence_after();
-                    const uint32_t d = tmem + (uint32_t) (b * bn);
-                    const uint32_t tst = smem_u32(Tst + s * tstage_bytes);
-                    uint32_t acc = 0;
-                    for (int piece = 0; piece < 2; piece++) {
-                        const int ntp = (piece == 0) ? p.nT : 1;
-                        for (int pn = 0; pn < p.npanel; pn++) {
-                            const uint64_t ad0 = sdesc_sw128(
-                                smem_u32(Ys + (piece * p.npanel + pn) * ypanel_bytes), 16, 1024);
-                            const int kmax = min(4, p.ksteps - 4 * pn);  // skip all-zero steps
-                            for (int tp = 0; tp < ntp; tp++) {
-                                const uint64_t bd0 = sdesc_sw128(
-                                    tst + (tp * p.npanel + pn) * tpanel_bytes, 16, 1024);
+                    const uint32_t d = tmem + (uint32_t) (SP_COL + b * P2_TILE);
+                    const uint64_t bd = tdesc_k + (uint64_t) (s * (TSTAGE_BYTES >> 4));
 #pragma unroll
-                                for (int kk = 0; kk < 4; kk++) {
-                                    if (kk < kmax) {
-                                        mma_ss_w(d, ad0 + 2 * kk, bd0 + 2 * kk, id1, acc);
-                                        acc = 1;
-                                    }
-                                }
-                            }
+                    for (int piece = 0; piece < 2; piece++) {
+#pragma unroll
+                        for (int tp = 0; tp < (piece == 0 ? NT : 1); tp++) {
+#pragma unroll
+                            for (int ks = 0; ks < KS; ks++)
+                                mma_ts_w(d, tmem + (uint32_t) (Y_COL + piece * YCOLS + ks * 8),
+                                         bd + (uint64_t) ((tp * NP + ks / 4) * (TPANEL_BYTES >> 4) +
+                                                          2 * (ks % 4)),
+                                         id1, (piece | tp | ks) ? 1u : 0u);
                         }
                     }
                     mma_commit_w(&s_full[b]);
                 }
                 if (t > t0) {
-                    // R T of the previous tile: A = R (TMEM), B = the same T tile, MN-major
-                    const int j = jt - 1;
-                    const int s = j % p.nstage, b = j & 1;
-                    if (j == first_j && nunit > 0 &&
-                        !mbar_wait_w(rt_empty, (nunit - 1) & 1, p.status, 25)) {
-                        ok = false;
-                        break;
-                    }
-                    if (!mbar_wait_w(&p_full[b], (j >> 1) & 1, p.status, 26)) {
+                    // R T += R (TMEM, hi/lo) x the same T tile, MN-major, N = Dp
+                    const int j = jt - 1, b = j & 1;
+                    if (!mbar_wait_w(&p_full[b], (uint32_t) ((j >> 1) & 1), p.status, 26)) {
                         ok = false;
                         break;
                     }
                     tc_fence_after();
-                    const uint32_t tst = smem_u32(Tst + s * tstage_bytes);
+                    const uint64_t bd = tdesc_mn + (uint64_t) (sp * (TSTAGE_BYTES >> 4));
+                    const uint32_t a0 = tmem + (uint32_t) (SP_COL + b * P2_TILE);
+#pragma unroll
                     for (int rp = 0; rp < 2; rp++) {
-                        const int ntp = (rp == 0) ? p.nT : 1;
-                        for (int tp = 0; tp < ntp; tp++) {
-                            const uint64_t bd0 =
-                                sdesc_sw128(tst + tp * p.npanel * tpanel_bytes, tpanel_bytes, 1024);
-                            for (int kk = 0; kk < bn / 16; kk++) {
-                                const uint32_t a = tmem + (uint32_t) (b * bn + (kk >> 2) * 64 +
-                                                                      rp * 32 + (kk & 3) * 8);
-                                mma_ts_w(rt_tmem, a, bd0 + (uint64_t) (kk * (2048 >> 4)), id2, rt_acc);
-                                rt_acc = 1;
-                            }
+#pragma unroll
+                        for (int tp = 0; tp < (rp == 0 ? NT : 1); tp++) {
+#pragma unroll
+                            for (int kk = 0; kk < P2_TILE / 16; kk++)
+                                // points 16 kk .. 16 kk + 15 belong to group kk / 2, whose
+                                // 32 columns hold R hi (16) then R lo (16)
+                                mma_ts_w(rt_tmem,
+                                         a0 + (uint32_t) ((kk >> 1) * 32 + rp * 16 + (kk & 1) * 8),
+                                         bd + (uint64_t) (tp * NP * (TPANEL_BYTES >> 4) + kk * (2048 >> 4)),
+                                         id2, (t - 1 > t0 || rp | tp | kk) ? 1u : 0u);
                         }
                     }
-                    mma_commit_w(&t_empty[s]);
+                    mma_commit_w(&t_empty[sp]);
                 }
-                if (t < t1)
+                if (t < t1) {
+                    sp = s;
+                    if (++s == nstage) {
+                        s = 0;
+                        ph ^= 1u;
+                    }
                     jt++;
+                }
             }
             if (!ok)
                 break;
@@ -623,85 +620,30 @@ __global__ void __launch_bounds__(P2_THREADS, 1)
         if (!ok)
             failed = 1;
     } else if (warp >= 2) {
-        // ---------------- responsibilities and the R T drain ----------------
-        // group g (warps 2-5 / 6-9) handles points 64 g .. 64 g + 63 of each tile
-        const int q = warp & 3;
-        const int g = (warp - 2) >> 2;
-        const int row = q * 32 + lane;  // centre within the tile
+        // ---------------- responsibilities, the R T drain and the centre loads ----------------
+        const int q = warp & 3;                 // TMEM lane quarter
+        const int g = (warp - 2) >> 2;          // point group: points 32 g .. 32 g + 31 of a tile
+        const int row = q * 32 + lane;          // centre within the tile
         const uint32_t lane_base = tmem + ((uint32_t) (q * 32) << 16);
-        if (g < ng) {
-            int jt = 0, nunit = 0;
-            bool ok = true;
-            for (int v = blockIdx.x; ok && v < p.nunits; v += gridDim.x) {
-                int u, kt, t0, t1;
-                unit_of(p, v, u, kt, t0, t1);
-                for (int t = t0; t < t1; t++, jt++) {
-                    const int s = jt % p.nstage, b = jt & 1;
-                    if (!mbar_wait(&t_full[s], (jt / p.nstage) & 1, p.status, 27) ||
-                        !mbar_wait(&s_full[b], (jt >> 1) & 1, p.status, 28)) {
-                        ok = false;
-                        break;
-                    }
-                    tc_fence_after();
-                    const uint32_t col0 = (uint32_t) (b * bn + g * 64);
-                    uint32_t va[32], vb[32];
-                    tmem_ld32(lane_base + col0, va);
-                    tmem_ld32(lane_base + col0 + 32, vb);
-                    tmem_ld_wait();
-                    const float4 *cqs = cq + s * bn + g * 64;
-                    uint32_t hi[32], lo[32];
-#pragma unroll
-                    for (int j = 0; j < 16; j++) {
-                        float r[4];
-#pragma unroll
-                        for (int e = 0; e < 4; e++) {
-                            const int n = 4 * j + e;  // point within the sub-block
-                            const float a = (n < 32) ? __uint_as_float(va[n]) : __uint_as_float(vb[n - 32]);
-                            const float4 c = cqs[n];
-                            r[e] = ex2(fmaf(a - c.x, c.y, -c.z));
-                        }
-#pragma unroll
-                        for (int e = 0; e < 4; e += 2) {
-                            const uint32_t h = pack_bf16(r[e], r[e + 1]);
-                            const float rl0 = r[e] - bf16lo_to_f32(h);
-                            const float rl1 = r[e + 1] - bf16hi_to_f32(h);
-                            hi[2 * j + e / 2] = h;
-                            lo[2 * j + e / 2] = pack_bf16(rl0, rl1);
-                        }
-                    }
-                    // R_hi over the first half of the sub-block, R_lo over the second
-                    uint32_t h16[16], l16[16];
-#pragma unroll
-                    for (int i = 0; i < 16; i++) {
-                        h16[i] = hi[i];
-                        l16[i] = lo[i];
-                    }
-                    tmem_st16(lane_base + col0, h16);
-                    tmem_st16(lane_base + col0 + 32, l16);
-#pragma unroll
-                    for (int i = 0; i < 16; i++) {
-                        h16[i] = hi[16 + i];
-                        l16[i] = lo[16 + i];
-                    }
-                    tmem_st16(lane_base + col0 + 16, h16);
-                    tmem_st16(lane_base + col0 + 48, l16);
-                    tmem_st_wait();
-                    tc_fence_before();
-                    mbar_arrive(&p_full[b]);
-                }
-                if (!ok)
-                    break;
-                // drain this unit's R T (FP32) to its slot; the groups split the columns
-                if (!mbar_wait(rt_full, nunit & 1, p.status, 29)) {
+        int jt = 0, s = 0, nunit = 0;
+        uint32_t ph = 0;
+        bool ok = true;
+        int prev_u = -1;
+        for (int v = blockIdx.x; ok && v < p.nunits; v += gridDim.x) {
+            int u, kt, t0, t1;
+            unit_of(p, v, u, kt, t0, t1);
+            if (nunit > 0) {
+                // drain the previous unit's R T (FP32) to its slot; the groups split the columns
+                if (!mbar_wait(rt_full, (nunit - 1) & 1, p.status, 29)) {
                     ok = false;
                     break;
                 }
                 tc_fence_after();
-                float *dst = p.RTpart + ((size_t) u * P2_BK + row) * p.Dp;
-                const int cw = p.Dp / ng;
-                for (int c0 = g * cw; c0 < (g + 1) * cw; c0 += 32) {
+                float *dst = p.RTpart + ((size_t) prev_u * P2_BK + row) * DP;
+#pragma unroll 1
+                for (int c0 = g * (DP / 2); c0 < (g + 1) * (DP / 2); c0 += 32) {
                     uint32_t vv[32];
-                    tmem_ld32(lane_base + 256 + (uint32_t) c0, vv);
+                    tmem_ld32(lane_base + (uint32_t) c0, vv);
                     tmem_ld_wait();
 #pragma unroll
                     for (int j = 0; j < 32; j += 4)
@@ -709,13 +651,88 @@ __global__ void __launch_bounds__(P2_THREADS, 1)
                             make_float4(__uint_as_float(vv[j]), __uint_as_float(vv[j + 1]),
                                         __uint_as_float(vv[j + 2]), __uint_as_float(vv[j + 3]));
                 }
-                tc_fence_before();
-                mbar_arrive(rt_empty);
-                nunit++;
             }
-            if (!ok)
-                failed = 1;
+            // this unit's centre row (group 0: Y hi, group 1: Y lo) into tensor memory;
+            // column j holds depths 2 j and 2 j + 1
+            {
+                const uint4 *src =
+                    (const uint4 *) (p.Yb + ((size_t) g * p.Kpad + (size_t) kt * P2_BK + row) * (DP / 2));
+#pragma unroll 1
+                for (int c0 = 0; c0 < YCOLS; c0 += 16) {
+                    uint32_t w[16];
+#pragma unroll
+                    for (int i = 0; i < 4; i++) {
+                        const uint4 x = src[c0 / 4 + i];
+                        w[4 * i] = x.x;
+                        w[4 * i + 1] = x.y;
+                        w[4 * i + 2] = x.z;
+                        w[4 * i + 3] = x.w;
+                    }
+                    tmem_st16(lane_base + (uint32_t) (Y_COL + g * YCOLS + c0), w);
+                }
+                tmem_st_wait();
+            }
+            tc_fence_before();
+            mbar_arrive(y_ready);
+            prev_u = u;
+            for (int t = t0; t < t1; t++, jt++) {
+                const int b = jt & 1;
+                if (!mbar_wait(&t_full[s], ph, p.status, 27) ||
+                    !mbar_wait(&s_full[b], (uint32_t) ((jt >> 1) & 1), p.status, 28)) {
+                    ok = false;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t col0 = (uint32_t) (SP_COL + b * P2_TILE + g * 32);
+                uint32_t va[32];
+                tmem_ld32(lane_base + col0, va);
+                tmem_ld_wait();
+                const float4 *cqs = cq + s * P2_TILE + g * 32;
+                uint32_t hi[16], lo[16];
+#pragma unroll
+                for (int j = 0; j < 16; j++) {
+                    const float4 c0 = cqs[2 * j], c1 = cqs[2 * j + 1];
+                    const float r0 = ex2(fmaf(__uint_as_float(va[2 * j]) - c0.x, c0.y, -c0.z));
+                    const float r1 = ex2(fmaf(__uint_as_float(va[2 * j + 1]) - c1.x, c1.y, -c1.z));
+                    const uint32_t h = pack_bf16(r0, r1);
+                    hi[j] = h;
+                    lo[j] = pack_bf16(r0 - bf16lo_to_f32(h), r1 - bf16hi_to_f32(h));
+                }
+                // over S: R hi in the group's first 16 columns, R lo in the next 16
+                tmem_st16(lane_base + col0, hi);
+                tmem_st16(lane_base + col0 + 16, lo);
+                tmem_st_wait();
+                tc_fence_before();
+                mbar_arrive(&p_full[b]);
+                if (++s == nstage) {
+                    s = 0;
+                    ph ^= 1u;
+                }
+            }
+            nunit++;
         }
+        if (ok && nunit > 0) {
+            // the last unit's R T
+            if (!mbar_wait(rt_full, (nunit - 1) & 1, p.status, 29)) {
+                ok = false;
+            } else {
+                tc_fence_after();
+                float *dst = p.RTpart + ((size_t) prev_u * P2_BK + row) * DP;
+#pragma unroll 1
+                for (int c0 = g * (DP / 2); c0 < (g + 1) * (DP / 2); c0 += 32) {
+                    uint32_t vv[32];
+                    tmem_ld32(lane_base + (uint32_t) c0, vv);
+                    tmem_ld_wait();
+#pragma unroll
+                    for (int j = 0; j < 32; j += 4)
+                        *(float4 *) (dst + c0 + j) =
+                            make_float4(__uint_as_float(vv[j]), __uint_as_float(vv[j + 1]),
+                                        __uint_as_float(vv[j + 2]), __uint_as_float(vv[j + 3]));
+                }
+            }
+        }
+        if (!ok)
+            failed = 1;
     }
     __syncthreads();
     if (failed && warp == 1) {
@@ -727,6 +744,20 @@ __global__ void __launch_bounds__(P2_THREADS, 1)
     tc_fence_after();
     if (warp == 0)
         tmem_dealloc(tmem, 512);
+}
+
+using P2Kernel = void (*)(const CUtensorMap, const P2Params);
+
+// the pass-2 instantiation for a shape (NP <= 3 panels, KL steps in the last, NT pieces)
+P2Kernel pass2_for(int np, int kl, int nt)
+{
+#define DGTM_P2(NP_, KL_, NT_) \
+    if (np == NP_ && kl == KL_ && nt == NT_) return tc_pass2_kernel<NP_, KL_, NT_>;
+#define DGTM_P2_KL(NP_, NT_) DGTM_P2(NP_, 1, NT_) DGTM_P2(NP_, 2, NT_) DGTM_P2(NP_, 3, NT_) DGTM_P2(NP_, 4, NT_)
+    DGTM_P2_KL(1, 1) DGTM_P2_KL(1, 2) DGTM_P2_KL(2, 1) DGTM_P2_KL(2, 2) DGTM_P2_KL(3, 1) DGTM_P2_KL(3, 2)
+#undef DGTM_P2_KL
+#undef DGTM_P2
+    return nullptr;
 }
 
 // ---------------------------------------------------------------------------
@@ -860,13 +891,14 @@ struct TcState {
     int ntiles2, units_per_k, nunits, grid2;
     size_t smem1, smem2;
     P1Kernel pass1;
+    P2Kernel pass2;
     __nv_bfloat16 *Tb, *Yb;
     float *Y32;
     float4 *colq;
     float *RTpart;
     int *status, *hstatus;
     const double *tt, *T64;
-    CUtensorMap tmT1, tmT2, tmY1, tmY2;
+    CUtensorMap tmT2, tmY1;
 };
 
 static int grid_for(size_t n, int per = 256, int cap = 8192)
@@ -890,8 +922,10 @@ int tc_create(TcState **out, int N, int D, int K, int sms, const double *T64, co
                   major, minor);
         return DGTM_ENOTSUP;
     }
-    if (D + 3 > 256) {
-        set_error(DGTM_ENOTSUP, "the split-BF16 form supports D <= 253 (D = %d)", D);
+    if (D + 3 > 3 * PANEL_ELEMS) {
+        // pass 2 keeps the R T accumulator (D + 3 padded to 64-column panels),
+        // two S/P buffers and the centres in the 512 tensor-memory columns
+        set_error(DGTM_ENOTSUP, "the split-BF16 form supports D <= 189 (D = %d)", D);
         return DGTM_ENOTSUP;
     }
     TcState *st = new TcState();
@@ -930,10 +964,10 @@ int tc_create(TcState **out, int N, int D, int K, int sms, const double *T64, co
         return fail(DGTM_ECUDA);
     }
     st->nT = (*st->hstatus) ? 2 : 1;
-    // exact 0/1 data: two 128-point tiles per pass-1 CTA and 128-point pass-2
-    // tiles; split data (two T pieces) halve both to fit shared memory
+    // exact 0/1 data: two 128-point tiles per pass-1 CTA; split data (two T
+    // pieces) one, to fit tensor memory.  Pass-2 tiles are 64 points.
     st->ntile1 = (st->nT == 1) ? 2 : 1;
-    st->bn2 = (st->nT == 1) ? 128 : 64;
+    st->bn2 = P2_TILE;
 
     const size_t tpl = (size_t) st->Npad * st->Dp, ypl = (size_t) st->Kpad * st->Dp;
     // pass 2 work units
@@ -962,14 +996,11 @@ int tc_create(TcState **out, int N, int D, int K, int sms, const double *T64, co
         set_error(DGTM_ECUDA, "t_split: %s", cudaGetErrorString(e));
         return fail(DGTM_ECUDA);
     }
-    // tensor maps: T pieces stacked by rows, Y pieces stacked by rows
-    if ((rc = make_tmap_bf16(&st->tmT1, st->Tb, (uint64_t) st->nT * st->Npad, st->Dp, st->Dp,
-                             P1_TILE, PANEL_ELEMS)) != DGTM_OK ||
-        (rc = make_tmap_bf16(&st->tmT2, st->Tb, (uint64_t) st->nT * st->Npad, st->Dp, st->Dp,
-                             st->bn2, PANEL_ELEMS)) != DGTM_OK ||
+    // tensor maps: T pieces stacked by rows (pass-2 tiles), Y pieces stacked by
+    // rows (pass-1 chunks)
+    if ((rc = make_tmap_bf16(&st->tmT2, st->Tb, (uint64_t) st->nT * st->Npad, st->Dp, st->Dp,
+                             P2_TILE, PANEL_ELEMS)) != DGTM_OK ||
         (rc = make_tmap_bf16(&st->tmY1, st->Yb, 2 * (uint64_t) st->Kpad, st->Dp, st->Dp, P1_BK,
-                             PANEL_ELEMS)) != DGTM_OK ||
-        (rc = make_tmap_bf16(&st->tmY2, st->Yb, 2 * (uint64_t) st->Kpad, st->Dp, st->Dp, P2_BK,
                              PANEL_ELEMS)) != DGTM_OK)
         return fail(rc);
     // shared memory plans
@@ -981,11 +1012,18 @@ int tc_create(TcState **out, int N, int D, int K, int sms, const double *T64, co
     if (ns1 > 12)
         ns1 = 12;
     st->pass1 = pass1_for(st->npanel, st->ksteps - 4 * (st->npanel - 1), st->nT);
-    const size_t y2 = (size_t) 2 * st->npanel * P2_BK * 128;
-    const size_t ts2 = (size_t) st->nT * st->npanel * st->bn2 * 128 + st->bn2 * 16;
-    int ns2 = (int) ((SMEM_LIMIT - 1024 - bar_bytes - y2) / ts2);
-    if (ns2 > 4)
-        ns2 = 4;
+    // pass 2: the point-tile ring (T pieces + column statistics); the centres
+    // live in tensor memory
+    const size_t ts2 = (size_t) st->nT * st->npanel * P2_TILE * 128 + P2_TILE * 16;
+    int ns2 = (int) ((SMEM_LIMIT - 1024 - bar_bytes) / ts2);
+    if (ns2 > 8)
+        ns2 = 8;
+    const int klast = st->ksteps - 4 * (st->npanel - 1);
+    st->pass2 = (st->npanel <= 3) ? pass2_for(st->npanel, klast, st->nT) : nullptr;
+    if (!st->pass2) {
+        set_error(DGTM_ENOTSUP, "the split-BF16 form supports D <= 189 (D = %d)", D);
+        return fail(DGTM_ENOTSUP);
+    }
     if (ns1 < 2 || ns2 < 2 || !st->pass1) {
         set_error(DGTM_ENOTSUP, "the split-BF16 form does not fit shared memory (D = %d)", D);
         return fail(DGTM_ENOTSUP);
@@ -993,11 +1031,11 @@ int tc_create(TcState **out, int N, int D, int K, int sms, const double *T64, co
     st->nstage1 = ns1;
     st->nstage2 = ns2;
     st->smem1 = 1024 + (size_t) ns1 * slot1 + bar_bytes;
-    st->smem2 = 1024 + y2 + (size_t) ns2 * ts2 + bar_bytes;
+    st->smem2 = 1024 + (size_t) ns2 * ts2 + bar_bytes;
     e = cudaFuncSetAttribute(st->pass1, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int) st->smem1);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(tc_pass2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        e = cudaFuncSetAttribute(st->pass2, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int) st->smem2);
     if (e != cudaSuccess) {
         set_error(DGTM_ECUDA, "tc_create: %s", cudaGetErrorString(e));
@@ -1073,21 +1111,18 @@ int tc_mstep_pass(TcState *st, const double2 *, double, cudaStream_t s, int *nla
     P2Params p;
     p.D = st->D;
     p.Dp = st->Dp;
-    p.npanel = st->npanel;
-    p.nT = st->nT;
     p.Npad = st->Npad;
     p.Kpad = st->Kpad;
-    p.bn = st->bn2;
     p.ntiles = st->ntiles2;
     p.units_per_k = st->units_per_k;
     p.ktiles = (st->K + P2_BK - 1) / P2_BK;
     p.nunits = st->nunits;
     p.nstage = st->nstage2;
-    p.ksteps = st->ksteps;
+    p.Yb = (const uint32_t *) st->Yb;
     p.colq = st->colq;
     p.RTpart = st->RTpart;
     p.status = st->status;
-    tc_pass2_kernel<<<st->grid2, P2_THREADS, st->smem2, s>>>(st->tmT2, st->tmY2, p);
+    st->pass2<<<st->grid2, P2_THREADS, st->smem2, s>>>(st->tmT2, p);
     DGTM_CUDA_TRY(cudaGetLastError());
     *nlaunch = 1;
     return DGTM_OK;

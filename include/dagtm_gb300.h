@@ -59,7 +59,8 @@ const char *dgtm_last_error_string(void);
 /*
  * Create a context: uploads T (N x D, leading dimension ldT) and FI
  * (K x M1, leading dimension ldFI) to the current device.  precision is one
- * of DGTM_FP64, DGTM_FP32, DGTM_BF16X3.
+ * of DGTM_FP64, DGTM_FP32, DGTM_BF16X3.  DGTM_BF16X3 needs a Blackwell
+ * (sm_10x) device and D <= 189; otherwise it returns DGTM_ENOTSUP.
  * Replaces the set-up of dagtm/dagtm.cxx:1031-1101 (allocation of the Kbar x
  * Nbar D and R blocks, hyperslab read of T) for a single process.
  */
