@@ -40,14 +40,14 @@ WORKLOAD = dict(N=1_000_000, D=166, K=8000, L=3, M=64, s=2.0, nproto=20, seed=0)
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--form", default="bf16x3", choices=["bf16x3", "fp64", "fp32"])
     ap.add_argument("--n", type=int, default=WORKLOAD["N"], help="data points (default 1M)")
     ap.add_argument("--fp64-steps", type=int, default=2,
                     help="timed EM iterations of the FP64 form beside the headline (0: skip)")
-    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--cpu-sample", type=int, default=1024,
                     help="points in the bounded CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -275,8 +275,8 @@ def main_gb300(args):
     ms_step = ms / args.steps
     value = world * args.steps / (ms / 1000.0)
     launches = sum(p["launches"] for p in phases.values())
-    e2e_ms, h2d, d2h = e2e_steps(torch, pkg, ctx, args.e2e_steps, beta, temp0, stream_cls)
-    e2e_value = world * args.e2e_steps / (e2e_ms / 1000.0)
+    e2e_ms, h2d, d2h = e2e_steps(torch, pkg, ctx, max(1, args.e2e_steps), beta, temp0, stream_cls)
+    e2e_value = world * max(1, args.e2e_steps) / (e2e_ms / 1000.0)
     ctx.close()
 
     peaks, peak_src = measured_peaks()

@@ -244,15 +244,19 @@ __global__ void __launch_bounds__(P1_THREADS, 1)
             // piece tp holds depths 2j (low half) and 2j + 1
             for (int tp = 0; tp < NT; tp++) {
                 const uint4 *src = (const uint4 *) (p.Tb + ((size_t) tp * p.Npad + n) * ACOL);
+                uint4 w[ACOL / 4];  // the whole row in flight at once
+#pragma unroll
+                for (int j = 0; j < ACOL / 4; j++)
+                    w[j] = src[j];
+#pragma unroll
                 for (int c0 = 0; c0 < ACOL; c0 += 16) {
                     uint32_t v[16];
 #pragma unroll
                     for (int j = 0; j < 4; j++) {
-                        const uint4 w = src[c0 / 4 + j];
-                        v[4 * j] = w.x;
-                        v[4 * j + 1] = w.y;
-                        v[4 * j + 2] = w.z;
-                        v[4 * j + 3] = w.w;
+                        v[4 * j] = w[c0 / 4 + j].x;
+                        v[4 * j + 1] = w[c0 / 4 + j].y;
+                        v[4 * j + 2] = w[c0 / 4 + j].z;
+                        v[4 * j + 3] = w[c0 / 4 + j].w;
                     }
                     tmem_st16(lane_base + (uint32_t) ((g * NT + tp) * ACOL + c0), v);
                 }
@@ -263,7 +267,10 @@ __global__ void __launch_bounds__(P1_THREADS, 1)
 
             float m = -INFINITY;
             int kstar = 0;
-            double s1 = 0.0, s2 = 0.0;
+            // shifted sums at temperature 1 and at `temp`, FP32 with Kahan
+            // compensation (the FP64 pipe of this part is too narrow for the
+            // per-chunk update); the result carries ~2 ulp of FP32
+            float s1 = 0.f, s2 = 0.f, k1 = 0.f, k2 = 0.f;
             for (int c = 0; c < p.nchunk; c++) {
                 const int rg = region(g, c);
                 if (!mbar_wait(&acc_full[rg], ruse(c) & 1, p.status, 15)) {
@@ -295,8 +302,11 @@ __global__ void __launch_bounds__(P1_THREADS, 1)
                 const float mx = fmaxf(fmaxf(mxq[0], mxq[1]), fmaxf(mxq[2], mxq[3]));
                 if (mx > m) {
                     if (m > -INFINITY) {
-                        s1 *= (double) ex2((m - mx) * p.c1l);
-                        s2 *= (double) ex2((m - mx) * p.c2l);
+                        const float f1 = ex2((m - mx) * p.c1l), f2 = ex2((m - mx) * p.c2l);
+                        s1 *= f1;
+                        k1 *= f1;
+                        s2 *= f2;
+                        k2 *= f2;
                     }
                     int j0 = P1_BK;
 #pragma unroll
@@ -327,11 +337,21 @@ __global__ void __launch_bounds__(P1_THREADS, 1)
                             e1[u] += ex2((__uint_as_float(v[j + u]) - m) * p.c1l);
                     }
                 }
-                s1 += (double) ((e1[0] + e1[1]) + (e1[2] + e1[3]));
-                s2 += (double) ((e2[0] + e2[1]) + (e2[2] + e2[3]));
+                {
+                    const float y1 = ((e1[0] + e1[1]) + (e1[2] + e1[3])) - k1;
+                    const float u1 = s1 + y1;
+                    k1 = (u1 - s1) - y1;
+                    s1 = u1;
+                    const float y2 = ((e2[0] + e2[1]) + (e2[2] + e2[3])) - k2;
+                    const float u2 = s2 + y2;
+                    k2 = (u2 - s2) - y2;
+                    s2 = u2;
+                }
             }
-            if (!p.two_temps)
+            if (!p.two_temps) {
                 s2 = s1;
+                k2 = k1;
+            }
             // exact (FP32) distance to the best centre, from the unsplit centre
             // and the data, then the per-point terms
             if (ok && n < p.N) {
@@ -339,26 +359,33 @@ __global__ void __launch_bounds__(P1_THREADS, 1)
                 const float *yk = p.Y32 + (size_t) k * p.D;
                 float dsum = 0.f;
                 if (NT == 1) {
-                    // the data are exact in BF16
-                    const uint32_t *tr = p.Tb + (size_t) n * ACOL;
-                    for (int d = 0; d < p.D; d += 2) {
-                        const uint32_t w = tr[d / 2];
-                        const float df0 = yk[d] - __uint_as_float(w << 16);
-                        dsum = fmaf(df0, df0, dsum);
-                        if (d + 1 < p.D) {
-                            const float df1 = yk[d + 1] - __uint_as_float(w & 0xFFFF0000u);
-                            dsum = fmaf(df1, df1, dsum);
+                    // the data are exact in BF16: 8 values per 16-byte load
+                    const uint4 *tr = (const uint4 *) (p.Tb + (size_t) n * ACOL);
+#pragma unroll 4
+                    for (int d0 = 0; d0 < p.D; d0 += 8) {
+                        const uint4 w4 = tr[d0 / 8];
+                        const uint32_t ww[4] = {w4.x, w4.y, w4.z, w4.w};
+#pragma unroll
+                        for (int e = 0; e < 8; e++) {
+                            if (d0 + e < p.D) {
+                                const uint32_t b = ww[e / 2];
+                                const float t = __uint_as_float((e & 1) ? (b & 0xFFFF0000u) : (b << 16));
+                                const float df = yk[d0 + e] - t;
+                                dsum = fmaf(df, df, dsum);
+                            }
                         }
                     }
                 } else {
                     const double *tn = p.T64 + (size_t) n * p.D;
+#pragma unroll 8
                     for (int d = 0; d < p.D; d++) {
                         const float df = yk[d] - (float) tn[d];
                         dsum = fmaf(df, df, dsum);
                     }
                 }
                 const double dstar = (double) dsum;
-                const double ls1 = log(s1), ls2 = log(s2);
+                // FP32 logarithms of the FP32 sums (the FP64 pipe is narrow here)
+                const double ls1 = (double) logf(s1 - k1), ls2 = (double) logf(s2 - k2);
                 const double ls_sel = p.isDA ? ls2 : ls1;
                 const double c_sel = p.isDA ? p.c2 : p.c1;
                 t1 = -p.c1 * dstar + ls1;
@@ -366,8 +393,9 @@ __global__ void __launch_bounds__(P1_THREADS, 1)
                 double lsn = ls_sel;
                 float4 cq = make_float4(m, (float) (2.0 * c_sel) * LOG2E,
                                         (float) (ls_sel * 1.4426950408889634), 0.f);
-                // comm/mpicomm.c:382-389 zero-column fallback
-                if (exp(-p.c1 * dstar) == 0.0) {
+                // comm/mpicomm.c:382-389 zero-column fallback (exp(-700) is far
+                // from underflow, so the FP64 exp runs only near the limit)
+                if (p.c1 * dstar > 700.0 && exp(-p.c1 * dstar) == 0.0) {
                     lsn = NAN;
                     if (p.isDA) {
                         t1 = -INFINITY;
@@ -389,14 +417,21 @@ __global__ void __launch_bounds__(P1_THREADS, 1)
         red[256 + g * P1_TILE + row] = t2;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        double a = 0.0, b2 = 0.0;
-        for (int i = 0; i < NTILE * P1_TILE; i++) {
-            a += red[i];
-            b2 += red[256 + i];
-        }
-        p.part[2 * blockIdx.x] = a;
-        p.part[2 * blockIdx.x + 1] = b2;
+    if (warp < 2) {
+        // fixed-order sum of the CTA's per-point terms: warp 0 the temperature-1
+        // terms, warp 1 the `temp` terms; each lane a contiguous run, then a
+        // butterfly over the lanes
+        constexpr int PER = NTILE * P1_TILE / 32;
+        const double *src = red + warp * 256 + lane * PER;
+        double a = 0.0;
+#pragma unroll
+        for (int i = 0; i < PER; i++)
+            a += src[i];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            a += __shfl_xor_sync(0xffffffffu, a, o);
+        if (lane == 0)
+            p.part[2 * blockIdx.x + warp] = a;
     }
     if (failed && warp == 1) {
         // let every issued MMA finish before the accumulators are released
