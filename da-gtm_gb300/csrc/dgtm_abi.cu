@@ -52,7 +52,7 @@ struct dgtm_ctx {
     // M-step
     int nsplit, n_per_split;
     double *Gpart, *RTpart;
-    double *G, *RT, *A, *B, *work, *bterm;
+    double *G, *RT, *A, *B, *work, *bterm, *abpart;
     double *scal;      // device scalars
     int *flag;         // device status
     double *hscal;     // pinned host scalars
@@ -164,7 +164,7 @@ void free_ctx(dgtm_ctx *c)
     if (!c)
         return;
     void *ptrs[] = {c->T64, c->T32, c->tt, c->FI, c->Y64, c->Y32, c->yy, c->W, c->colstat,
-                    c->part, c->Gpart, c->RTpart, c->G, c->RT, c->A, c->B, c->work, c->bterm,
+                    c->part, c->Gpart, c->RTpart, c->G, c->RT, c->A, c->B, c->work, c->bterm, c->abpart,
                     c->scal, c->flag};
     for (void *p : ptrs)
         if (p)
@@ -265,6 +265,7 @@ int dgtm_ctx_create(int N, int D, int K, int M1, const double *T, int ldT, const
     CK(dev_alloc(&c->B, (size_t) M1 * D));
     CK(dev_alloc(&c->work, 2 * (size_t) M1 * M1 + (size_t) M1 * D));
     CK(dev_alloc(&c->bterm, K));
+    CK(dev_alloc(&c->abpart, form_ab_scratch_doubles(M1, D)));
     CK(dev_alloc(&c->scal, 8));
     CK(dev_alloc(&c->flag, 4));
     CKC(cudaMallocHost((void **) &c->hscal, 8 * sizeof(double)));
@@ -469,7 +470,8 @@ int dgtm_mstep(dgtm_ctx *ctx, double *W, int ldW, double *Y, int ldY, double *be
                                       ctx->RT, ctx->stream));
         nsmall += 1;
     }
-    DGTM_TRY(launch_form_ab(ctx->FI, ctx->G, ctx->RT, K, M1, D, ctx->A, ctx->B, ctx->stream));
+    DGTM_TRY(launch_form_ab(ctx->FI, ctx->G, ctx->RT, K, M1, D, ctx->A, ctx->B, ctx->abpart,
+                            ctx->stream));
     DGTM_TRY(launch_solve(ctx->A, ctx->B, M1, D, ctx->solver, ctx->W, ctx->work, ctx->flag,
                           ctx->stream));
     DGTM_TRY(launch_update_y(ctx->FI, ctx->W, ctx->G, ctx->RT, K, M1, D, ctx->Y64, ctx->yy,

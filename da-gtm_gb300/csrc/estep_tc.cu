@@ -883,22 +883,47 @@ __global__ void y_split_kernel(const double *__restrict__ Y64, int K, int D, int
 }
 
 // RT[k][d] = sum_u RTpart[kt][u][k % 128][d]; G[k] from the column of ones.
+// The FP32 slot values are summed with an error-free FP32 TwoSum (the rounding
+// error of each addition is carried in a second FP32 word), in slot order,
+// and hi + lo is formed in FP64: as exact as FP64 accumulation of the same
+// FP32 inputs would be, without loading the narrow FP64 pipe.
 __global__ void slot_reduce_kernel(const float *__restrict__ RTpart, int K, int D, int Dp, int U,
                                    double *__restrict__ G, double *__restrict__ RT)
 {
     const size_t total = (size_t) K * (D + 1);
+    const size_t ustride = (size_t) P2_BK * Dp;
     for (size_t i = blockIdx.x * (size_t) blockDim.x + threadIdx.x; i < total;
          i += (size_t) gridDim.x * blockDim.x) {
         const int k = (int) (i / (D + 1)), d = (int) (i % (D + 1));
         const int kt = k / P2_BK, kl = k % P2_BK;
         const float *src = RTpart + ((size_t) kt * U * P2_BK + kl) * Dp + d;
-        double s = 0.0;
-        for (int u = 0; u < U; u++)
-            s += (double) src[(size_t) u * P2_BK * Dp];
+        float hi = 0.f, lo = 0.f;
+        int u = 0;
+        for (; u + 8 <= U; u += 8) {
+            float x[8];
+#pragma unroll
+            for (int j = 0; j < 8; j++)
+                x[j] = src[(size_t) (u + j) * ustride];
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                const float t = hi + x[j];
+                const float bp = t - hi;
+                lo += (hi - (t - bp)) + (x[j] - bp);
+                hi = t;
+            }
+        }
+        for (; u < U; u++) {
+            const float xv = src[(size_t) u * ustride];
+            const float t = hi + xv;
+            const float bp = t - hi;
+            lo += (hi - (t - bp)) + (xv - bp);
+            hi = t;
+        }
+        const double sum = (double) hi + (double) lo;
         if (d < D)
-            RT[(size_t) k * D + d] = s;
+            RT[(size_t) k * D + d] = sum;
         else
-            G[k] = s;
+            G[k] = sum;
     }
 }
 

@@ -52,9 +52,11 @@ int launch_r_block(const double *T, const double *Y, const double *tt, const dou
 // Sum nsplit slices in a fixed order: G[k] = sum_s Gpart[s][k], RT = sum_s RTpart[s].
 int launch_reduce_slices(const double *Gpart, const double *RTpart, int nsplit, int K,
                          int D, double *G, double *RT, cudaStream_t s);
-// A = FI^T diag(G) FI (M1 x M1), B = FI^T RT (M1 x D).
+// A = FI^T diag(G) FI (M1 x M1), B = FI^T RT (M1 x D); scratch holds
+// form_ab_scratch_doubles(M1, D) doubles of slice partials.
+size_t form_ab_scratch_doubles(int M1, int D);
 int launch_form_ab(const double *FI, const double *G, const double *RT, int K, int M1,
-                   int D, double *A, double *B, cudaStream_t s);
+                   int D, double *A, double *B, double *scratch, cudaStream_t s);
 // W = A^{-1} B by Cholesky (solver 0) or symmetric-eigen pseudo-inverse (solver 1).
 // work: M1*M1 + M1 doubles (+ M1*M1 for solver 1).  flag[0] != 0 on failure.
 int launch_solve(const double *A, const double *B, int M1, int D, int solver, double *W,

@@ -1,8 +1,10 @@
 // mstep.cu -- the small FP64 kernels of the M-step, shared by every form.
 //
 //   reduce_slices : G_k = sum_s Gpart[s][k], RT = sum_s RTpart[s] (fixed order)
-//   form_ab       : A = FI^T diag(G) FI, B = FI^T RT     (dagtm/dagtm.cxx:1715-1761)
-//   solve         : A W = B, FP64 Cholesky (numerically dependent pivots dropped)
+//   form_ab       : A = FI^T diag(G) FI, B = FI^T RT     (dagtm/dagtm.cxx:1715-1761),
+//                   K-sliced 4 x 4 register tiles, slice partials summed in order
+//   solve         : A W = B, FP64 Cholesky (numerically dependent pivots dropped;
+//                   one-block factorisation, one warp per right-hand side)
 //                   or symmetric-eigen pseudo-inverse
 //                   with exactly-zero eigenvalues dropped (the semantics of
 //                   gsl_linalg_SV_solve used by dagtm_solve2, comm/comm.c:1299-1348)
@@ -53,46 +55,129 @@ int launch_reduce_slices(const double *Gpart, const double *RTpart, int nsplit, 
     return DGTM_OK;
 }
 
-// grid (M1, ceil((D + M1) / 32)); warp w sums k in its chunk, lane = output column.
-__global__ void __launch_bounds__(256) form_ab_kernel(const double *__restrict__ FI,
-                                                      const double *__restrict__ G,
-                                                      const double *__restrict__ RT, int K,
-                                                      int M1, int D, double *__restrict__ A,
-                                                      double *__restrict__ B)
+// C = FI^T [RT | diag(G) FI] (M1 x (D + M1)): B = C[:, :D], A = C[:, D:].
+// The K rows are cut into slices; each thread keeps a 4 x 4 FP64 tile of C
+// over its slice, fed from shared-memory copies of KC rows of FI and of the
+// right operand; the slices' partial tiles are then summed in slice order.
+// The FP64 pipe (about 2 FMA per clock per SM on this part) bounds this.
+constexpr int AB_THREADS = 256;
+constexpr int AB_SLICES = 76;
+
+__global__ void __launch_bounds__(AB_THREADS) form_ab_partial_kernel(
+    const double *__restrict__ FI, const double *__restrict__ G, const double *__restrict__ RT,
+    int K, int M1, int D, int M1p, int Wp, int kc, int slice_len, double *__restrict__ Cpart)
 {
-    __shared__ double part[8][33];
-    const int m = blockIdx.x;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int c = blockIdx.y * 32 + lane;
-    const int chunk = (K + 7) / 8;
-    const int kb = warp * chunk, ke = min(K, kb + chunk);
-    double s = 0.0;
-    if (c < D) {
-        for (int k = kb; k < ke; k++)
-            s += FI[(size_t) k * M1 + m] * RT[(size_t) k * D + c];
-    } else if (c < D + M1) {
-        const int j = c - D;
-        for (int k = kb; k < ke; k++)
-            s += FI[(size_t) k * M1 + m] * (FI[(size_t) k * M1 + j] * G[k]);
+    extern __shared__ double sh[];
+    double *FIs = sh;                       // kc x M1p
+    double *Rs = sh + (size_t) kc * M1p;    // kc x Wp
+    const int W = D + M1;
+    const int nct = Wp / 4;
+    const int tile = blockIdx.y * AB_THREADS + threadIdx.x;
+    const bool active = tile < (M1p / 4) * nct;
+    const int m0 = active ? (tile / nct) * 4 : 0, c0 = active ? (tile % nct) * 4 : 0;
+    const int kb = blockIdx.x * slice_len, ke = min(K, kb + slice_len);
+    double acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+            acc[i][j] = 0.0;
+    for (int k0 = kb; k0 < ke; k0 += kc) {
+        const int nk = min(kc, ke - k0);
+        __syncthreads();
+        for (int e = threadIdx.x; e < kc * M1p; e += AB_THREADS) {
+            const int r = e / M1p, m = e % M1p;
+            FIs[e] = (r < nk && m < M1) ? FI[(size_t) (k0 + r) * M1 + m] : 0.0;
+        }
+        for (int e = threadIdx.x; e < kc * Wp; e += AB_THREADS) {
+            const int r = e / Wp, c = e % Wp;
+            double v = 0.0;
+            if (r < nk) {
+                const int k = k0 + r;
+                if (c < D)
+                    v = RT[(size_t) k * D + c];
+                else if (c < W)
+                    v = G[k] * FI[(size_t) k * M1 + (c - D)];
+            }
+            Rs[e] = v;
+        }
+        __syncthreads();
+        if (active) {
+            for (int r = 0; r < nk; r++) {
+                const double2 a01 = *(const double2 *) &FIs[(size_t) r * M1p + m0];
+                const double2 a23 = *(const double2 *) &FIs[(size_t) r * M1p + m0 + 2];
+                const double2 b01 = *(const double2 *) &Rs[(size_t) r * Wp + c0];
+                const double2 b23 = *(const double2 *) &Rs[(size_t) r * Wp + c0 + 2];
+                const double av[4] = {a01.x, a01.y, a23.x, a23.y};
+                const double bv[4] = {b01.x, b01.y, b23.x, b23.y};
+#pragma unroll
+                for (int i = 0; i < 4; i++)
+#pragma unroll
+                    for (int j = 0; j < 4; j++)
+                        acc[i][j] = fma(av[i], bv[j], acc[i][j]);
+            }
+        }
     }
-    part[warp][lane] = s;
-    __syncthreads();
-    if (warp == 0) {
-        double t = 0.0;
-        for (int w = 0; w < 8; w++)
-            t += part[w][lane];
-        if (c < D)
-            B[(size_t) m * D + c] = t;
-        else if (c < D + M1)
-            A[(size_t) m * M1 + (c - D)] = t;
+    if (!active)
+        return;
+    double *dst = Cpart + (size_t) blockIdx.x * M1 * W;
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+            if (m0 + i < M1 && c0 + j < W)
+                dst[(size_t) (m0 + i) * W + c0 + j] = acc[i][j];
+}
+
+// sum over slices in slice order; A is written from its upper triangle and
+// mirrored, so it is exactly symmetric
+__global__ void form_ab_reduce_kernel(const double *__restrict__ Cpart, int nslice, int M1, int D,
+                                      double *__restrict__ A, double *__restrict__ B)
+{
+    const int W = D + M1;
+    const size_t total = (size_t) M1 * W;
+    for (size_t i = blockIdx.x * (size_t) blockDim.x + threadIdx.x; i < total;
+         i += (size_t) gridDim.x * blockDim.x) {
+        const int m = (int) (i / W), c = (int) (i % W);
+        if (c >= D && c - D < m)
+            continue;
+        double sum = 0.0;
+        for (int sl = 0; sl < nslice; sl++)
+            sum += Cpart[(size_t) sl * total + i];
+        if (c < D) {
+            B[(size_t) m * D + c] = sum;
+        } else {
+            const int j = c - D;
+            A[(size_t) m * M1 + j] = sum;
+            A[(size_t) j * M1 + m] = sum;
+        }
     }
 }
 
+size_t form_ab_scratch_doubles(int M1, int D) { return (size_t) AB_SLICES * M1 * (D + M1); }
+
 int launch_form_ab(const double *FI, const double *G, const double *RT, int K, int M1, int D,
-                   double *A, double *B, cudaStream_t s)
+                   double *A, double *B, double *scratch, cudaStream_t s)
 {
-    dim3 grid(M1, ceil_div(D + M1, 32));
-    form_ab_kernel<<<grid, 256, 0, s>>>(FI, G, RT, K, M1, D, A, B);
+    const int M1p = (M1 + 3) / 4 * 4, Wp = (D + M1 + 3) / 4 * 4;
+    int kc = (int) ((48 * 1024) / (sizeof(double) * (size_t) (M1p + Wp)));
+    if (kc > 16)
+        kc = 16;
+    if (kc < 1) {
+        set_error(DGTM_ENOTSUP, "form_ab: M1 + D too large (%d)", M1 + D);
+        return DGTM_ENOTSUP;
+    }
+    const int slice_len = ceil_div(K, AB_SLICES);
+    const int nslice = ceil_div(K, slice_len);
+    const int ntiles = (M1p / 4) * (Wp / 4);
+    const dim3 grid(nslice, ceil_div(ntiles, AB_THREADS));
+    const size_t smem = sizeof(double) * (size_t) kc * (M1p + Wp);
+    form_ab_partial_kernel<<<grid, AB_THREADS, smem, s>>>(FI, G, RT, K, M1, D, M1p, Wp, kc,
+                                                          slice_len, scratch);
+    DGTM_CUDA_TRY(cudaGetLastError());
+    const size_t total = (size_t) M1 * (D + M1);
+    int blocks = (int) ((total + 255) / 256);
+    form_ab_reduce_kernel<<<blocks, 256, 0, s>>>(scratch, nslice, M1, D, A, B);
     DGTM_CUDA_TRY(cudaGetLastError());
     return DGTM_OK;
 }
@@ -104,18 +189,15 @@ constexpr int SOLVE_THREADS = 512;
 constexpr int SMEM_SOLVE_MAX = 110;  // M1 up to which L lives in shared memory
 
 // Left-looking Cholesky, L[i][j] = (A[i][j] - sum_{p<j} L[i][p] L[j][p]) / L[j][j],
-// then forward and back substitution, one right-hand side per thread.
-// A pivot that keeps less than CHOL_DROP of its diagonal (the column adds no
-// new direction at FP64 precision) is dropped: that unknown is fixed at 0,
-// which keeps the solve defined when A = FI^T diag(G) FI is numerically
-// singular (wide basis functions).  flag[1] counts the dropped pivots.
+// in one block; L goes to `work`.  A pivot that keeps less than CHOL_DROP of
+// its diagonal (the column adds no new direction at FP64 precision) is
+// dropped: its diagonal is stored as 0 and that unknown is fixed at 0, which
+// keeps the solve defined when A = FI^T diag(G) FI is numerically singular
+// (wide basis functions).  flag[1] counts the dropped pivots.
 constexpr double CHOL_DROP = 1e-12;
 
 __global__ void __launch_bounds__(SOLVE_THREADS) cholesky_kernel(const double *__restrict__ A,
-                                                                const double *__restrict__ B,
-                                                                int M1, int D,
-                                                                double *__restrict__ W,
-                                                                double *__restrict__ work,
+                                                                int M1, double *__restrict__ work,
                                                                 int *flag)
 {
     extern __shared__ double sh[];
@@ -155,29 +237,74 @@ __global__ void __launch_bounds__(SOLVE_THREADS) cholesky_kernel(const double *_
             L[(size_t) i * M1 + j] = (ljj != 0.0) ? L[(size_t) i * M1 + j] / ljj : 0.0;
         __syncthreads();
     }
-    if (threadIdx.x == 0)
+    if (L != work)
+        for (int i = threadIdx.x; i < M1 * M1; i += blockDim.x)
+            work[i] = L[i];
+    if (threadIdx.x == 0) {
+        flag[0] = bad ? DGTM_ENONFINITE : 0;
         flag[1] = ndrop;
-    if (bad) {
-        if (threadIdx.x == 0)
-            flag[0] = DGTM_ENONFINITE;
+    }
+}
+
+// Forward and back substitution with L from cholesky_kernel: one warp per
+// right-hand side (column of B), the lanes split each dot product, a fixed
+// shuffle tree sums it; many blocks, so the D columns run on many SMs.
+constexpr int TRI_WARPS = 4;
+
+__global__ void __launch_bounds__(TRI_WARPS * 32) tri_solve_kernel(const double *__restrict__ Lg,
+                                                                  const double *__restrict__ B,
+                                                                  int M1, int D, int l_in_smem,
+                                                                  const int *__restrict__ flag,
+                                                                  double *__restrict__ W)
+{
+    extern __shared__ double sh[];
+    double *Ws = sh;                                   // TRI_WARPS x M1
+    double *Ls = sh + (size_t) TRI_WARPS * M1;         // M1 x M1 when it fits
+    if (flag[0] != 0)
+        return;  // non-finite factorisation: reported by the host
+    const double *L = Lg;
+    if (l_in_smem) {
+        for (int i = threadIdx.x; i < M1 * M1; i += blockDim.x)
+            Ls[i] = Lg[i];
+        __syncthreads();
+        L = Ls;
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int c = blockIdx.x * TRI_WARPS + warp;
+    if (c >= D)
         return;
+    double *w = Ws + (size_t) warp * M1;
+    for (int i = 0; i < M1; i++) {
+        double part = 0.0;
+        for (int p = lane; p < i; p += 32)
+            part += L[(size_t) i * M1 + p] * w[p];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            part += __shfl_down_sync(0xffffffffu, part, o);
+        part = __shfl_sync(0xffffffffu, part, 0);
+        const double lii = L[(size_t) i * M1 + i];
+        const double v = B[(size_t) i * D + c] - part;
+        if (lane == 0)
+            w[i] = (lii != 0.0) ? v / lii : 0.0;
+        __syncwarp();
     }
-    for (int c = threadIdx.x; c < D; c += blockDim.x) {
-        for (int i = 0; i < M1; i++) {
-            const double lii = L[(size_t) i * M1 + i];
-            double v = B[(size_t) i * D + c];
-            for (int p = 0; p < i; p++)
-                v -= L[(size_t) i * M1 + p] * W[(size_t) p * D + c];
-            W[(size_t) i * D + c] = (lii != 0.0) ? v / lii : 0.0;
-        }
-        for (int i = M1 - 1; i >= 0; i--) {
-            const double lii = L[(size_t) i * M1 + i];
-            double v = W[(size_t) i * D + c];
-            for (int p = i + 1; p < M1; p++)
-                v -= L[(size_t) p * M1 + i] * W[(size_t) p * D + c];
-            W[(size_t) i * D + c] = (lii != 0.0) ? v / lii : 0.0;
-        }
+    for (int i = M1 - 1; i >= 0; i--) {
+        double part = 0.0;
+        for (int p = i + 1 + lane; p < M1; p += 32)
+            part += L[(size_t) p * M1 + i] * w[p];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            part += __shfl_down_sync(0xffffffffu, part, o);
+        part = __shfl_sync(0xffffffffu, part, 0);
+        const double lii = L[(size_t) i * M1 + i];
+        const double v = w[i] - part;
+        __syncwarp();
+        if (lane == 0)
+            w[i] = (lii != 0.0) ? v / lii : 0.0;
+        __syncwarp();
     }
+    for (int i = lane; i < M1; i += 32)
+        W[(size_t) i * D + c] = w[i];
 }
 
 // Parallel cyclic Jacobi (round-robin pairing) on the symmetric A, then
@@ -307,7 +434,15 @@ int launch_solve(const double *A, const double *B, int M1, int D, int solver, do
         DGTM_CUDA_TRY(cudaFuncSetAttribute(cholesky_kernel,
                                            cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int) (smem > 0 ? smem : 1)));
-        cholesky_kernel<<<1, SOLVE_THREADS, smem, s>>>(A, B, M1, D, W, work, flag);
+        cholesky_kernel<<<1, SOLVE_THREADS, smem, s>>>(A, M1, work, flag);
+        DGTM_CUDA_TRY(cudaGetLastError());
+        const size_t lbytes = sizeof(double) * (size_t) M1 * M1;
+        const int l_in_smem = lbytes <= 96 * 1024;
+        const size_t tsmem = sizeof(double) * (size_t) TRI_WARPS * M1 + (l_in_smem ? lbytes : 0);
+        DGTM_CUDA_TRY(cudaFuncSetAttribute(tri_solve_kernel,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int) tsmem));
+        tri_solve_kernel<<<ceil_div(D, TRI_WARPS), TRI_WARPS * 32, tsmem, s>>>(work, B, M1, D,
+                                                                             l_in_smem, flag, W);
     }
     DGTM_CUDA_TRY(cudaGetLastError());
     return DGTM_OK;
