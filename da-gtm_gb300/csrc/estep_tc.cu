@@ -78,6 +78,19 @@ struct P1Params {
     int *status;
 };
 
+// lowest j in block B (columns 32 B .. 32 B + 31) with v[j] == mx; the block
+// is known to hold mx.  Constant indices keep v in registers.
+template <int B>
+__device__ __forceinline__ int first_equal(const uint32_t (&v)[P1_BK], float mx)
+{
+    int j0 = 32 * B + 31;
+#pragma unroll
+    for (int j = 31; j >= 0; j--)
+        if (__uint_as_float(v[32 * B + j]) == mx)
+            j0 = 32 * B + j;
+    return j0;
+}
+
 // TMEM map of pass 1: the point tiles (MMA operand A, BF16 pairs) from column
 // 0, the two 128-column accumulators at columns 256 and 384.
 constexpr int P1_ACC_COL = 256;
@@ -291,13 +304,13 @@ __global__ void __launch_bounds__(P1_THREADS, 1)
                 }
                 tc_fence_before();
                 mbar_arrive(&acc_empty[rg]);
+                // maxima of the four 32-column blocks (four independent chains)
                 float mxq[4] = {-INFINITY, -INFINITY, -INFINITY, -INFINITY};
 #pragma unroll
-                for (int j = 0; j < P1_BK; j += 4) {
-                    mxq[0] = fmaxf(mxq[0], __uint_as_float(v[j]));
-                    mxq[1] = fmaxf(mxq[1], __uint_as_float(v[j + 1]));
-                    mxq[2] = fmaxf(mxq[2], __uint_as_float(v[j + 2]));
-                    mxq[3] = fmaxf(mxq[3], __uint_as_float(v[j + 3]));
+                for (int j = 0; j < 32; j += 2) {
+#pragma unroll
+                    for (int u = 0; u < 4; u++)
+                        mxq[u] = fmax3(mxq[u], __uint_as_float(v[32 * u + j]), __uint_as_float(v[32 * u + j + 1]));
                 }
                 const float mx = fmaxf(fmaxf(mxq[0], mxq[1]), fmaxf(mxq[2], mxq[3]));
                 if (mx > m) {
@@ -308,34 +321,54 @@ __global__ void __launch_bounds__(P1_THREADS, 1)
                         s2 *= f2;
                         k2 *= f2;
                     }
-                    int j0 = P1_BK;
-#pragma unroll
-                    for (int j = P1_BK - 1; j >= 0; j--) {
-                        if (__uint_as_float(v[j]) == mx)
-                            j0 = j;
-                    }
+                    // lowest index attaining the maximum: first block holding it,
+                    // then a scan of that block only
+                    int j0;
+                    if (mxq[0] == mx)
+                        j0 = first_equal<0>(v, mx);
+                    else if (mxq[1] == mx)
+                        j0 = first_equal<1>(v, mx);
+                    else if (mxq[2] == mx)
+                        j0 = first_equal<2>(v, mx);
+                    else
+                        j0 = first_equal<3>(v, mx);
                     m = mx;
                     kstar = c * P1_BK + j0;
                 }
-                // four independent accumulation chains per sum
-                float e1[4] = {0.f, 0.f, 0.f, 0.f}, e2[4] = {0.f, 0.f, 0.f, 0.f};
-                if (p.two_temps) {
+                // four independent accumulation chains per sum (element j goes
+                // to chain j % 4), as two packed pairs: (0, 1) and (2, 3)
+                float e1[4], e2[4];
+                {
+                    const f2 mm = f2_pack(m, m), k1 = f2_pack(p.c1l, p.c1l);
+                    f2 a1 = f2_pack(0.f, 0.f), b1 = a1, a2 = a1, b2 = a1;
+                    if (p.two_temps) {
+                        const f2 k2 = f2_pack(p.c2l, p.c2l);
 #pragma unroll
-                    for (int j = 0; j < P1_BK; j += 4) {
+                        for (int j = 0; j < P1_BK; j += 4) {
+                            const f2 xa = f2_sub(f2_pack(__uint_as_float(v[j]), __uint_as_float(v[j + 1])), mm);
+                            const f2 xb = f2_sub(f2_pack(__uint_as_float(v[j + 2]), __uint_as_float(v[j + 3])), mm);
+                            a1 = f2_add(a1, f2_ex2(f2_mul(xa, k1)));
+                            b1 = f2_add(b1, f2_ex2(f2_mul(xb, k1)));
+                            a2 = f2_add(a2, f2_ex2(f2_mul(xa, k2)));
+                            b2 = f2_add(b2, f2_ex2(f2_mul(xb, k2)));
+                        }
+                    } else {
 #pragma unroll
-                        for (int u = 0; u < 4; u++) {
-                            const float x = __uint_as_float(v[j + u]) - m;
-                            e1[u] += ex2(x * p.c1l);
-                            e2[u] += ex2(x * p.c2l);
+                        for (int j = 0; j < P1_BK; j += 4) {
+                            const f2 xa = f2_sub(f2_pack(__uint_as_float(v[j]), __uint_as_float(v[j + 1])), mm);
+                            const f2 xb = f2_sub(f2_pack(__uint_as_float(v[j + 2]), __uint_as_float(v[j + 3])), mm);
+                            a1 = f2_add(a1, f2_ex2(f2_mul(xa, k1)));
+                            b1 = f2_add(b1, f2_ex2(f2_mul(xb, k1)));
                         }
                     }
-                } else {
-#pragma unroll
-                    for (int j = 0; j < P1_BK; j += 4) {
-#pragma unroll
-                        for (int u = 0; u < 4; u++)
-                            e1[u] += ex2((__uint_as_float(v[j + u]) - m) * p.c1l);
-                    }
+                    e1[0] = f2_lo(a1);
+                    e1[1] = f2_hi(a1);
+                    e1[2] = f2_lo(b1);
+                    e1[3] = f2_hi(b1);
+                    e2[0] = f2_lo(a2);
+                    e2[1] = f2_hi(a2);
+                    e2[2] = f2_lo(b2);
+                    e2[3] = f2_hi(b2);
                 }
                 {
                     const float y1 = ((e1[0] + e1[1]) + (e1[2] + e1[3])) - k1;

@@ -278,6 +278,66 @@ __device__ __forceinline__ float ex2(float x)
     return y;
 }
 
+// ---------------------------------------------------------------- packed FP32 pairs
+// Two FP32 lanes in one 64-bit register pair; add / sub / mul are the same
+// round-to-nearest operations per lane as the scalar forms, in one instruction.
+struct f2 {
+    uint64_t v;
+};
+
+__device__ __forceinline__ f2 f2_pack(float lo, float hi)
+{
+    f2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r.v) : "f"(lo), "f"(hi));
+    return r;
+}
+
+__device__ __forceinline__ float f2_lo(f2 a)
+{
+    float lo, hi;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(a.v));
+    return lo;
+}
+
+__device__ __forceinline__ float f2_hi(f2 a)
+{
+    float lo, hi;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(a.v));
+    return hi;
+}
+
+__device__ __forceinline__ f2 f2_add(f2 a, f2 b)
+{
+    f2 r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
+    return r;
+}
+
+__device__ __forceinline__ f2 f2_sub(f2 a, f2 b)
+{
+    f2 r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
+    return r;
+}
+
+__device__ __forceinline__ f2 f2_mul(f2 a, f2 b)
+{
+    f2 r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
+    return r;
+}
+
+// max of three FP32 values in one instruction
+__device__ __forceinline__ float fmax3(float a, float b, float c)
+{
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+
+// ex2 of both lanes (the special-function unit has no paired form)
+__device__ __forceinline__ f2 f2_ex2(f2 a) { return f2_pack(ex2(f2_lo(a)), ex2(f2_hi(a))); }
+
 // Pack two floats into BF16x2 (round to nearest): lo -> bits 0..15, hi -> 16..31.
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi)
 {
