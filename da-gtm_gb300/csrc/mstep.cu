@@ -188,12 +188,30 @@ int launch_form_ab(const double *FI, const double *G, const double *RT, int K, i
 constexpr int SOLVE_THREADS = 512;
 constexpr int SMEM_SOLVE_MAX = 110;  // M1 up to which L lives in shared memory
 
-// Left-looking Cholesky, L[i][j] = (A[i][j] - sum_{p<j} L[i][p] L[j][p]) / L[j][j],
-// in one block; L goes to `work`.  A pivot that keeps less than CHOL_DROP of
-// its diagonal (the column adds no new direction at FP64 precision) is
-// dropped: its diagonal is stored as 0 and that unknown is fixed at 0, which
-// keeps the solve defined when A = FI^T diag(G) FI is numerically singular
-// (wide basis functions).  flag[1] counts the dropped pivots.
+// 1/sqrt(d) for a positive normal d: an FP32 estimate refined by two
+// Newton-Raphson steps for f(r) = 1/r^2 - d, r <- r (3 - d r^2) / 2 (each
+// step doubles the correct bits: 23 -> 46 -> full FP64).  Outside the FP32
+// exponent range the FP64 library square root is used.
+__device__ __forceinline__ double rsqrt_nr(double d)
+{
+    if (!(d > 1e-30 && d < 1e30))
+        return 1.0 / sqrt(d);
+    double r = (double) rsqrtf((float) d);
+#pragma unroll
+    for (int it = 0; it < 2; it++)
+        r = r * fma(-0.5 * d * r, r, 1.5);
+    return r;
+}
+
+// Right-looking Cholesky in one block: per column j, the pivot's reciprocal
+// square root (thread 0), the scaled column, then the rank-1 update of the
+// trailing lower triangle by all threads.  A pivot that keeps less than
+// CHOL_DROP of its diagonal (the column adds no new direction at FP64
+// precision) is dropped: its diagonal and column are stored as 0 and that
+// unknown is fixed at 0, which keeps the solve defined when
+// A = FI^T diag(G) FI is numerically singular (wide basis functions).
+// L (lower triangle) goes to work[0 .. M1*M1), the reciprocal diagonal to
+// work[M1*M1 .. M1*M1 + M1) (0 for a dropped pivot); flag[1] counts the drops.
 constexpr double CHOL_DROP = 1e-12;
 
 __global__ void __launch_bounds__(SOLVE_THREADS) cholesky_kernel(const double *__restrict__ A,
@@ -202,7 +220,9 @@ __global__ void __launch_bounds__(SOLVE_THREADS) cholesky_kernel(const double *_
 {
     extern __shared__ double sh[];
     double *L = (M1 <= SMEM_SOLVE_MAX) ? sh : work;
+    double *inv = work + (size_t) M1 * M1;
     __shared__ int bad, ndrop;
+    __shared__ double rj;
     if (threadIdx.x == 0) {
         bad = 0;
         ndrop = 0;
@@ -211,16 +231,9 @@ __global__ void __launch_bounds__(SOLVE_THREADS) cholesky_kernel(const double *_
         L[i] = A[i];
     __syncthreads();
     for (int j = 0; j < M1; j++) {
-        const double ajj = A[(size_t) j * M1 + j];
-        for (int i = j + threadIdx.x; i < M1; i += blockDim.x) {
-            double v = L[(size_t) i * M1 + j];
-            for (int p = 0; p < j; p++)
-                v -= L[(size_t) i * M1 + p] * L[(size_t) j * M1 + p];
-            L[(size_t) i * M1 + j] = v;
-        }
-        __syncthreads();
         if (threadIdx.x == 0) {
-            const double d = L[(size_t) j * M1 + j];
+            const double d = L[(size_t) j * M1 + j], ajj = A[(size_t) j * M1 + j];
+            double r = 0.0;
             if (!isfinite(d)) {
                 bad = 1;
                 L[(size_t) j * M1 + j] = 0.0;
@@ -228,13 +241,31 @@ __global__ void __launch_bounds__(SOLVE_THREADS) cholesky_kernel(const double *_
                 ndrop++;
                 L[(size_t) j * M1 + j] = 0.0;  // marks a dropped unknown
             } else {
-                L[(size_t) j * M1 + j] = sqrt(d);
+                r = rsqrt_nr(d);
+                L[(size_t) j * M1 + j] = d * r;
             }
+            inv[j] = r;
+            rj = r;
         }
         __syncthreads();
-        const double ljj = L[(size_t) j * M1 + j];
+        const double r = rj;
         for (int i = j + 1 + threadIdx.x; i < M1; i += blockDim.x)
-            L[(size_t) i * M1 + j] = (ljj != 0.0) ? L[(size_t) i * M1 + j] / ljj : 0.0;
+            L[(size_t) i * M1 + j] *= r;
+        __syncthreads();
+        // L[i][k] -= L[i][j] L[k][j] for j < k <= i, packed over the triangle
+        const int n = M1 - 1 - j;
+        const int npair = n * (n + 1) / 2;
+        for (int t = threadIdx.x; t < npair; t += blockDim.x) {
+            // row offset ii with ii (ii + 1) / 2 <= t
+            int ii = (int) ((sqrtf(8.0f * (float) t + 1.0f) - 1.0f) * 0.5f);
+            while ((ii + 1) * (ii + 2) / 2 <= t)
+                ii++;
+            while (ii * (ii + 1) / 2 > t)
+                ii--;
+            const int kk = t - ii * (ii + 1) / 2;
+            const int i = j + 1 + ii, k = j + 1 + kk;
+            L[(size_t) i * M1 + k] -= L[(size_t) i * M1 + j] * L[(size_t) k * M1 + j];
+        }
         __syncthreads();
     }
     if (L != work)
@@ -246,10 +277,13 @@ __global__ void __launch_bounds__(SOLVE_THREADS) cholesky_kernel(const double *_
     }
 }
 
-// Forward and back substitution with L from cholesky_kernel: one warp per
-// right-hand side (column of B), the lanes split each dot product, a fixed
-// shuffle tree sums it; many blocks, so the D columns run on many SMs.
+// Forward (L y = b) and back (L^T w = y) substitution, right-looking: one warp
+// per right-hand side (column of B), lane l holding entries l, l + 32, ...;
+// step i broadcasts the finished entry i and every lane updates its later
+// (forward) or earlier (back) entries with one FMA.  Many blocks, so the D
+// columns run on many SMs.
 constexpr int TRI_WARPS = 4;
+constexpr int TRI_MAXR = 8;  // entries per lane: M1 <= 256
 
 __global__ void __launch_bounds__(TRI_WARPS * 32) tri_solve_kernel(const double *__restrict__ Lg,
                                                                   const double *__restrict__ B,
@@ -258,53 +292,72 @@ __global__ void __launch_bounds__(TRI_WARPS * 32) tri_solve_kernel(const double 
                                                                   double *__restrict__ W)
 {
     extern __shared__ double sh[];
-    double *Ws = sh;                                   // TRI_WARPS x M1
-    double *Ls = sh + (size_t) TRI_WARPS * M1;         // M1 x M1 when it fits
     if (flag[0] != 0)
         return;  // non-finite factorisation: reported by the host
     const double *L = Lg;
+    const double *inv = Lg + (size_t) M1 * M1;
     if (l_in_smem) {
-        for (int i = threadIdx.x; i < M1 * M1; i += blockDim.x)
-            Ls[i] = Lg[i];
+        for (int i = threadIdx.x; i < M1 * M1 + M1; i += blockDim.x)
+            sh[i] = Lg[i];
         __syncthreads();
-        L = Ls;
+        L = sh;
+        inv = sh + (size_t) M1 * M1;
     }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int c = blockIdx.x * TRI_WARPS + warp;
     if (c >= D)
         return;
-    double *w = Ws + (size_t) warp * M1;
-    for (int i = 0; i < M1; i++) {
-        double part = 0.0;
-        for (int p = lane; p < i; p += 32)
-            part += L[(size_t) i * M1 + p] * w[p];
+    double x[TRI_MAXR];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1)
-            part += __shfl_down_sync(0xffffffffu, part, o);
-        part = __shfl_sync(0xffffffffu, part, 0);
-        const double lii = L[(size_t) i * M1 + i];
-        const double v = B[(size_t) i * D + c] - part;
-        if (lane == 0)
-            w[i] = (lii != 0.0) ? v / lii : 0.0;
-        __syncwarp();
+    for (int r = 0; r < TRI_MAXR; r++) {
+        const int p = lane + 32 * r;
+        x[r] = (p < M1) ? B[(size_t) p * D + c] : 0.0;
     }
-    for (int i = M1 - 1; i >= 0; i--) {
-        double part = 0.0;
-        for (int p = i + 1 + lane; p < M1; p += 32)
-            part += L[(size_t) p * M1 + i] * w[p];
+    // forward: y_i = x_i / L_ii, then x_p -= L_pi y_i for p > i; entry i sits
+    // in register rb = i / 32 of lane i % 32 (rb a constant after unrolling)
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1)
-            part += __shfl_down_sync(0xffffffffu, part, o);
-        part = __shfl_sync(0xffffffffu, part, 0);
-        const double lii = L[(size_t) i * M1 + i];
-        const double v = w[i] - part;
-        __syncwarp();
-        if (lane == 0)
-            w[i] = (lii != 0.0) ? v / lii : 0.0;
-        __syncwarp();
+    for (int rb = 0; rb < TRI_MAXR; rb++) {
+        if (32 * rb >= M1)
+            break;
+        const int iend = min(32, M1 - 32 * rb);
+        for (int il = 0; il < iend; il++) {
+            const int i = 32 * rb + il;
+            const double yi = __shfl_sync(0xffffffffu, x[rb], il) * inv[i];
+#pragma unroll
+            for (int r = 0; r < TRI_MAXR; r++) {
+                const int p = lane + 32 * r;
+                if (p == i)
+                    x[r] = yi;
+                else if (p > i && p < M1)
+                    x[r] = fma(-L[(size_t) p * M1 + i], yi, x[r]);
+            }
+        }
     }
-    for (int i = lane; i < M1; i += 32)
-        W[(size_t) i * D + c] = w[i];
+    // back: w_i = y_i / L_ii, then y_p -= L_ip w_i for p < i
+#pragma unroll
+    for (int rb = TRI_MAXR - 1; rb >= 0; rb--) {
+        if (32 * rb >= M1)
+            continue;
+        const int iend = min(32, M1 - 32 * rb);
+        for (int il = iend - 1; il >= 0; il--) {
+            const int i = 32 * rb + il;
+            const double wi = __shfl_sync(0xffffffffu, x[rb], il) * inv[i];
+#pragma unroll
+            for (int r = 0; r < TRI_MAXR; r++) {
+                const int p = lane + 32 * r;
+                if (p == i)
+                    x[r] = wi;
+                else if (p < i)
+                    x[r] = fma(-L[(size_t) i * M1 + p], wi, x[r]);
+            }
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < TRI_MAXR; r++) {
+        const int p = lane + 32 * r;
+        if (p < M1)
+            W[(size_t) p * D + c] = x[r];
+    }
 }
 
 // Parallel cyclic Jacobi (round-robin pairing) on the symmetric A, then
@@ -423,6 +476,10 @@ int launch_solve(const double *A, const double *B, int M1, int D, int solver, do
                  double *work, int *flag, cudaStream_t s)
 {
     DGTM_CUDA_TRY(cudaMemsetAsync(flag, 0, 2 * sizeof(int), s));
+    if (solver != DGTM_SOLVE_SVD && M1 > 32 * TRI_MAXR) {
+        set_error(DGTM_ENOTSUP, "the Cholesky solver supports M1 <= %d", 32 * TRI_MAXR);
+        return DGTM_ENOTSUP;
+    }
     if (solver == DGTM_SOLVE_SVD && M1 > 2 * SOLVE_THREADS - 2) {
         set_error(DGTM_ENOTSUP, "the eigen-SVD solver supports M1 <= %d", 2 * SOLVE_THREADS - 2);
         return DGTM_ENOTSUP;
@@ -436,9 +493,9 @@ int launch_solve(const double *A, const double *B, int M1, int D, int solver, do
                                            (int) (smem > 0 ? smem : 1)));
         cholesky_kernel<<<1, SOLVE_THREADS, smem, s>>>(A, M1, work, flag);
         DGTM_CUDA_TRY(cudaGetLastError());
-        const size_t lbytes = sizeof(double) * (size_t) M1 * M1;
+        const size_t lbytes = sizeof(double) * ((size_t) M1 * M1 + M1);
         const int l_in_smem = lbytes <= 96 * 1024;
-        const size_t tsmem = sizeof(double) * (size_t) TRI_WARPS * M1 + (l_in_smem ? lbytes : 0);
+        const size_t tsmem = l_in_smem ? lbytes : 16;
         DGTM_CUDA_TRY(cudaFuncSetAttribute(tri_solve_kernel,
                                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int) tsmem));
         tri_solve_kernel<<<ceil_div(D, TRI_WARPS), TRI_WARPS * 32, tsmem, s>>>(work, B, M1, D,
