@@ -291,11 +291,15 @@ def main_gb300(args):
         peak_note = f"{form} nominal (no measured {form} peak)"
     achieved = flops / (per_launch_ms / 1000.0) / 1e12
     traffic = traffic_summary().get(f"{form}:{dom}")
+    traffic_note = None
     if traffic is not None:
         traffic = traffic.get("bytes_per_point", 0.0) * N
+        traffic_note = "ncu dram__bytes_read.sum + dram__bytes_write.sum per point (profiles/traffic.json), x N"
     roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": achieved / peak, "traffic": traffic, "kernel": dom,
-                "per_launch_ms": per_launch_ms, "peak_source": peak_note}
+                "per_launch_ms": per_launch_ms, "peak_source": peak_note,
+                "frac_of_burst_peak": achieved / peaks.get("bf16_tflops", peak) if form == "bf16x3" else None,
+                "traffic_source": traffic_note}
 
     fp64 = None
     if args.fp64_steps > 0 and form != "fp64":
