@@ -112,7 +112,8 @@ constexpr int P1_ACC_COL = 256;
 // ---------------------------------------------------------------------------
 template <int NP, int KL, int NT>
 __global__ void __launch_bounds__(P1_THREADS, 1)
-    tc_pass1_kernel(const __grid_constant__ CUtensorMap tmY, const P1Params p)
+    tc_pass1_kernel(const __grid_constant__ CUtensorMap tmY, const __grid_constant__ CUtensorMap tmT,
+                    const P1Params p)
 {
     constexpr int NTILE = (NT == 1) ? 2 : 1;
     constexpr int ACOL = NP * 32;                      // TMEM columns of one data piece
@@ -125,8 +126,9 @@ __global__ void __launch_bounds__(P1_THREADS, 1)
     uint64_t *bars = (uint64_t *) (Yslot + nslot * SLOT_BYTES);
     uint64_t *y_full = bars;
     uint64_t *y_empty = bars + nslot;
-    uint64_t *a_ready = bars + 2 * nslot;
-    uint64_t *acc_full = a_ready + 1;   // [region]
+    uint64_t *t_full = bars + 2 * nslot;  // the data tiles are in shared memory
+    uint64_t *t_done = t_full + 1;        // ... and copied into tensor memory
+    uint64_t *acc_full = t_done + 1;      // [region]
     uint64_t *acc_empty = acc_full + 2;
     uint64_t *drain = acc_empty + 2;
     uint32_t *tmem_sh = (uint32_t *) (drain + 1);
@@ -142,7 +144,8 @@ __global__ void __launch_bounds__(P1_THREADS, 1)
             mbar_init(&y_full[s], 1);
             mbar_init(&y_empty[s], 1);
         }
-        mbar_init(a_ready, 128 * NTILE);
+        mbar_init(t_full, 1);
+        mbar_init(t_done, 1);
         for (int b = 0; b < 2; b++) {
             mbar_init(&acc_full[b], 1);
             mbar_init(&acc_empty[b], 128);
@@ -162,13 +165,30 @@ __global__ void __launch_bounds__(P1_THREADS, 1)
     auto ruse = [&](int c) { return NTILE == 2 ? c : (c >> 1); };
 
     if (warp == 0 && lane == 0) {
-        // ---------------- producer: the Y ring, one piece of a chunk per slot ----------------
+        // ---------------- producer ----------------
         prefetch_tmap(&tmY);
+        prefetch_tmap(&tmT);
+        // the CTA's two data pieces (tiles g = 0, 1, or pieces hi, lo of one
+        // tile) into the last two slots, for the copy into tensor memory
+        mbar_expect_tx(t_full, (uint32_t) (2 * SLOT_BYTES));
+#pragma unroll
+        for (int s2 = 0; s2 < 2; s2++) {
+            const int g = (NTILE == 2) ? s2 : 0, tp = (NT == 2) ? s2 : 0;
+#pragma unroll
+            for (int pn = 0; pn < NP; pn++)
+                tma_load_2d(Yslot + (nslot - 2 + s2) * SLOT_BYTES + pn * PANEL_BYTES, &tmT, t_full,
+                            PANEL_ELEMS * pn, tp * p.Npad + n0 + g * P1_TILE);
+        }
+        // the Y ring, one piece of a chunk per slot
         int q = 0;
         uint32_t ph = 0;
         for (int it = 0; it < 2 * p.nchunk; it++) {
             if (it >= nslot && !mbar_wait(&y_empty[q], ph ^ 1u, p.status, 11)) {
                 failed = 1;
+                break;
+            }
+            if (it < nslot && q >= nslot - 2 && !mbar_wait(t_done, 0, p.status, 17)) {
+                failed = 1;  // the slot still held a data piece
                 break;
             }
             const int c = it >> 1, piece = it & 1;
@@ -186,7 +206,24 @@ __global__ void __launch_bounds__(P1_THREADS, 1)
         // ---------------- MMA issuer (whole warp; one elected lane issues) ----------------
         const uint32_t idesc = idesc_bf16(P1_TILE, P1_BK, 0, 0);
         const uint64_t ydesc0 = sdesc_sw128(smem_u32(Yslot), 16, 1024);
-        bool ok = mbar_wait_w(a_ready, 0, p.status, 12);
+        // data pieces: shared memory -> tensor memory (the MMA A operand; piece
+        // s2 goes to columns s2 * ACOL, column j holding depths 2 j and 2 j + 1)
+        bool ok = mbar_wait_w(t_full, 0, p.status, 12);
+        if (ok) {
+            tc_fence_after();
+            const uint64_t tdesc = ydesc0 + (uint64_t) ((nslot - 2) * (SLOT_BYTES >> 4));
+#pragma unroll
+            for (int s2 = 0; s2 < 2; s2++)
+#pragma unroll
+                for (int pn = 0; pn < NP; pn++)
+#pragma unroll
+                    for (int kk = 0; kk < (pn == NP - 1 ? KL : 4); kk++)
+                        tmem_cp_w(tmem + (uint32_t) (s2 * ACOL + pn * 32 + kk * 8),
+                                  tdesc + (uint64_t) (s2 * (SLOT_BYTES >> 4) + pn * (PANEL_BYTES >> 4) + 2 * kk));
+            mma_commit_w(t_done);
+            ok = mbar_wait_w(t_done, 0, p.status, 12);
+            tc_fence_after();
+        }
         int q0 = 0;
         uint32_t ph0 = 0;
         for (int c = 0; ok && c < p.nchunk; c++) {
@@ -253,31 +290,6 @@ __global__ void __launch_bounds__(P1_THREADS, 1)
         double t1 = 0.0, t2 = 0.0;
         bool ok = true;
         if (g < NTILE) {
-            // this thread's data row into tensor memory (A operand): column j of
-            // piece tp holds depths 2j (low half) and 2j + 1
-            for (int tp = 0; tp < NT; tp++) {
-                const uint4 *src = (const uint4 *) (p.Tb + ((size_t) tp * p.Npad + n) * ACOL);
-                uint4 w[ACOL / 4];  // the whole row in flight at once
-#pragma unroll
-                for (int j = 0; j < ACOL / 4; j++)
-                    w[j] = src[j];
-#pragma unroll
-                for (int c0 = 0; c0 < ACOL; c0 += 16) {
-                    uint32_t v[16];
-#pragma unroll
-                    for (int j = 0; j < 4; j++) {
-                        v[4 * j] = w[c0 / 4 + j].x;
-                        v[4 * j + 1] = w[c0 / 4 + j].y;
-                        v[4 * j + 2] = w[c0 / 4 + j].z;
-                        v[4 * j + 3] = w[c0 / 4 + j].w;
-                    }
-                    tmem_st16(lane_base + (uint32_t) ((g * NT + tp) * ACOL + c0), v);
-                }
-            }
-            tmem_st_wait();
-            tc_fence_before();
-            mbar_arrive(a_ready);
-
             float m = -INFINITY;
             int kstar = 0;
             // shifted sums at temperature 1 and at `temp`, FP32 with Kahan
@@ -386,36 +398,59 @@ __global__ void __launch_bounds__(P1_THREADS, 1)
                 k2 = k1;
             }
             // exact (FP32) distance to the best centre, from the unsplit centre
-            // and the data, then the per-point terms
-            if (ok && n < p.N) {
-                const int k = min(kstar, p.K - 1);
-                const float *yk = p.Y32 + (size_t) k * p.D;
-                float dsum = 0.f;
-                if (NT == 1) {
-                    // the data are exact in BF16: 8 values per 16-byte load
-                    const uint4 *tr = (const uint4 *) (p.Tb + (size_t) n * ACOL);
-#pragma unroll 4
-                    for (int d0 = 0; d0 < p.D; d0 += 8) {
-                        const uint4 w4 = tr[d0 / 8];
-                        const uint32_t ww[4] = {w4.x, w4.y, w4.z, w4.w};
+            // and the data, then the per-point terms.  With exact (0/1) data the
+            // row is read back from tensor memory (the A operand, warp-
+            // collective, so outside the per-point branch), 64 dimensions per
+            // batch of centre loads.
+            const bool active = ok && n < p.N;
+            const int kb = min(kstar, p.K - 1);
+            const float *yk = p.Y32 + (size_t) kb * p.D;
+            float dsum = 0.f;
+            if (NT == 1) {
+#pragma unroll 1
+                for (int b = 0; b < NP; b++) {
+                    uint32_t tw[32];
+                    tmem_ld32p(lane_base + (uint32_t) (g * ACOL + 32 * b), tw);
+                    float yv[64];
+                    const int d0 = 64 * b;
+                    if (active) {
+                        if ((p.D & 1) == 0) {
+                            // even D: every row starts on an 8-byte boundary
 #pragma unroll
-                        for (int e = 0; e < 8; e++) {
+                            for (int e = 0; e < 32; e++) {
+                                const float2 y2 = (d0 + 2 * e < p.D) ? *(const float2 *) (yk + d0 + 2 * e)
+                                                                     : make_float2(0.f, 0.f);
+                                yv[2 * e] = y2.x;
+                                yv[2 * e + 1] = y2.y;
+                            }
+                        } else {
+#pragma unroll
+                            for (int e = 0; e < 64; e++)
+                                yv[e] = (d0 + e < p.D) ? yk[d0 + e] : 0.f;
+                        }
+                    }
+                    tmem_ld_wait();
+                    if (active) {
+#pragma unroll
+                        for (int e = 0; e < 64; e++) {
                             if (d0 + e < p.D) {
-                                const uint32_t b = ww[e / 2];
-                                const float t = __uint_as_float((e & 1) ? (b & 0xFFFF0000u) : (b << 16));
-                                const float df = yk[d0 + e] - t;
+                                const uint32_t w = tw[e >> 1];
+                                const float t = __uint_as_float((e & 1) ? (w & 0xFFFF0000u) : (w << 16));
+                                const float df = yv[e] - t;
                                 dsum = fmaf(df, df, dsum);
                             }
                         }
                     }
-                } else {
-                    const double *tn = p.T64 + (size_t) n * p.D;
-#pragma unroll 8
-                    for (int d = 0; d < p.D; d++) {
-                        const float df = yk[d] - (float) tn[d];
-                        dsum = fmaf(df, df, dsum);
-                    }
                 }
+            } else if (active) {
+                const double *tn = p.T64 + (size_t) n * p.D;
+#pragma unroll 8
+                for (int d = 0; d < p.D; d++) {
+                    const float df = yk[d] - (float) tn[d];
+                    dsum = fmaf(df, df, dsum);
+                }
+            }
+            if (active) {
                 const double dstar = (double) dsum;
                 // FP32 logarithms of the FP32 sums (the FP64 pipe is narrow here)
                 const double ls1 = (double) logf(s1 - k1), ls2 = (double) logf(s2 - k2);
@@ -960,7 +995,7 @@ __global__ void slot_reduce_kernel(const float *__restrict__ RTpart, int K, int 
     }
 }
 
-using P1Kernel = void (*)(const CUtensorMap, const P1Params);
+using P1Kernel = void (*)(const CUtensorMap, const CUtensorMap, const P1Params);
 
 // the pass-1 instantiation for a shape (NP panels, KL steps in the last, NT pieces)
 P1Kernel pass1_for(int np, int kl, int nt)
@@ -991,7 +1026,7 @@ struct TcState {
     float *RTpart;
     int *status, *hstatus;
     const double *tt, *T64;
-    CUtensorMap tmT2, tmY1;
+    CUtensorMap tmT1, tmT2, tmY1;
 };
 
 static int grid_for(size_t n, int per = 256, int cap = 8192)
@@ -1089,9 +1124,11 @@ int tc_create(TcState **out, int N, int D, int K, int sms, const double *T64, co
         set_error(DGTM_ECUDA, "t_split: %s", cudaGetErrorString(e));
         return fail(DGTM_ECUDA);
     }
-    // tensor maps: T pieces stacked by rows (pass-2 tiles), Y pieces stacked by
-    // rows (pass-1 chunks)
-    if ((rc = make_tmap_bf16(&st->tmT2, st->Tb, (uint64_t) st->nT * st->Npad, st->Dp, st->Dp,
+    // tensor maps: T pieces stacked by rows (pass-1 data tiles, pass-2 tiles),
+    // Y pieces stacked by rows (pass-1 chunks)
+    if ((rc = make_tmap_bf16(&st->tmT1, st->Tb, (uint64_t) st->nT * st->Npad, st->Dp, st->Dp,
+                             P1_TILE, PANEL_ELEMS)) != DGTM_OK ||
+        (rc = make_tmap_bf16(&st->tmT2, st->Tb, (uint64_t) st->nT * st->Npad, st->Dp, st->Dp,
                              P2_TILE, PANEL_ELEMS)) != DGTM_OK ||
         (rc = make_tmap_bf16(&st->tmY1, st->Yb, 2 * (uint64_t) st->Kpad, st->Dp, st->Dp, P1_BK,
                              PANEL_ELEMS)) != DGTM_OK)
@@ -1193,7 +1230,7 @@ int tc_estep(TcState *st, const double *, double c1, double c2, int isDA, double
     p.part = part;
     p.status = st->status;
     DGTM_CUDA_TRY(cudaMemsetAsync(st->status, 0, sizeof(int), s));
-    st->pass1<<<tc_pass1_blocks(st), P1_THREADS, st->smem1, s>>>(st->tmY1, p);
+    st->pass1<<<tc_pass1_blocks(st), P1_THREADS, st->smem1, s>>>(st->tmY1, st->tmT1, p);
     DGTM_CUDA_TRY(cudaGetLastError());
     *nlaunch = 1;
     return DGTM_OK;

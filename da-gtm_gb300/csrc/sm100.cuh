@@ -217,6 +217,20 @@ __device__ __forceinline__ void mma_commit_w(uint64_t *bar)
         : "memory");
 }
 
+// Shared memory -> tensor memory copy of one 128-row x 256-bit slice (16 BF16
+// of K per row, 8 TMEM columns), read through the same shared-memory matrix
+// descriptor the MMA uses; row r lands in lane r, so the result is the MMA's
+// A-from-tensor-memory layout.  Asynchronous, ordered with the issuing
+// thread's MMAs and tracked by mma_commit; one elected lane of a converged warp.
+__device__ __forceinline__ void tmem_cp_w(uint32_t taddr, uint64_t s_desc)
+{
+    asm volatile(
+        "{\n\t.reg .pred e;\n\telect.sync _|e, 0xffffffff;\n\t"
+        "@e tcgen05.cp.cta_group::1.128x256b [%0], %1;\n\t}" ::"r"(taddr),
+        "l"(s_desc)
+        : "memory");
+}
+
 // mbar_wait by every lane of a warp, with one outcome for the whole warp.
 __device__ __forceinline__ bool mbar_wait_w(uint64_t *bar, uint32_t parity, int *status, int code,
                                             uint64_t limit_ns = 4000000000ull)
@@ -288,23 +302,13 @@ struct f2 {
 __device__ __forceinline__ f2 f2_pack(float lo, float hi)
 {
     f2 r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r.v) : "f"(lo), "f"(hi));
+    r.v = ((uint64_t) __float_as_uint(hi) << 32) | (uint64_t) __float_as_uint(lo);
     return r;
 }
 
-__device__ __forceinline__ float f2_lo(f2 a)
-{
-    float lo, hi;
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(a.v));
-    return lo;
-}
+__device__ __forceinline__ float f2_lo(f2 a) { return __uint_as_float((uint32_t) a.v); }
 
-__device__ __forceinline__ float f2_hi(f2 a)
-{
-    float lo, hi;
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(a.v));
-    return hi;
-}
+__device__ __forceinline__ float f2_hi(f2 a) { return __uint_as_float((uint32_t) (a.v >> 32)); }
 
 __device__ __forceinline__ f2 f2_add(f2 a, f2 b)
 {
