@@ -13,6 +13,18 @@
 #include <stdlib.h>
 #include <string.h>
 
+// Row-block copy.  When both pitches equal the row width the block is
+// contiguous and goes through a plain 1D copy: the 2D host-to-device path
+// costs several times as long for the same bytes (0.33 ms against 0.06 ms for
+// an 8000 x 166 FP64 block on GB300).
+static cudaError_t copy_rows(void *dst, size_t dpitch, const void *src, size_t spitch,
+                             size_t width, size_t height, cudaMemcpyKind kind, cudaStream_t s)
+{
+    if (dpitch == width && spitch == width)
+        return cudaMemcpyAsync(dst, src, width * height, kind, s);
+    return cudaMemcpy2DAsync(dst, dpitch, src, spitch, width, height, kind, s);
+}
+
 namespace dgtm {
 
 static thread_local char g_err[512] = "";
@@ -271,9 +283,9 @@ int dgtm_ctx_create(int N, int D, int K, int M1, const double *T, int ldT, const
     CKC(cudaMallocHost((void **) &c->hscal, 8 * sizeof(double)));
     CKC(cudaMallocHost((void **) &c->hflag, 4 * sizeof(int)));
 
-    CKC(cudaMemcpy2DAsync(c->T64, sizeof(double) * D, T, sizeof(double) * (size_t) ldT,
+    CKC(copy_rows(c->T64, sizeof(double) * D, T, sizeof(double) * (size_t) ldT,
                           sizeof(double) * D, N, cudaMemcpyHostToDevice, c->stream));
-    CKC(cudaMemcpy2DAsync(c->FI, sizeof(double) * M1, FI, sizeof(double) * (size_t) ldFI,
+    CKC(copy_rows(c->FI, sizeof(double) * M1, FI, sizeof(double) * (size_t) ldFI,
                           sizeof(double) * M1, K, cudaMemcpyHostToDevice, c->stream));
     CK(launch_norms(c->T64, N, D, c->tt, c->stream));
     CK(launch_sum_ratio(c->tt, N, 0.0, 1.0, c->scal, c->stream));
@@ -340,7 +352,7 @@ int dgtm_set_Y(dgtm_ctx *ctx, const double *Y, int ldY)
         set_error(DGTM_EINVAL, "bad Y (ldY=%d, D=%d)", ldY, ctx->D);
         return DGTM_EINVAL;
     }
-    DGTM_CUDA_TRY(cudaMemcpy2DAsync(ctx->Y64, sizeof(double) * ctx->D, Y,
+    DGTM_CUDA_TRY(copy_rows(ctx->Y64, sizeof(double) * ctx->D, Y,
                                     sizeof(double) * (size_t) ldY, sizeof(double) * ctx->D,
                                     ctx->K, cudaMemcpyHostToDevice, ctx->stream));
     DGTM_TRY(launch_norms(ctx->Y64, ctx->K, ctx->D, ctx->yy, ctx->stream));
@@ -358,7 +370,7 @@ int dgtm_get_Y(dgtm_ctx *ctx, double *Y, int ldY)
         set_error(DGTM_EINVAL, "bad Y (ldY=%d, D=%d)", ldY, ctx->D);
         return DGTM_EINVAL;
     }
-    DGTM_CUDA_TRY(cudaMemcpy2DAsync(Y, sizeof(double) * (size_t) ldY, ctx->Y64,
+    DGTM_CUDA_TRY(copy_rows(Y, sizeof(double) * (size_t) ldY, ctx->Y64,
                                     sizeof(double) * ctx->D, sizeof(double) * ctx->D, ctx->K,
                                     cudaMemcpyDeviceToHost, ctx->stream));
     return sync_and_check(ctx);
@@ -375,7 +387,7 @@ int dgtm_get_W(dgtm_ctx *ctx, double *W, int ldW)
         set_error(DGTM_ESTATE, "no M-step has run yet");
         return DGTM_ESTATE;
     }
-    DGTM_CUDA_TRY(cudaMemcpy2DAsync(W, sizeof(double) * (size_t) ldW, ctx->W,
+    DGTM_CUDA_TRY(copy_rows(W, sizeof(double) * (size_t) ldW, ctx->W,
                                     sizeof(double) * ctx->D, sizeof(double) * ctx->D, ctx->M1,
                                     cudaMemcpyDeviceToHost, ctx->stream));
     return sync_and_check(ctx);
@@ -486,11 +498,11 @@ int dgtm_mstep(dgtm_ctx *ctx, double *W, int ldW, double *Y, int ldY, double *be
     DGTM_CUDA_TRY(cudaMemcpyAsync(ctx->hflag, ctx->flag, 2 * sizeof(int), cudaMemcpyDeviceToHost,
                                   ctx->stream));
     if (W)
-        DGTM_CUDA_TRY(cudaMemcpy2DAsync(W, sizeof(double) * (size_t) ldW, ctx->W,
+        DGTM_CUDA_TRY(copy_rows(W, sizeof(double) * (size_t) ldW, ctx->W,
                                         sizeof(double) * D, sizeof(double) * D, M1,
                                         cudaMemcpyDeviceToHost, ctx->stream));
     if (Y)
-        DGTM_CUDA_TRY(cudaMemcpy2DAsync(Y, sizeof(double) * (size_t) ldY, ctx->Y64,
+        DGTM_CUDA_TRY(copy_rows(Y, sizeof(double) * (size_t) ldY, ctx->Y64,
                                         sizeof(double) * D, sizeof(double) * D, K,
                                         cudaMemcpyDeviceToHost, ctx->stream));
     if (ctx->tc)
@@ -531,7 +543,7 @@ int dgtm_get_stats(dgtm_ctx *ctx, double *G, double *RT, int ldRT)
         DGTM_CUDA_TRY(cudaMemcpyAsync(G, ctx->G, sizeof(double) * ctx->K, cudaMemcpyDeviceToHost,
                                       ctx->stream));
     if (RT)
-        DGTM_CUDA_TRY(cudaMemcpy2DAsync(RT, sizeof(double) * (size_t) ldRT, ctx->RT,
+        DGTM_CUDA_TRY(copy_rows(RT, sizeof(double) * (size_t) ldRT, ctx->RT,
                                         sizeof(double) * ctx->D, sizeof(double) * ctx->D,
                                         ctx->K, cudaMemcpyDeviceToHost, ctx->stream));
     return sync_and_check(ctx);
@@ -614,7 +626,7 @@ int dgtm_map(dgtm_ctx *ctx, const double *X, int L, double *M, int ldM)
         r = launch_map(ctx->T64, ctx->Y64, ctx->tt, ctx->yy, ctx->colstat, ctx->N, ctx->D, ctx->K,
                        c, dX, L, dM, ctx->stream);
         if (r == DGTM_OK)
-            e = cudaMemcpy2DAsync(M, sizeof(double) * (size_t) ldM, dM, sizeof(double) * L,
+            e = copy_rows(M, sizeof(double) * (size_t) ldM, dM, sizeof(double) * L,
                                   sizeof(double) * L, ctx->N, cudaMemcpyDeviceToHost,
                                   ctx->stream);
     }
@@ -648,7 +660,7 @@ int dgtm_get_R_block(dgtm_ctx *ctx, int k0, int nk, int n0, int nn, double *R, i
                            k0, nk, n0, nn, dR, ctx->stream);
     cudaError_t e = cudaSuccess;
     if (r == DGTM_OK)
-        e = cudaMemcpy2DAsync(R, sizeof(double) * (size_t) ldR, dR, sizeof(double) * nn,
+        e = copy_rows(R, sizeof(double) * (size_t) ldR, dR, sizeof(double) * nn,
                               sizeof(double) * nn, nk, cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess)
         e = cudaStreamSynchronize(ctx->stream);
