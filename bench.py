@@ -59,6 +59,22 @@ def dist_env():
             int(os.environ.get("LOCAL_RANK", "0")))
 
 
+def max_over_ranks(x, world):
+    """Max of a per-rank number over all ranks (the slowest rank times the job)."""
+    if world <= 1:
+        return float(x)
+    import torch
+    dev = "cuda" if torch.distributed.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], device=dev, dtype=torch.float64)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(steps, ms, world):
+    """Weak scaling: every rank runs `steps` iterations of its own problem in `ms`."""
+    return world * steps / (ms / 1000.0)
+
+
 def make_problem(n):
     ds = importlib.import_module("da-gtm_gb300.datasets")
     st = importlib.import_module("da-gtm_gb300.gtm_setup")
@@ -183,10 +199,7 @@ def run_form(torch, pkg, form, T, FI, Y0, beta0, temp0, steps, warmup, rank, wor
     ms, beta = time_steps(torch, ctx, steps, beta, temp0, stream)
     if sampler:
         sampler.__exit__(None, None, None)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, world)
     phases = ctx.timing()
     ctx.set_timing(False)
     return ctx, ms, phases, (sampler.summary() if sampler else None), beta
@@ -273,10 +286,11 @@ def main_gb300(args):
                                              args.steps, args.warmup, rank, world, stream_cls,
                                              clocks=(rank == 0))
     ms_step = ms / args.steps
-    value = world * args.steps / (ms / 1000.0)
+    value = whole_job_rate(args.steps, ms, world)
     launches = sum(p["launches"] for p in phases.values())
     e2e_ms, h2d, d2h = e2e_steps(torch, pkg, ctx, max(1, args.e2e_steps), beta, temp0, stream_cls)
-    e2e_value = world * max(1, args.e2e_steps) / (e2e_ms / 1000.0)
+    e2e_ms = max_over_ranks(e2e_ms, world)
+    e2e_value = whole_job_rate(max(1, args.e2e_steps), e2e_ms, world)
     ctx.close()
 
     peaks, peak_src = measured_peaks()
