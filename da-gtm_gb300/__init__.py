@@ -33,7 +33,8 @@ ERRORS = {1: "EINVAL", 2: "ECUDA", 3: "ENOTSPD", 4: "ENONFINITE", 5: "ETIMEOUT",
 # every symbol the header declares (checked by the CPU tests)
 ABI_SYMBOLS = ("dgtm_version", "dgtm_last_error_string", "dgtm_ctx_create", "dgtm_ctx_destroy",
                "dgtm_set_solver", "dgtm_set_Y", "dgtm_get_Y", "dgtm_get_W", "dgtm_estep",
-               "dgtm_mstep", "dgtm_get_stats", "dgtm_map", "dgtm_get_R_block", "dgtm_set_timing",
+               "dgtm_mstep", "dgtm_get_stats", "dgtm_map", "dgtm_get_R_block", "dgtm_next_ctemp",
+               "dgtm_set_timing",
                "dgtm_reset_timing", "dgtm_get_timing", "dgtm_get_stream", "dgtm_selftest",
                "dgtm_fe_workspace_size", "dgtm_fe_forward", "dgtm_fe_backward",
                "dgtm_fe_forward_noalloc")
@@ -75,6 +76,7 @@ def load_library(path: str = LIB_PATH):
         "dgtm_get_stats": (i, [vp, _dp, _dp, i]),
         "dgtm_map": (i, [vp, _dp, i, _dp, i]),
         "dgtm_get_R_block": (i, [vp, i, i, i, i, _dp, i]),
+        "dgtm_next_ctemp": (i, [vp, d, d, d, _dp, _dp]),
         "dgtm_set_timing": (i, [vp, i]),
         "dgtm_reset_timing": (i, [vp]),
         "dgtm_get_timing": (i, [vp, _dp, ctypes.POINTER(ctypes.c_longlong),
@@ -233,6 +235,16 @@ class Context:
         _check(load_library().dgtm_get_R_block(self._h, k0, nk, n0, nn, _p(R), nn))
         return R
 
+    def next_ctemp(self, temp: float, beta: float, eps: float, gg=None) -> float:
+        """Next critical temperature (AUTO cooling) from the last E-step's R;
+        gg: per-centre weights (the G of the last M-step), None: row sums of R."""
+        out = ctypes.c_double()
+        g = None if gg is None else _f64(np.asarray(gg).reshape(self.K))
+        _check(load_library().dgtm_next_ctemp(self._h, float(temp), float(beta), float(eps),
+                                              _p(g) if g is not None else None,
+                                              ctypes.byref(out)))
+        return out.value
+
 
 QUEUE_SIZE = 50  # dagtm/dagtm.cxx:45 INIT_QUEUE_SIZE
 
@@ -252,7 +264,12 @@ class RunResult:
 def anneal(ctx: Context, beta: float, temp: float, isDA: int = 1, schedule: str = "exp",
            alpha: float = 0.99, delta: float = 0.1, eps: float = 1e-6, iter0: int = 0,
            maxloop: int = 0, log=None) -> RunResult:
-    """Temperature loop of dagtm/dagtm.cxx:1508-2206 (EXP / LINEAR, no HDA).
+    """Temperature loop of dagtm/dagtm.cxx:1508-2206 (EXP / LINEAR / AUTO, no HDA).
+
+    AUTO (dagtm/dagtm.cxx:1919-1934): the next temperature is the critical
+    temperature from ``Context.next_ctemp`` with the G of the last M-step as
+    weights (the reference's vggsub), or temp * alpha when that is not below
+    the current temperature.
 
     Starts from the centres already loaded into ``ctx`` (a fresh set-up or a
     restart, dagtm/dagtm.cxx:1161-1232) and mirrors the reference's order:
@@ -266,6 +283,7 @@ def anneal(ctx: Context, beta: float, temp: float, isDA: int = 1, schedule: str 
     qual = 0.0
     isLast = False
     W = None
+    G_last = None
     while True:
         if temp < 1.0:
             temp = 1.0
@@ -292,19 +310,30 @@ def anneal(ctx: Context, beta: float, temp: float, isDA: int = 1, schedule: str 
             if abs(diff) < eps:
                 break
             if nloop > QUEUE_SIZE:
-                avg_old = sum(queue) / QUEUE_SIZE
-                queue[qnext] = qual
-                qnext = (qnext + 1) % QUEUE_SIZE
-                avg = sum(queue) / QUEUE_SIZE
-                if abs(avg - avg_old) < eps:
+                # a queue still holding DBL_MAX sums to inf and the test fails,
+                # as in the reference (comm/comm.c:1742-1746)
+                with np.errstate(over="ignore", invalid="ignore"):
+                    avg_old = sum(queue) / QUEUE_SIZE
+                    queue[qnext] = qual
+                    qnext = (qnext + 1) % QUEUE_SIZE
+                    avg = sum(queue) / QUEUE_SIZE
+                    stalled = abs(avg - avg_old) < eps
+                if stalled:
                     break
             beta, W, _ = ctx.mstep(want_W=True)
+            if schedule == "auto":
+                G_last = ctx.get_stats()[0]
             if maxloop and nloop >= maxloop:
                 isLast = True
                 break
         if isDA and not isLast:
             if schedule == "linear":
                 temp -= delta
+            elif schedule == "auto":
+                ctemp = ctx.next_ctemp(temp, beta, eps, gg=G_last)
+                if ctemp >= temp:
+                    ctemp = temp * alpha  # no valid next critical temperature
+                temp = ctemp
             else:
                 temp *= alpha
         else:

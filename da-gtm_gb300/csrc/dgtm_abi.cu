@@ -13,6 +13,8 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <vector>
+
 // Row-block copy.  When both pitches equal the row width the block is
 // contiguous and goes through a plain 1D copy: the 2D host-to-device path
 // costs several times as long for the same bytes (0.33 ms against 0.06 ms for
@@ -639,6 +641,84 @@ int dgtm_map(dgtm_ctx *ctx, const double *X, int L, double *M, int ldM)
         return DGTM_ECUDA;
     }
     return r;
+}
+
+int dgtm_next_ctemp(dgtm_ctx *ctx, double temp, double beta, double eps, const double *gg,
+                    double *ctemp)
+{
+    DGTM_TRY(check_ctx(ctx));
+    if (!ctemp || !(beta > 0.0)) {
+        set_error(DGTM_EINVAL, "dgtm_next_ctemp: bad arguments (beta=%g)", beta);
+        return DGTM_EINVAL;
+    }
+    if (!ctx->stats_valid) {
+        set_error(DGTM_ESTATE, "dgtm_next_ctemp needs an E-step on the current centres first");
+        return DGTM_ESTATE;
+    }
+    const int N = ctx->N, D = ctx->D, K = ctx->K;
+    const double c = ctx->isDA ? ctx->beta / (2.0 * ctx->temp) : ctx->beta / 2.0;
+    bool in_smem = false;
+    const size_t per = ctemp_scratch_doubles(D, 1, &in_smem);
+    int kb = (int) ((size_t) (256u << 20) / (per * sizeof(double)));
+    if (kb < 1)
+        kb = 1;
+    if (kb > K)
+        kb = K;
+    double *scratch = nullptr, *dgg = nullptr, *dgsum = nullptr, *dout = nullptr;
+    std::vector<double> out((size_t) 2 * K), gsum(K);
+    int rc = dev_alloc(&scratch, ctemp_scratch_doubles(D, kb, &in_smem));
+    if (rc == DGTM_OK)
+        rc = dev_alloc(&dgsum, K);
+    if (rc == DGTM_OK)
+        rc = dev_alloc(&dout, (size_t) 2 * K);
+    if (rc == DGTM_OK && gg)
+        rc = dev_alloc(&dgg, K);
+    cudaError_t e = cudaSuccess;
+    if (rc == DGTM_OK && gg)
+        e = cudaMemcpyAsync(dgg, gg, sizeof(double) * K, cudaMemcpyHostToDevice, ctx->stream);
+    // eigenvalues at or above (temp - eps) gg 2 / beta are dropped (comm/mpicomm.c:624)
+    const double lim_scale = (temp - eps) * 2.0 / beta;
+    for (int k0 = 0; rc == DGTM_OK && e == cudaSuccess && k0 < K; k0 += kb) {
+        const int nb = (K - k0 < kb) ? K - k0 : kb;
+        rc = launch_ctemp_batch(ctx->T64, ctx->Y64, ctx->tt, ctx->yy, ctx->colstat, N, D, K, c,
+                                k0, nb, gg ? dgg + k0 : nullptr, lim_scale, scratch, dgsum + k0,
+                                dout + (size_t) 2 * k0, ctx->stream);
+    }
+    if (rc == DGTM_OK && e == cudaSuccess)
+        e = cudaMemcpyAsync(out.data(), dout, sizeof(double) * 2 * K, cudaMemcpyDeviceToHost,
+                            ctx->stream);
+    if (rc == DGTM_OK && e == cudaSuccess)
+        e = cudaMemcpyAsync(gsum.data(), dgsum, sizeof(double) * K, cudaMemcpyDeviceToHost,
+                            ctx->stream);
+    if (rc == DGTM_OK && e == cudaSuccess)
+        e = cudaStreamSynchronize(ctx->stream);
+    cudaFree(scratch);
+    cudaFree(dgsum);
+    cudaFree(dout);
+    cudaFree(dgg);
+    if (rc != DGTM_OK)
+        return rc;
+    if (e != cudaSuccess) {
+        set_error(DGTM_ECUDA, "dgtm_next_ctemp: %s", cudaGetErrorString(e));
+        return DGTM_ECUDA;
+    }
+    // comm/mpicomm.c:582-585, 625-627, 664-669
+    double cmax = -HUGE_VAL;
+    for (int k = 0; k < K; k++) {
+        const double g = gg ? gg[k] : gsum[k];
+        double ck;
+        if (g == 0.0) {
+            ck = HUGE_VAL;
+        } else {
+            const double lmax = out[(size_t) 2 * k] > out[(size_t) 2 * k + 1] ? out[(size_t) 2 * k]
+                                                                              : out[(size_t) 2 * k + 1];
+            ck = beta / 2 / g * lmax;
+        }
+        if (ck > cmax)
+            cmax = ck;
+    }
+    *ctemp = cmax;
+    return DGTM_OK;
 }
 
 int dgtm_get_R_block(dgtm_ctx *ctx, int k0, int nk, int n0, int nn, double *R, int ldR)

@@ -65,6 +65,16 @@ int launch_solve(const double *A, const double *B, int M1, int D, int solver, do
 int launch_update_y(const double *FI, const double *W, const double *G, const double *RT,
                     int K, int M1, int D, double *Y, double *yy, double *bterm,
                     cudaStream_t s);
+// AUTO cooling (ctemp.cu): scratch doubles per batch of kb centres and
+// whether the eigen kernel keeps its D x D block in shared memory.
+size_t ctemp_scratch_doubles(int D, int kb, bool *eig_in_smem);
+// For centres k0 .. k0+kb-1: gsum = row sums of R, out[2 i + w] = largest
+// eigenvalue of 2 S1 (w = 0) / 2 (S1 - S2) (w = 1) below lim_scale * gg_i
+// (eigenvalues at or above it count as 0).  gg_dev null: gg = gsum.
+int launch_ctemp_batch(const double *T, const double *Y, const double *tt, const double *yy,
+                       const double2 *colstat, int N, int D, int K, double c, int k0, int kb,
+                       const double *gg_dev, double lim_scale, double *scratch, double *gsum_dev,
+                       double *out_dev, cudaStream_t s);
 // yy = |y|^2 for a given Y.
 int launch_norms(const double *X, int rows, int D, double *out, cudaStream_t s);
 // out[0] = sum_i v[i] (fixed order) + add; out[1] = num / out[0].

@@ -218,7 +218,7 @@ struct Opts {
     double alpha = 0.99, delta = 0.1, eps = 1e-6, eps2 = 1e-3, start_temp = 1.0, width = 2.0;
     bool need_ctemp = true, isDA = true, checkpointing = true, log_progress = false,
          save_R = false, log_file = false, interpolation = false;
-    int schedule = 0;  // 0 EXP, 1 LINEAR
+    int schedule = 0;  // 0 EXP, 1 LINEAR, 2 AUTO
     unsigned long seed = 0;
     std::string in = "INPUT.h5", out, restart, prefix = "ckp.";
     std::string dT = "T", dX = "X", dFI = "FI", dW = "W", dY = "Y", dR = "R", dbeta = "beta",
@@ -233,7 +233,7 @@ void help()
         "-a number    : alpha (default: 0.99)",
         "-b name      : dataset name for beta (default: beta)",
         "-B name      : dataset name for label (default: lb)",
-        "-c schedule  : cooling schedule [exp|linear] (default : exp)",
+        "-c schedule  : cooling schedule [auto|exp|linear] (default : exp)",
         "-e number    : precision (default: 1e-6)",
         "-f dataset   : dataset name for FI (default: FI)",
         "-F form      : arithmetic [fp64|fp32|bf16x3] (default: fp64)",
@@ -284,7 +284,7 @@ Opts parse(int argc, char **argv)
             else if (!strcasecmp(optarg, "linear"))
                 o.schedule = 1;
             else if (!strcasecmp(optarg, "auto"))
-                die("the AUTO cooling schedule is not part of this build");
+                o.schedule = 2;
             else
                 die("unknown cooling schedule: %s", optarg);
             break;
@@ -613,6 +613,7 @@ int main(int argc, char **argv)
     std::vector<double> queue(QUEUE, DBL_MAX), tr_temp, tr_llh, tr_free;
     double llh = 0, nfree = 0, qual = 0, qual_old = 0, diff = DBL_MAX;
     bool isLast = false, stats_current = false;
+    std::vector<double> G_last;  // G of the last M-step (AUTO schedule)
     int lloop = 0;
     W.assign((size_t) (M + 1) * D, 0.0);
     bool have_W = false;
@@ -684,6 +685,11 @@ int main(int argc, char **argv)
             }
             check(dgtm_mstep(ctx, W.data(), D, nullptr, D, &beta), "dgtm_mstep");
             have_W = true;
+            if (o.schedule == 2) {
+                // the AUTO schedule weighs centres by the G of the last M-step
+                G_last.resize(K);
+                check(dgtm_get_stats(ctx, G_last.data(), nullptr, D), "dgtm_get_stats");
+            }
             stats_current = false;
             if (maxloop && nloop >= maxloop) {
                 isLast = true;
@@ -691,10 +697,21 @@ int main(int argc, char **argv)
             }
         }
         if (o.isDA && !isLast) {
-            if (o.schedule == 1)
+            if (o.schedule == 1) {
                 temp -= o.delta;
-            else
+            } else if (o.schedule == 2) {
+                // dagtm/dagtm.cxx:1919-1934: the next critical temperature, with
+                // the G of the last M-step as the per-centre weights
+                double ct = 0.0;
+                check(dgtm_next_ctemp(ctx, temp, beta, o.eps,
+                                      G_last.empty() ? nullptr : G_last.data(), &ct),
+                      "dgtm_next_ctemp");
+                if (ct >= temp)
+                    ct = temp * o.alpha;  // no valid next critical temperature
+                temp = ct;
+            } else {
                 temp *= o.alpha;
+            }
         } else {
             break;
         }
@@ -720,7 +737,9 @@ int main(int argc, char **argv)
     if (o.isDA) {
         fprintf(g_log, "%20s = %.10g\n", "Start Temp", start_temp);
         fprintf(g_log, "%20s = %.10g\n", "1st Critical Temp", first_ctemp);
-        if (o.schedule == 0) {
+        if (o.schedule == 2) {
+            fprintf(g_log, "%20s = %s\n", "Cooling Schedule", "AUTO");
+        } else if (o.schedule == 0) {
             fprintf(g_log, "%20s = %s\n", "Cooling Schedule", "EXP");
             fprintf(g_log, "%20s = %g\n", "alpha", o.alpha);
         } else {

@@ -133,6 +133,23 @@ int dgtm_get_R_block(dgtm_ctx *ctx, int k0, int nk, int n0, int nn, double *R,
                      int ldR);
 
 /*
+ * Next critical temperature of the AUTO cooling schedule, from the
+ * responsibilities R of the last E-step.  For each centre k, with
+ * x_n = t_n - y_k:  S1 = sum_n R_kn x_n x_n^T, S2 = sum_n R_kn^2 x_n x_n^T,
+ * H_k = [[2 S1 - S2, -S2], [-S2, 2 S1 - S2]]; the eigenvalues of H_k at or
+ * above (temp - eps) gg_k 2 / beta count as 0, ctemp_k = beta / 2 / gg_k
+ * times the largest (HUGE_VAL when gg_k = 0), and *ctemp = max_k ctemp_k.
+ * gg: K weights on the host (the reference passes its G of the last M-step),
+ * or NULL for the row sums of the current R.  FP64.  The work is about
+ * K N D^2 FMA plus K eigenproblems of size D: meant for the problem sizes
+ * the reference runs AUTO on.
+ * Replaces dagtm_mpi_next_ctemp and its helper (comm/mpicomm.c:562-674) with
+ * dagtm_vector_max (comm/comm.c:2149-2161), called at dagtm/dagtm.cxx:1919-1934.
+ */
+int dgtm_next_ctemp(dgtm_ctx *ctx, double temp, double beta, double eps, const double *gg,
+                    double *ctemp);
+
+/*
  * Per-phase device timers, the counterpart of the reference's LOG_TICTOC
  * phase counters (comm/log.h:35-75, printed by logfullWithPID at
  * dagtm/dagtm.cxx:2286).  When enabled, CUDA events bracket each phase on the

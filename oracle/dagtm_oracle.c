@@ -755,6 +755,93 @@ double orc_ctemp(int N, int D, const double *T)
     return lmax * beta;
 }
 
+/* comm/mpicomm.c:562-637 (dagtm_mpi_next_ctemp_helper) for every centre, the
+ * maximum over centres of comm/mpicomm.c:640-674, and the limit filter of
+ * dagtm_vector_max (comm/comm.c:2149-2161).  Written as the reference does it:
+ * Xc = T - y_k, rows scaled by sqrt(r) (S1 = 2 Xc^T Xc), scaled again (S12 =
+ * -Xc^T Xc), S11 = S1 + S12, H = [[S11, S12], [S12, S11]], eigenvalues of the
+ * 2D x 2D H. */
+double orc_next_ctemp(int N, int D, int K, const double *T, const double *Y, const double *R,
+                      const double *gg, double temp, double beta, double eps)
+{
+    const double GG_MIN_ = 1e-250;
+    double *Xc = (double *) malloc(sizeof(double) * (size_t) N * D);
+    double *resp = (double *) malloc(sizeof(double) * (size_t) N);
+    double *S1 = (double *) malloc(sizeof(double) * (size_t) D * D);
+    double *S12 = (double *) malloc(sizeof(double) * (size_t) D * D);
+    double *H = (double *) malloc(sizeof(double) * (size_t) 4 * D * D);
+    double *lam = (double *) malloc(sizeof(double) * (size_t) 2 * D);
+    double cmax = -HUGE_VAL;
+    for (int k = 0; k < K; k++) {
+        const double g = gg[k];
+        double ck;
+        if (g == 0) {
+            ck = HUGE_VAL;
+        } else {
+            for (int n = 0; n < N; n++)
+                for (int d = 0; d < D; d++)
+                    Xc[(size_t) n * D + d] = T[(size_t) n * D + d] - Y[(size_t) k * D + d];
+            for (int n = 0; n < N; n++)
+                resp[n] = sqrt(R[(size_t) k * N + n]);
+            for (int n = 0; n < N; n++)
+                for (int d = 0; d < D; d++)
+                    Xc[(size_t) n * D + d] *= resp[n];
+            for (int i = 0; i < D; i++)
+                for (int j = 0; j < D; j++) {
+                    double acc = 0.0;
+                    for (int n = 0; n < N; n++)
+                        acc += Xc[(size_t) n * D + i] * Xc[(size_t) n * D + j];
+                    S1[(size_t) i * D + j] = 2.0 * acc;
+                }
+            for (int n = 0; n < N; n++)
+                for (int d = 0; d < D; d++)
+                    Xc[(size_t) n * D + d] *= resp[n];
+            for (int i = 0; i < D; i++)
+                for (int j = 0; j < D; j++) {
+                    double acc = 0.0;
+                    for (int n = 0; n < N; n++)
+                        acc += Xc[(size_t) n * D + i] * Xc[(size_t) n * D + j];
+                    S12[(size_t) i * D + j] = -1.0 * acc;
+                }
+            const int D2 = 2 * D;
+            for (int i = 0; i < D; i++)
+                for (int j = 0; j < D; j++) {
+                    const double s11 = S1[(size_t) i * D + j] + S12[(size_t) i * D + j];
+                    const double s12 = S12[(size_t) i * D + j];
+                    H[(size_t) i * D2 + j] = s11;
+                    H[(size_t) (D + i) * D2 + D + j] = s11;
+                    H[(size_t) i * D2 + D + j] = s12;
+                    H[(size_t) (D + i) * D2 + j] = s12;
+                }
+            if (g < GG_MIN_)
+                for (size_t e = 0; e < (size_t) D2 * D2; e++)
+                    H[e] *= 1.0 / GG_MIN_;
+            orc_eig_sym(D2, H, lam);
+            if (g < GG_MIN_)
+                for (int i = 0; i < D2; i++)
+                    lam[i] *= GG_MIN_;
+            const double limit = (temp - eps) * g * 2 / beta;
+            double lmax = -HUGE_VAL;
+            for (int i = 0; i < D2; i++) {
+                if (lam[i] >= limit)
+                    lam[i] = 0.0;
+                if (lam[i] > lmax)
+                    lmax = lam[i];
+            }
+            ck = beta / 2 / g * lmax;
+        }
+        if (ck > cmax)
+            cmax = ck;
+    }
+    free(Xc);
+    free(resp);
+    free(S1);
+    free(S12);
+    free(H);
+    free(lam);
+    return cmax;
+}
+
 /* ------------------------------------------------------------------ */
 /* EM iteration and the annealing loop                                 */
 /* ------------------------------------------------------------------ */

@@ -89,6 +89,10 @@ void orc_sd(int N, int D, const double *T, const double *mu, double *sd);
 double orc_ctemp(int N, int D, const double *T);
 /* Largest eigenvalue helper (cyclic Jacobi), exposed for tests. */
 int orc_eig_sym(int n, const double *S, double *lambda);
+/* Next critical temperature of the AUTO schedule (comm/mpicomm.c:562-674,
+ * comm/comm.c:2149-2161); R is K x N, gg the K weights (vggsub). */
+double orc_next_ctemp(int N, int D, int K, const double *T, const double *Y, const double *R,
+                      const double *gg, double temp, double beta, double eps);
 /* MT19937 stream helper for tests: n uniforms from gsl_rng_set(seed). */
 void orc_mt_uniform(unsigned long seed, int n, double *out);
 

@@ -66,6 +66,7 @@ def lib():
             "orc_sd": (None, [i, i, _dp, _dp, _dp]),
             "orc_ctemp": (d, [i, i, _dp]),
             "orc_eig_sym": (i, [i, _dp, _dp]),
+            "orc_next_ctemp": (d, [i, i, i, _dp, _dp, _dp, _dp, d, d, d]),
             "orc_mt_uniform": (None, [u, i, _dp]),
             "orc_em_iteration": (i, [i, i, i, i, _dp, _dp, _dp, _dp, _dp, i, d,
                                      _dp, _dp, _dp, _dp, _dp, _dp, i]),
@@ -235,6 +236,14 @@ def stp3_rnd(seed, T, L, K, M, s=2.0):
 def ctemp(T):
     T = _c(T)
     return float(lib().orc_ctemp(T.shape[0], T.shape[1], _p(T)))
+
+
+def next_ctemp(T, Y, R, gg, temp, beta, eps):
+    """AUTO schedule: the next critical temperature (R is K x N, gg the K weights)."""
+    T, Y, R, gg = _c(T), _c(Y), _c(R), _c(np.asarray(gg, float))
+    N, D = T.shape
+    K = Y.shape[0]
+    return float(lib().orc_next_ctemp(N, D, K, _p(T), _p(Y), _p(R), _p(gg), temp, beta, eps))
 
 
 def eig_sym(S):

@@ -29,6 +29,6 @@ def test_help_lists_reference_options(built_lib):
 
 
 def test_unsupported_options_are_refused(built_lib):
-    for args in (["-c", "auto"], ["-H"], ["-g", "spacefilling"]):
+    for args in (["-H"], ["-g", "spacefilling"], ["-c", "fast"]):
         out = subprocess.run([DRIVER] + args, capture_output=True, text=True)
         assert out.returncode != 0

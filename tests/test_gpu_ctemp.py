@@ -1,0 +1,97 @@
+"""AUTO cooling: dgtm_next_ctemp against the oracle's restatement of
+dagtm_mpi_next_ctemp (comm/mpicomm.c:562-674).
+
+The oracle builds each centre's 2D x 2D H and takes all its eigenvalues, as
+the reference does; the library takes the two D x D diagonal blocks of H
+after the orthogonal block transform.  The same responsibilities go into both
+(the FP64 form reproduces the oracle's R to ~1e-12), so the critical
+temperatures agree to FP64 eigenvalue accuracy: 1e-9 relative.  The split-BF16
+form's R carries its stated 1e-4 error.
+"""
+import importlib
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def sub(pkg, name):
+    return importlib.import_module(pkg.__name__ + "." + name)
+
+
+def problem(pkg, kind, N, D, K, seed=5):
+    ds = sub(pkg, "datasets")
+    st = sub(pkg, "gtm_setup")
+    if kind == "binary":
+        T = ds.fingerprints(N, D, 8, seed=seed)
+    else:
+        T = ds.gaussian_mixture(N, D, 5, 0.2, seed=seed)
+    L = 2
+    X, FI = st.setup_grid(L, K, 4, 1.0)
+    rng = np.random.default_rng(seed)
+    Y = T[rng.integers(0, N, K)] * 0.6 + 0.2 + 0.05 * rng.standard_normal((K, D))
+    return T, FI, Y
+
+
+def oracle_ctemp(orc, T, Y, beta, temp, eps, gg=None):
+    R, _, _ = orc.resp(orc.dist(Y, T), beta, 1, temp)
+    if gg is None:
+        gg = R.sum(axis=1)
+    return orc.next_ctemp(T, Y, R, gg, temp, beta, eps), R
+
+
+@pytest.mark.parametrize("kind,N,D,K,form,tol", [
+    ("binary", 600, 20, 64, "fp64", 1e-9),
+    ("real", 500, 13, 49, "fp64", 1e-9),
+    ("real", 300, 170, 9, "fp64", 1e-9),     # D x D block beyond shared memory
+    ("binary", 600, 20, 64, "bf16x3", 1e-4),
+])
+def test_next_ctemp_matches_oracle(pkg, orc, kind, N, D, K, form, tol):
+    T, FI, Y = problem(pkg, kind, N, D, K)
+    beta, temp, eps = 30.0 / D, 4.0, 1e-6
+    ref, R = oracle_ctemp(orc, T, Y, beta, temp, eps)
+    with pkg.Context(T, FI, form) as c:
+        c.set_Y(Y)
+        c.estep(beta, 1, temp)
+        got = c.next_ctemp(temp, beta, eps)
+        got_w = c.next_ctemp(temp, beta, eps, gg=R.sum(axis=1))
+    assert np.isfinite(ref) and ref < temp
+    assert got == pytest.approx(ref, rel=tol)
+    assert got_w == pytest.approx(ref, rel=tol)
+
+
+def test_next_ctemp_oil(pkg, orc, golden):
+    T, Y, FI, beta = golden["T"], golden["Y"], golden["FI"], golden["beta"][0]
+    temp, eps = 2.5, 1e-6
+    R, _, _ = orc.resp(orc.dist(Y, T), beta, 1, temp)
+    gg = R.sum(axis=1) * 1.01  # weights other than the current row sums
+    ref = orc.next_ctemp(T, Y, R, gg, temp, beta, eps)
+    with pkg.Context(T, FI, "fp64") as c:
+        c.set_Y(Y)
+        c.estep(beta, 1, temp)
+        got = c.next_ctemp(temp, beta, eps, gg=gg)
+    assert got == pytest.approx(ref, rel=1e-9)
+
+
+def test_zero_weight_gives_huge(pkg):
+    T, FI, Y = problem(pkg, "binary", 256, 16, 25)
+    with pkg.Context(T, FI, "fp64") as c:
+        c.set_Y(Y)
+        c.estep(2.0, 1, 3.0)
+        gg = np.ones(25)
+        gg[3] = 0.0
+        assert c.next_ctemp(3.0, 2.0, 1e-6, gg=gg) == np.inf
+
+
+def test_anneal_auto_cools_monotonically(pkg, orc):
+    T, FI, Y = problem(pkg, "real", 800, 8, 49)
+    with pkg.Context(T, FI, "fp64") as c:
+        c.set_Y(Y)
+        run = pkg.anneal(c, 6.0, 3.0, schedule="auto", alpha=0.9, eps=1e-5, maxloop=80)
+    temps = []
+    for t in run.temp_trace:
+        if not temps or t != temps[-1]:
+            temps.append(t)
+    assert temps[0] == 3.0 and len(temps) >= 2
+    assert all(a > b for a, b in zip(temps, temps[1:]))

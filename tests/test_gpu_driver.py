@@ -98,3 +98,28 @@ def test_signal_forces_a_checkpoint_and_exit(tmp_path):
     assert len(files) == 1
     n = int(H5File(str(files[0])).read("iter")[0])
     assert str(files[0]).endswith(f"sig.{n}.h5")
+
+
+def test_auto_schedule_matches_package_loop(tmp_path, pkg, golden):
+    # -c auto: after each temperature the next one is the critical temperature
+    # of dgtm_next_ctemp (or temp * alpha when none is below the current one)
+    out = run(["-i", OIL_IN, "-o", "auto.h5", "-K", "125", "-L", "3", "-M", "8", "-s", "3",
+               "-j", "60", "-c", "auto", "-a", "0.9", "-e", "1e-3", "-F", "fp64"], tmp_path)
+    assert "Cooling Schedule = AUTO" in " ".join(out.split())
+    tr = trace(out)
+    temps = []
+    for t in tr[:, 3]:
+        if not temps or t != temps[-1]:
+            temps.append(t)
+    assert len(temps) >= 2 and all(a > b for a, b in zip(temps, temps[1:]))
+    st = __import__("importlib").import_module(pkg.__name__ + ".gtm_setup")
+    T = golden["T_in"].astype(np.float64)
+    _, FI0, W0, beta0 = st.random_init(T, 3, 125, 8, 2.0, seed=3)
+    with pkg.Context(T, FI0, "fp64", solver="svd") as c:
+        c.set_Y(FI0 @ W0)
+        ref = pkg.anneal(c, beta0, st.start_temp(T, 0.9), schedule="auto", alpha=0.9, eps=1e-3,
+                         maxloop=60)
+    n = min(len(tr), len(ref.nfree_trace))
+    assert n >= 10
+    assert np.allclose(tr[:n, 3], ref.temp_trace[:n], rtol=1e-6)
+    assert np.allclose(tr[:n, 4], ref.nfree_trace[:n], rtol=1e-5, atol=1e-6)
