@@ -525,6 +525,13 @@ struct P2Params {
 };
 
 constexpr int P2_TILE = 64;  // points per tile (MMA N of the distance product)
+// R T is accumulated in tensor memory over at most this many tiles (4096
+// points) and then moved to the unit's FP32 slot: the tensor pipe's FP32
+// accumulation rounds each MMA's sum down a little, which over a whole
+// 16384-point unit came to ~6e-5 of G and R T (4096 points: ~1e-5).  The
+// first segment of a unit is stored, the later ones are added at L2
+// (round-to-nearest).
+constexpr int P2_SEG_TILES = 64;
 
 // The CTAs take units v = blockIdx.x, blockIdx.x + gridDim.x, ... in point-
 // major order, so at any time all CTAs stream the same few point tiles (which
@@ -575,7 +582,8 @@ __global__ void __launch_bounds__(P2_THREADS, 1)
     uint64_t *rt_full = p_full + 2;
     uint64_t *y_ready = rt_full + 1;       // centres loaded and R T drained
     uint64_t *drain = y_ready + 1;
-    uint32_t *tmem_sh = (uint32_t *) (drain + 1);
+    uint64_t *seg_full = drain + 1;        // a segment's R T is complete in tensor memory
+    uint32_t *tmem_sh = (uint32_t *) (seg_full + 1);
     __shared__ int failed;
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -593,6 +601,7 @@ __global__ void __launch_bounds__(P2_THREADS, 1)
         mbar_init(rt_full, 1);
         mbar_init(y_ready, 256);
         mbar_init(drain, 1);
+        mbar_init(seg_full, 1);
         fence_barrier_init();
     }
     if (warp == 0) {
@@ -655,6 +664,7 @@ __global__ void __launch_bounds__(P2_THREADS, 1)
                 break;
             }
             tc_fence_after();
+            int seg_t = t0;  // the first tile of the segment MMA 2 accumulates
             for (int t = t0; t <= t1; t++) {
                 if (t < t1) {
                     // S = Y T^T for tile jt: M = 128 centres, N = 64 points
@@ -701,10 +711,16 @@ __global__ void __launch_bounds__(P2_THREADS, 1)
                                 mma_ts_w(rt_tmem,
                                          a0 + (uint32_t) ((kk >> 1) * 32 + rp * 16 + (kk & 1) * 8),
                                          bd + (uint64_t) (tp * NP * (TPANEL_BYTES >> 4) + kk * (2048 >> 4)),
-                                         id2, (t - 1 > t0 || rp | tp | kk) ? 1u : 0u);
+                                         id2, (t - 1 > seg_t || rp | tp | kk) ? 1u : 0u);
                         }
                     }
                     mma_commit_w(&t_empty[sp]);
+                    if (t == seg_t + P2_SEG_TILES && t < t1) {
+                        // a segment ends that is not the unit's last: the
+                        // responsibility warps move it out before tile t's MMA 2
+                        mma_commit_w(seg_full);
+                        seg_t = t;
+                    }
                 }
                 if (t < t1) {
                     sp = s;
@@ -728,10 +744,32 @@ __global__ void __launch_bounds__(P2_THREADS, 1)
         const int g = (warp - 2) >> 2;          // point group: points 32 g .. 32 g + 31 of a tile
         const int row = q * 32 + lane;          // centre within the tile
         const uint32_t lane_base = tmem + ((uint32_t) (q * 32) << 16);
-        int jt = 0, s = 0, nunit = 0;
+        // this group's half of the R T accumulator (FP32) to the unit's slot:
+        // stored for a unit's first segment, added at L2 for the later ones;
+        // each slot element has this one writer, in program order
+        auto move_rt = [&](int uslot, bool add) {
+            float *dst = p.RTpart + ((size_t) uslot * P2_BK + row) * DP;
+#pragma unroll 1
+            for (int c0 = g * (DP / 2); c0 < (g + 1) * (DP / 2); c0 += 32) {
+                uint32_t vv[32];
+                tmem_ld32(lane_base + (uint32_t) c0, vv);
+                tmem_ld_wait();
+#pragma unroll
+                for (int j = 0; j < 32; j += 4) {
+                    const float a = __uint_as_float(vv[j]), b = __uint_as_float(vv[j + 1]);
+                    const float c = __uint_as_float(vv[j + 2]), d = __uint_as_float(vv[j + 3]);
+                    if (add)
+                        red_add_f32x4(dst + c0 + j, a, b, c, d);
+                    else
+                        *(float4 *) (dst + c0 + j) = make_float4(a, b, c, d);
+                }
+            }
+        };
+        int jt = 0, s = 0, nunit = 0, nseg = 0;
         uint32_t ph = 0;
         bool ok = true;
         int prev_u = -1;
+        bool prev_add = false;  // the previous unit had more than one segment
         for (int v = blockIdx.x; ok && v < p.nunits; v += gridDim.x) {
             int u, kt, t0, t1;
             unit_of(p, v, u, kt, t0, t1);
@@ -742,18 +780,7 @@ __global__ void __launch_bounds__(P2_THREADS, 1)
                     break;
                 }
                 tc_fence_after();
-                float *dst = p.RTpart + ((size_t) prev_u * P2_BK + row) * DP;
-#pragma unroll 1
-                for (int c0 = g * (DP / 2); c0 < (g + 1) * (DP / 2); c0 += 32) {
-                    uint32_t vv[32];
-                    tmem_ld32(lane_base + (uint32_t) c0, vv);
-                    tmem_ld_wait();
-#pragma unroll
-                    for (int j = 0; j < 32; j += 4)
-                        *(float4 *) (dst + c0 + j) =
-                            make_float4(__uint_as_float(vv[j]), __uint_as_float(vv[j + 1]),
-                                        __uint_as_float(vv[j + 2]), __uint_as_float(vv[j + 3]));
-                }
+                move_rt(prev_u, prev_add);
             }
             // this unit's centre row (group 0: Y hi, group 1: Y lo) into tensor memory;
             // column j holds depths 2 j and 2 j + 1
@@ -778,6 +805,8 @@ __global__ void __launch_bounds__(P2_THREADS, 1)
             tc_fence_before();
             mbar_arrive(y_ready);
             prev_u = u;
+            prev_add = t1 - t0 > P2_SEG_TILES;
+            int seg_r = t0 + P2_SEG_TILES;  // the first tile of the next segment
             for (int t = t0; t < t1; t++, jt++) {
                 const int b = jt & 1;
                 if (!mbar_wait(&t_full[s], ph, p.status, 27) ||
@@ -805,6 +834,18 @@ __global__ void __launch_bounds__(P2_THREADS, 1)
                 tmem_st16(lane_base + col0, hi);
                 tmem_st16(lane_base + col0 + 16, lo);
                 tmem_st_wait();
+                if (t == seg_r) {
+                    // the finished segment out of tensor memory before this tile's
+                    // p_full lets its MMA 2 start the next one over it
+                    if (!mbar_wait(seg_full, (uint32_t) (nseg & 1), p.status, 31)) {
+                        ok = false;
+                        break;
+                    }
+                    nseg++;
+                    tc_fence_after();
+                    move_rt(u, t > t0 + P2_SEG_TILES);
+                    seg_r += P2_SEG_TILES;
+                }
                 tc_fence_before();
                 mbar_arrive(&p_full[b]);
                 if (++s == nstage) {
@@ -820,18 +861,7 @@ __global__ void __launch_bounds__(P2_THREADS, 1)
                 ok = false;
             } else {
                 tc_fence_after();
-                float *dst = p.RTpart + ((size_t) prev_u * P2_BK + row) * DP;
-#pragma unroll 1
-                for (int c0 = g * (DP / 2); c0 < (g + 1) * (DP / 2); c0 += 32) {
-                    uint32_t vv[32];
-                    tmem_ld32(lane_base + (uint32_t) c0, vv);
-                    tmem_ld_wait();
-#pragma unroll
-                    for (int j = 0; j < 32; j += 4)
-                        *(float4 *) (dst + c0 + j) =
-                            make_float4(__uint_as_float(vv[j]), __uint_as_float(vv[j + 1]),
-                                        __uint_as_float(vv[j + 2]), __uint_as_float(vv[j + 3]));
-                }
+                move_rt(prev_u, prev_add);
             }
         }
         if (!ok)

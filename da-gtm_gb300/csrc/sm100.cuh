@@ -331,6 +331,15 @@ __device__ __forceinline__ f2 f2_mul(f2 a, f2 b)
     return r;
 }
 
+// Fire-and-forget FP32 add of four consecutive floats in global memory
+// (performed at L2, round-to-nearest); addr must be 16-byte aligned.
+__device__ __forceinline__ void red_add_f32x4(float *addr, float a, float b, float c, float d)
+{
+    asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(addr), "f"(a), "f"(b), "f"(c),
+                 "f"(d)
+                 : "memory");
+}
+
 // max of three FP32 values in one instruction
 __device__ __forceinline__ float fmax3(float a, float b, float c)
 {
