@@ -526,12 +526,20 @@ struct P2Params {
 
 constexpr int P2_TILE = 64;  // points per tile (MMA N of the distance product)
 // R T is accumulated in tensor memory over at most this many tiles (4096
-// points) and then moved to the unit's FP32 slot: the tensor pipe's FP32
-// accumulation rounds each MMA's sum down a little, which over a whole
-// 16384-point unit came to ~6e-5 of G and R T (4096 points: ~1e-5).  The
-// first segment of a unit is stored, the later ones are added at L2
-// (round-to-nearest).
+// points), a segment.  The tensor pipe's FP32 accumulation rounds each MMA's
+// sum down a little, which over a whole 16384-point unit came to ~6e-5 of G
+// and R T (4096 points: ~1e-5).  A power of two: the MMA warp finds segment
+// starts with a mask.
 constexpr int P2_SEG_TILES = 64;
+static_assert((P2_SEG_TILES & (P2_SEG_TILES - 1)) == 0, "segment length");
+
+// Where the segments of a unit are summed.  With shared memory to spare
+// (128 x (Dp + 4) FP32 beside at least four ring stages) they are summed
+// there in FP32 (round-to-nearest) and the unit's total is stored to its
+// slot.  Otherwise (two data pieces and three panels: the ring would drop to
+// two stages, which measured 1.5x slower) the first segment is stored to
+// the slot and the later ones are added at L2 with red.global.add.
+__host__ __device__ constexpr bool p2_segbuf(int np, int nt) { return nt * np <= 4; }
 
 // The CTAs take units v = blockIdx.x, blockIdx.x + gridDim.x, ... in point-
 // major order, so at any time all CTAs stream the same few point tiles (which
@@ -574,7 +582,12 @@ __global__ void __launch_bounds__(P2_THREADS, 1)
     const int nstage = p.nstage;
     unsigned char *Tst = base;
     float4 *cq = (float4 *) (Tst + nstage * TSTAGE_BYTES);  // nstage x 64
-    uint64_t *bars = (uint64_t *) (cq + nstage * P2_TILE);
+    // the unit's segment sums: 128 rows of DP + 4 floats (the pad spreads a
+    // quarter-warp's float4 accesses to one row each over all banks)
+    constexpr bool SEGBUF = p2_segbuf(NP, NT);
+    constexpr int RB = DP + 4;
+    float *rtbuf = (float *) (cq + nstage * P2_TILE);
+    uint64_t *bars = (uint64_t *) (rtbuf + (SEGBUF ? P2_BK * RB : 0));
     uint64_t *t_full = bars;
     uint64_t *t_empty = bars + nstage;
     uint64_t *s_full = bars + 2 * nstage;  // 2
@@ -582,8 +595,7 @@ __global__ void __launch_bounds__(P2_THREADS, 1)
     uint64_t *rt_full = p_full + 2;
     uint64_t *y_ready = rt_full + 1;       // centres loaded and R T drained
     uint64_t *drain = y_ready + 1;
-    uint64_t *seg_full = drain + 1;        // a segment's R T is complete in tensor memory
-    uint32_t *tmem_sh = (uint32_t *) (seg_full + 1);
+    uint32_t *tmem_sh = (uint32_t *) (drain + 1);
     __shared__ int failed;
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -601,7 +613,6 @@ __global__ void __launch_bounds__(P2_THREADS, 1)
         mbar_init(rt_full, 1);
         mbar_init(y_ready, 256);
         mbar_init(drain, 1);
-        mbar_init(seg_full, 1);
         fence_barrier_init();
     }
     if (warp == 0) {
@@ -664,7 +675,6 @@ __global__ void __launch_bounds__(P2_THREADS, 1)
                 break;
             }
             tc_fence_after();
-            int seg_t = t0;  // the first tile of the segment MMA 2 accumulates
             for (int t = t0; t <= t1; t++) {
                 if (t < t1) {
                     // S = Y T^T for tile jt: M = 128 centres, N = 64 points
@@ -711,16 +721,13 @@ __global__ void __launch_bounds__(P2_THREADS, 1)
                                 mma_ts_w(rt_tmem,
                                          a0 + (uint32_t) ((kk >> 1) * 32 + rp * 16 + (kk & 1) * 8),
                                          bd + (uint64_t) (tp * NP * (TPANEL_BYTES >> 4) + kk * (2048 >> 4)),
-                                         id2, (t - 1 > seg_t || rp | tp | kk) ? 1u : 0u);
+                                         id2, (((uint32_t) (t - 1 - t0) & (P2_SEG_TILES - 1)) != 0u ||
+                                               rp | tp | kk) ? 1u : 0u);
                         }
                     }
+                    // also tells the responsibility warps that a segment's
+                    // R T is complete
                     mma_commit_w(&t_empty[sp]);
-                    if (t == seg_t + P2_SEG_TILES && t < t1) {
-                        // a segment ends that is not the unit's last: the
-                        // responsibility warps move it out before tile t's MMA 2
-                        mma_commit_w(seg_full);
-                        seg_t = t;
-                    }
                 }
                 if (t < t1) {
                     sp = s;
@@ -744,10 +751,15 @@ __global__ void __launch_bounds__(P2_THREADS, 1)
         const int g = (warp - 2) >> 2;          // point group: points 32 g .. 32 g + 31 of a tile
         const int row = q * 32 + lane;          // centre within the tile
         const uint32_t lane_base = tmem + ((uint32_t) (q * 32) << 16);
-        // this group's half of the R T accumulator (FP32) to the unit's slot:
-        // stored for a unit's first segment, added at L2 for the later ones;
-        // each slot element has this one writer, in program order
-        auto move_rt = [&](int uslot, bool add) {
+        // This group's half of row `row` of the R T accumulator (FP32) out of
+        // tensor memory, at the end of a segment (last: the unit's last one;
+        // later: not the unit's first one).  With the shared-memory sums a
+        // segment other than the last is stored or added there, and the last
+        // one, plus the sums, is stored to the unit's slot; without them
+        // every segment goes to the slot, stored or added at L2.  Each element
+        // has this one owner thread, in program order.
+        float *const buf = rtbuf + row * RB;
+        auto move_rt = [&](bool last, bool later, int uslot) {
             float *dst = p.RTpart + ((size_t) uslot * P2_BK + row) * DP;
 #pragma unroll 1
             for (int c0 = g * (DP / 2); c0 < (g + 1) * (DP / 2); c0 += 32) {
@@ -756,20 +768,30 @@ __global__ void __launch_bounds__(P2_THREADS, 1)
                 tmem_ld_wait();
 #pragma unroll
                 for (int j = 0; j < 32; j += 4) {
-                    const float a = __uint_as_float(vv[j]), b = __uint_as_float(vv[j + 1]);
-                    const float c = __uint_as_float(vv[j + 2]), d = __uint_as_float(vv[j + 3]);
-                    if (add)
-                        red_add_f32x4(dst + c0 + j, a, b, c, d);
-                    else
-                        *(float4 *) (dst + c0 + j) = make_float4(a, b, c, d);
+                    float4 x = make_float4(__uint_as_float(vv[j]), __uint_as_float(vv[j + 1]),
+                                           __uint_as_float(vv[j + 2]), __uint_as_float(vv[j + 3]));
+                    if constexpr (SEGBUF) {
+                        if (later) {
+                            const float4 y = *(const float4 *) (buf + c0 + j);
+                            x.x += y.x;
+                            x.y += y.y;
+                            x.z += y.z;
+                            x.w += y.w;
+                        }
+                        *(float4 *) ((last ? dst : buf) + c0 + j) = x;
+                    } else if (later) {
+                        red_add_f32x4(dst + c0 + j, x.x, x.y, x.z, x.w);
+                    } else {
+                        *(float4 *) (dst + c0 + j) = x;
+                    }
                 }
             }
         };
-        int jt = 0, s = 0, nunit = 0, nseg = 0;
+        int jt = 0, s = 0, nunit = 0;
         uint32_t ph = 0;
         bool ok = true;
         int prev_u = -1;
-        bool prev_add = false;  // the previous unit had more than one segment
+        bool prev_multi = false;  // the previous unit had more than one segment
         for (int v = blockIdx.x; ok && v < p.nunits; v += gridDim.x) {
             int u, kt, t0, t1;
             unit_of(p, v, u, kt, t0, t1);
@@ -780,7 +802,7 @@ __global__ void __launch_bounds__(P2_THREADS, 1)
                     break;
                 }
                 tc_fence_after();
-                move_rt(prev_u, prev_add);
+                move_rt(true, prev_multi, prev_u);
             }
             // this unit's centre row (group 0: Y hi, group 1: Y lo) into tensor memory;
             // column j holds depths 2 j and 2 j + 1
@@ -805,7 +827,7 @@ __global__ void __launch_bounds__(P2_THREADS, 1)
             tc_fence_before();
             mbar_arrive(y_ready);
             prev_u = u;
-            prev_add = t1 - t0 > P2_SEG_TILES;
+            prev_multi = t1 - t0 > P2_SEG_TILES;
             int seg_r = t0 + P2_SEG_TILES;  // the first tile of the next segment
             for (int t = t0; t < t1; t++, jt++) {
                 const int b = jt & 1;
@@ -835,15 +857,17 @@ __global__ void __launch_bounds__(P2_THREADS, 1)
                 tmem_st16(lane_base + col0 + 16, lo);
                 tmem_st_wait();
                 if (t == seg_r) {
-                    // the finished segment out of tensor memory before this tile's
-                    // p_full lets its MMA 2 start the next one over it
-                    if (!mbar_wait(seg_full, (uint32_t) (nseg & 1), p.status, 31)) {
+                    // A segment ended with tile t - 1.  Its MMA 2 completes the
+                    // phase of its stage's t_empty that this wait names (the
+                    // next phase needs a p_full not yet given), and this tile's
+                    // p_full lets MMA 2 start the next segment over it.
+                    const int sq = s == 0 ? nstage - 1 : s - 1;
+                    if (!mbar_wait(&t_empty[sq], s == 0 ? ph ^ 1u : ph, p.status, 31)) {
                         ok = false;
                         break;
                     }
-                    nseg++;
                     tc_fence_after();
-                    move_rt(u, t > t0 + P2_SEG_TILES);
+                    move_rt(false, t > t0 + P2_SEG_TILES, u);
                     seg_r += P2_SEG_TILES;
                 }
                 tc_fence_before();
@@ -861,7 +885,7 @@ __global__ void __launch_bounds__(P2_THREADS, 1)
                 ok = false;
             } else {
                 tc_fence_after();
-                move_rt(prev_u, prev_add);
+                move_rt(true, prev_multi, prev_u);
             }
         }
         if (!ok)
@@ -1175,7 +1199,9 @@ int tc_create(TcState **out, int N, int D, int K, int sms, const double *T64, co
     // pass 2: the point-tile ring (T pieces + column statistics); the centres
     // live in tensor memory
     const size_t ts2 = (size_t) st->nT * st->npanel * P2_TILE * 128 + P2_TILE * 16;
-    int ns2 = (int) ((SMEM_LIMIT - 1024 - bar_bytes) / ts2);
+    const size_t rtbuf2 =
+        p2_segbuf(st->npanel, st->nT) ? (size_t) P2_BK * (st->npanel * PANEL_ELEMS + 4) * 4 : 0;
+    int ns2 = (int) ((SMEM_LIMIT - 1024 - bar_bytes - rtbuf2) / ts2);
     if (ns2 > 8)
         ns2 = 8;
     const int klast = st->ksteps - 4 * (st->npanel - 1);
@@ -1191,7 +1217,7 @@ int tc_create(TcState **out, int N, int D, int K, int sms, const double *T64, co
     st->nstage1 = ns1;
     st->nstage2 = ns2;
     st->smem1 = 1024 + (size_t) ns1 * slot1 + bar_bytes;
-    st->smem2 = 1024 + (size_t) ns2 * ts2 + bar_bytes;
+    st->smem2 = 1024 + (size_t) ns2 * ts2 + rtbuf2 + bar_bytes;
     e = cudaFuncSetAttribute(st->pass1, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int) st->smem1);
     if (e == cudaSuccess)

@@ -87,3 +87,36 @@ def test_wide_data_is_refused(pkg):
     with pytest.raises(pkg.DgtmError) as e:
         pkg.Context(T, FI, "bf16x3")
     assert e.value.code == 8
+
+
+# Pass 2 moves R T out of tensor memory every 64 tiles (4096 points); a unit
+# is 256 tiles.  N = 20000 gives one unit of four segments and one of a
+# single segment per centre tile.  Binary D = 166 and real D = 85 sum the
+# segments in shared memory; real D = 150 (two data pieces, three panels)
+# adds them to the slot at L2.
+@pytest.mark.parametrize("D,exact", [(166, True), (85, False), (150, False)],
+                         ids=["binary166-shared", "real85-shared", "real150-l2"])
+def test_multi_segment_units(pkg, orc, D, exact):
+    ds = sub(pkg, "datasets")
+    st = sub(pkg, "gtm_setup")
+    N, K, M = 20000, 125, 8
+    if exact:
+        T = ds.fingerprints(N, D, 12, seed=D)
+    else:
+        T = ds.gaussian_mixture(N, D, 6, 0.15, seed=D)
+    X, FI = st.setup_grid(3, K, M, 1.0)
+    rng = np.random.default_rng(D)
+    Y = T[rng.integers(0, N, K)] * 0.7 + 0.15 + 0.05 * rng.standard_normal((K, D))
+    beta, temp = 40.0 / D, 1.7
+    R, _, _ = orc.resp(orc.dist(Y, T), beta, 1, temp)
+    G, _, _ = orc.mstep_stats(R, FI, T)
+    RT = R @ T
+    with pkg.Context(T, FI, "bf16x3") as c:
+        c.set_Y(Y)
+        c.estep(beta, 1, temp)
+        c.mstep(want_W=False)
+        Gg, RTg = c.get_stats()
+    assert rel(Gg, G) <= 1e-4
+    assert rel(RTg, RT) <= 1e-4
+    assert abs(Gg.sum() - N) / N <= 2e-5
+    assert rel(RTg.sum(axis=0), T.sum(axis=0)) <= 2e-5
