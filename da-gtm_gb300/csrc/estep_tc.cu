@@ -25,14 +25,15 @@
 // copy each finished chunk to registers, release the accumulator and run the
 // online log-sum-exp over k at temperature 1 and at `temp`.
 //
-// Pass 2 (persistent, units of (128 centres) x 16384 points): the CTA
+// Pass 2 (persistent, units of (128 centres) x 16K-40K points): the CTA
 // keeps its 128 centres resident, streams 64-point T tiles, recomputes
 // acc (M = 128 centres, N = 64 points), turns it into R_kn with the pass-1
 // statistics, writes R as BF16 hi/lo back into tensor memory and multiplies
 // R by the same T tile read MN-major (M = 128, N = D padded, K = 16 points),
-// accumulating R T (and, through the column of ones, G = rowsum R) in TMEM.
-// Every unit's FP32 R T is written to its own slot; a fixed-order FP64 sum
-// over the slots gives RT and G.
+// accumulating R T (and, through the column of ones, G = rowsum R) in TMEM
+// over 4096-point segments, which are summed in shared memory.  Every unit's
+// FP32 R T is written to its own slot; a fixed-order sum over the slots
+// (TwoSum, exact to FP64) gives RT and G.
 #include "common.cuh"
 #include "sm100.cuh"
 #include "tc.cuh"
@@ -40,6 +41,9 @@
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <math.h>
+
+#include <algorithm>
+#include <vector>
 
 namespace dgtm {
 
@@ -56,7 +60,6 @@ constexpr int P1_TILE = 128;          // points per tile (MMA M); a CTA holds 1 
 constexpr int P1_BK = 128;            // centres per chunk (MMA N)
 constexpr int PANEL_ELEMS = 64;       // BF16 elements per 128-byte swizzle row
 constexpr int P2_BK = 128;            // centres per CTA (MMA M)
-constexpr int P2_UNIT_POINTS = 16384; // points per output slot
 constexpr int NPAD_ALIGN = 256;       // point padding (two pass-1 tiles)
 constexpr float LOG2E = 1.4426950408889634f;
 constexpr int SMEM_LIMIT = 227 * 1024;
@@ -517,7 +520,7 @@ __global__ void __launch_bounds__(P1_THREADS, 1)
 // pass 2
 // ---------------------------------------------------------------------------
 struct P2Params {
-    int D, Dp, Npad, Kpad, ntiles, units_per_k, ktiles, nunits, nstage;
+    int D, Dp, Npad, Kpad, ntiles, unit_tiles, units_per_k, ktiles, nunits, nstage;
     const uint32_t *Yb;   // 2 x Kpad x Dp BF16 (as BF16 pairs): the centre pieces
     const float4 *colq;   // Npad
     float *RTpart;        // nunits x 128 x Dp
@@ -550,9 +553,8 @@ __device__ __forceinline__ void unit_of(const P2Params &p, int v, int &u, int &k
     const int nu = v / p.ktiles;
     kt = v % p.ktiles;
     u = kt * p.units_per_k + nu;
-    constexpr int per_unit = P2_UNIT_POINTS / P2_TILE;
-    t0 = nu * per_unit;
-    t1 = min(p.ntiles, t0 + per_unit);
+    t0 = nu * p.unit_tiles;
+    t1 = min(p.ntiles, t0 + p.unit_tiles);
 }
 
 // Pass 2, a template on the operand shape like pass 1.  Tensor memory holds
@@ -593,7 +595,7 @@ __global__ void __launch_bounds__(P2_THREADS, 1)
     uint64_t *s_full = bars + 2 * nstage;  // 2
     uint64_t *p_full = s_full + 2;         // 2
     uint64_t *rt_full = p_full + 2;
-    uint64_t *y_ready = rt_full + 1;       // centres loaded and R T drained
+    uint64_t *y_ready = rt_full + 1;       // a unit's centres are in tensor memory
     uint64_t *drain = y_ready + 1;
     uint32_t *tmem_sh = (uint32_t *) (drain + 1);
     __shared__ int failed;
@@ -669,7 +671,8 @@ __global__ void __launch_bounds__(P2_THREADS, 1)
         for (int v = blockIdx.x; ok && v < p.nunits; v += gridDim.x) {
             int u, kt, t0, t1;
             unit_of(p, v, u, kt, t0, t1);
-            // the unit's centres are in tensor memory and the R T accumulator is free
+            // the unit's centres are in tensor memory; its first MMA 2 waits on
+            // a p_full given after the previous unit's R T has left
             if (!mbar_wait_w(y_ready, nunit & 1, p.status, 23)) {
                 ok = false;
                 break;
@@ -753,14 +756,17 @@ __global__ void __launch_bounds__(P2_THREADS, 1)
         const uint32_t lane_base = tmem + ((uint32_t) (q * 32) << 16);
         // This group's half of row `row` of the R T accumulator (FP32) out of
         // tensor memory, at the end of a segment (last: the unit's last one;
-        // later: not the unit's first one).  With the shared-memory sums a
-        // segment other than the last is stored or added there, and the last
-        // one, plus the sums, is stored to the unit's slot; without them
-        // every segment goes to the slot, stored or added at L2.  Each element
-        // has this one owner thread, in program order.
+        // later: not the unit's first one).  With the shared-memory sums the
+        // segment is stored or added there, and after the unit's last one the
+        // thread's half row (384 B at D_p = 192) goes to the unit's slot as one
+        // bulk copy by the TMA engine.  Without them every segment goes to the
+        // slot, stored or added at L2.  Each element has this one owner
+        // thread, in program order.
         float *const buf = rtbuf + row * RB;
         auto move_rt = [&](bool last, bool later, int uslot) {
             float *dst = p.RTpart + ((size_t) uslot * P2_BK + row) * DP;
+            if constexpr (SEGBUF)
+                bulk_wait_read();  // the previous unit's copy has left the half row
 #pragma unroll 1
             for (int c0 = g * (DP / 2); c0 < (g + 1) * (DP / 2); c0 += 32) {
                 uint32_t vv[32];
@@ -778,7 +784,7 @@ __global__ void __launch_bounds__(P2_THREADS, 1)
                             x.z += y.z;
                             x.w += y.w;
                         }
-                        *(float4 *) ((last ? dst : buf) + c0 + j) = x;
+                        *(float4 *) (buf + c0 + j) = x;
                     } else if (later) {
                         red_add_f32x4(dst + c0 + j, x.x, x.y, x.z, x.w);
                     } else {
@@ -786,48 +792,49 @@ __global__ void __launch_bounds__(P2_THREADS, 1)
                     }
                 }
             }
+            if constexpr (SEGBUF) {
+                if (last) {
+                    fence_proxy_async_smem();
+                    bulk_store(dst + g * (DP / 2), buf + g * (DP / 2), (uint32_t) (DP / 2 * 4));
+                    bulk_commit();
+                }
+            }
+        };
+        // The centre row of centre tile ktc (group 0: Y hi, group 1: Y lo) into
+        // tensor memory, column j holding depths 2 j and 2 j + 1, then y_ready.
+        // Every load is issued before the first store: one L2 round trip.
+        auto load_y = [&](int ktc) {
+            const uint4 *src =
+                (const uint4 *) (p.Yb + ((size_t) g * p.Kpad + (size_t) ktc * P2_BK + row) * (DP / 2));
+            uint4 x[YCOLS / 4];
+#pragma unroll
+            for (int i = 0; i < YCOLS / 4; i++)
+                x[i] = src[i];
+#pragma unroll
+            for (int c0 = 0; c0 < YCOLS; c0 += 16) {
+                uint32_t w[16];
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    w[4 * i] = x[c0 / 4 + i].x;
+                    w[4 * i + 1] = x[c0 / 4 + i].y;
+                    w[4 * i + 2] = x[c0 / 4 + i].z;
+                    w[4 * i + 3] = x[c0 / 4 + i].w;
+                }
+                tmem_st16(lane_base + (uint32_t) (Y_COL + g * YCOLS + c0), w);
+            }
+            tmem_st_wait();
+            tc_fence_before();
+            mbar_arrive(y_ready);
         };
         int jt = 0, s = 0, nunit = 0;
         uint32_t ph = 0;
         bool ok = true;
-        int prev_u = -1;
-        bool prev_multi = false;  // the previous unit had more than one segment
         for (int v = blockIdx.x; ok && v < p.nunits; v += gridDim.x) {
             int u, kt, t0, t1;
             unit_of(p, v, u, kt, t0, t1);
-            if (nunit > 0) {
-                // drain the previous unit's R T (FP32) to its slot; the groups split the columns
-                if (!mbar_wait(rt_full, (nunit - 1) & 1, p.status, 29)) {
-                    ok = false;
-                    break;
-                }
-                tc_fence_after();
-                move_rt(true, prev_multi, prev_u);
-            }
-            // this unit's centre row (group 0: Y hi, group 1: Y lo) into tensor memory;
-            // column j holds depths 2 j and 2 j + 1
-            {
-                const uint4 *src =
-                    (const uint4 *) (p.Yb + ((size_t) g * p.Kpad + (size_t) kt * P2_BK + row) * (DP / 2));
-#pragma unroll 1
-                for (int c0 = 0; c0 < YCOLS; c0 += 16) {
-                    uint32_t w[16];
-#pragma unroll
-                    for (int i = 0; i < 4; i++) {
-                        const uint4 x = src[c0 / 4 + i];
-                        w[4 * i] = x.x;
-                        w[4 * i + 1] = x.y;
-                        w[4 * i + 2] = x.z;
-                        w[4 * i + 3] = x.w;
-                    }
-                    tmem_st16(lane_base + (uint32_t) (Y_COL + g * YCOLS + c0), w);
-                }
-                tmem_st_wait();
-            }
-            tc_fence_before();
-            mbar_arrive(y_ready);
-            prev_u = u;
-            prev_multi = t1 - t0 > P2_SEG_TILES;
+            if (nunit == 0)
+                load_y(kt);
+            const bool multi = t1 - t0 > P2_SEG_TILES;
             int seg_r = t0 + P2_SEG_TILES;  // the first tile of the next segment
             for (int t = t0; t < t1; t++, jt++) {
                 const int b = jt & 1;
@@ -877,17 +884,28 @@ __global__ void __launch_bounds__(P2_THREADS, 1)
                     ph ^= 1u;
                 }
             }
+            if (!ok)
+                break;
+            // Every MMA 1 of this unit has completed (the s_full of its last
+            // tile), so the next unit's centres can replace these at once and
+            // its distance products start while this unit's R T drains.  That
+            // unit's first MMA 2 waits on a p_full given after the drain.
+            const int vn = v + gridDim.x;
+            if (vn < p.nunits) {
+                int un, ktn, t0n, t1n;
+                unit_of(p, vn, un, ktn, t0n, t1n);
+                load_y(ktn);
+            }
+            if (!mbar_wait(rt_full, nunit & 1, p.status, 29)) {
+                ok = false;
+                break;
+            }
+            tc_fence_after();
+            move_rt(true, multi, u);
             nunit++;
         }
-        if (ok && nunit > 0) {
-            // the last unit's R T
-            if (!mbar_wait(rt_full, (nunit - 1) & 1, p.status, 29)) {
-                ok = false;
-            } else {
-                tc_fence_after();
-                move_rt(true, prev_multi, prev_u);
-            }
-        }
+        if constexpr (SEGBUF)
+            bulk_wait();
         if (!ok)
             failed = 1;
     }
@@ -1066,11 +1084,41 @@ P1Kernel pass1_for(int np, int kl, int nt)
 
 }  // namespace
 
+// Pass-2 unit length in tiles.  CTA b takes units v = b, b + grid, ...; a
+// unit boundary costs about four tiles' time (pipeline drain, centre reload,
+// R T drain) and each unit adds a slot to the final sum (~0.02 tile-times).
+// Among whole-segment lengths of 256..640 tiles (16K..40K points) take the
+// one that minimises the busiest CTA's tiles + 4 x its units, + 0.02 x all
+// units.  At N = 1M, K = 8000 on 152 SMs that is 384 tiles, which measured
+// fastest of 256 / 384 / 512 / 640 (5.56 ms against 5.72 / 5.65 / 5.63).
+static int p2_unit_tiles(int ntiles, int ktiles, int grid_max)
+{
+    int best = 256;
+    double best_cost = 0.0;
+    std::vector<long> work;
+    for (int ut = 256; ut <= 640; ut += P2_SEG_TILES) {
+        const long upk = (ntiles + ut - 1) / ut;
+        const long nunits = upk * ktiles;
+        const int grid = nunits < grid_max ? (int) nunits : grid_max;
+        work.assign((size_t) grid, 0);
+        for (long v = 0; v < nunits; v++) {
+            const long t0 = (v / ktiles) * ut;
+            work[(size_t) (v % grid)] += std::min<long>(ntiles - t0, ut) + 4;
+        }
+        const double cost = (double) *std::max_element(work.begin(), work.end()) + 0.02 * (double) nunits;
+        if (ut == 256 || cost < best_cost) {
+            best_cost = cost;
+            best = ut;
+        }
+    }
+    return best;
+}
+
 struct TcState {
     int N, D, K, sms;
     int Dp, npanel, Npad, Kpad, nT, ksteps;
     int nchunk, nstage1, nstage2, ntile1, bn2;
-    int ntiles2, units_per_k, nunits, grid2;
+    int ntiles2, unit_tiles, units_per_k, nunits, grid2;
     size_t smem1, smem2;
     P1Kernel pass1;
     P2Kernel pass2;
@@ -1154,8 +1202,9 @@ int tc_create(TcState **out, int N, int D, int K, int sms, const double *T64, co
     const size_t tpl = (size_t) st->Npad * st->Dp, ypl = (size_t) st->Kpad * st->Dp;
     // pass 2 work units
     st->ntiles2 = st->Npad / st->bn2;
-    st->units_per_k = (st->Npad + P2_UNIT_POINTS - 1) / P2_UNIT_POINTS;
     const int ktiles2 = (K + P2_BK - 1) / P2_BK;
+    st->unit_tiles = p2_unit_tiles(st->ntiles2, ktiles2, sms);
+    st->units_per_k = (st->ntiles2 + st->unit_tiles - 1) / st->unit_tiles;
     st->nunits = ktiles2 * st->units_per_k;
     st->grid2 = st->nunits < sms ? st->nunits : sms;
 
@@ -1300,6 +1349,7 @@ int tc_mstep_pass(TcState *st, const double2 *, double, cudaStream_t s, int *nla
     p.Npad = st->Npad;
     p.Kpad = st->Kpad;
     p.ntiles = st->ntiles2;
+    p.unit_tiles = st->unit_tiles;
     p.units_per_k = st->units_per_k;
     p.ktiles = (st->K + P2_BK - 1) / P2_BK;
     p.nunits = st->nunits;

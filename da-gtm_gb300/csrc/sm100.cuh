@@ -108,6 +108,32 @@ __device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t b
         : "memory");
 }
 
+// Shared -> global copy of `bytes` by the TMA engine, in this thread's bulk
+// group; both addresses 16-byte aligned, bytes a multiple of 16.  The
+// thread's earlier generic writes to the source need fence_proxy_async_smem
+// first.
+__device__ __forceinline__ void bulk_store(void *dst, const void *src, uint32_t bytes)
+{
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"((uint64_t) dst),
+                 "r"(smem_u32(src)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+
+// this thread's bulk stores have read their shared-memory sources
+__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+
+// this thread's bulk stores have completed
+__device__ __forceinline__ void bulk_wait() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+
+// orders this thread's generic-proxy shared-memory writes before later
+// async-proxy (TMA) reads of them
+__device__ __forceinline__ void fence_proxy_async_smem()
+{
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
 __device__ __forceinline__ void prefetch_tmap(const void *tmap)
 {
     asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t) tmap) : "memory");
