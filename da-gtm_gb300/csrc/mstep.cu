@@ -187,6 +187,7 @@ int launch_form_ab(const double *FI, const double *G, const double *RT, int K, i
 // ---------------------------------------------------------------------------
 constexpr int SOLVE_THREADS = 512;
 constexpr int SMEM_SOLVE_MAX = 110;  // M1 up to which L lives in shared memory
+constexpr int TRI_MAXR = 8;  // registers per lane in the substitution: M1 <= 256
 
 // 1/sqrt(d) for a positive normal d: an FP32 estimate refined by two
 // Newton-Raphson steps for f(r) = 1/r^2 - d, r <- r (3 - d r^2) / 2 (each
@@ -203,88 +204,106 @@ __device__ __forceinline__ double rsqrt_nr(double d)
     return r;
 }
 
-// Right-looking Cholesky in one block: per column j, the pivot's reciprocal
-// square root (thread 0), the scaled column, then the rank-1 update of the
-// trailing lower triangle by all threads.  A pivot that keeps less than
-// CHOL_DROP of its diagonal (the column adds no new direction at FP64
-// precision) is dropped: its diagonal and column are stored as 0 and that
-// unknown is fixed at 0, which keeps the solve defined when
+// Right-looking Cholesky in one block, one barrier per column.  Thread t
+// owns rows i = t/4, t/4 + 64, ... and in each the columns k = t (mod 4).
+// Column j stays unscaled while it is in use: after the barrier of step j
+// every thread reads the pivot's reciprocal square root r_j, updates its
+// trailing elements as L[i][k] -= (a_ij r_j^2) a_kj (a: the unscaled column
+// j), and the scaled a_ij r_j goes to the unused upper triangle at [j][i].
+// The next pivot is the first element its owner updates in a step; the
+// owner takes its reciprocal square root and publishes it before its other
+// rows.  A last pass moves the scaled columns to the lower triangle.  A pivot
+// that keeps less than CHOL_DROP of its diagonal (the column adds no new
+// direction at FP64 precision) is dropped: its diagonal and column are stored
+// as 0 and that unknown is fixed at 0, which keeps the solve defined when
 // A = FI^T diag(G) FI is numerically singular (wide basis functions).
 // L (lower triangle) goes to work[0 .. M1*M1), the reciprocal diagonal to
 // work[M1*M1 .. M1*M1 + M1) (0 for a dropped pivot); flag[1] counts the drops.
 constexpr double CHOL_DROP = 1e-12;
+constexpr int CHOL_THREADS = 256;
 
-__global__ void __launch_bounds__(SOLVE_THREADS) cholesky_kernel(const double *__restrict__ A,
-                                                                int M1, double *__restrict__ work,
-                                                                int *flag)
+__device__ __forceinline__ void chol_pivot(double *L, const double *adiag, int M1, int j,
+                                           double *rinv, int *bad, int *ndrop)
+{
+    const size_t jj = (size_t) j * M1 + j;
+    const double d = L[jj], ajj = adiag[j];
+    double r = 0.0;
+    if (!isfinite(d)) {
+        *bad = 1;
+        L[jj] = 0.0;
+    } else if (!(d > CHOL_DROP * ajj)) {
+        (*ndrop)++;
+        L[jj] = 0.0;  // marks a dropped unknown
+    } else {
+        r = rsqrt_nr(d);
+        L[jj] = d * r;
+    }
+    rinv[j] = r;
+}
+
+__global__ void __launch_bounds__(CHOL_THREADS) cholesky_kernel(const double *__restrict__ A,
+                                                               int M1, double *__restrict__ work,
+                                                               int *flag)
 {
     extern __shared__ double sh[];
     double *L = (M1 <= SMEM_SOLVE_MAX) ? sh : work;
-    double *inv = work + (size_t) M1 * M1;
+    __shared__ double rinv[32 * TRI_MAXR], adiag[32 * TRI_MAXR];  // pivots: 1/sqrt, A's diagonal
     __shared__ int bad, ndrop;
-    __shared__ double rj;
-    if (threadIdx.x == 0) {
+    const int tid = threadIdx.x, q = tid & 3, r0 = tid >> 2;
+    const size_t n2 = (size_t) M1 * M1;
+    if (tid == 0) {
         bad = 0;
         ndrop = 0;
     }
-    for (int i = threadIdx.x; i < M1 * M1; i += blockDim.x)
-        L[i] = A[i];
+#pragma unroll 4
+    for (size_t e = tid; e < n2; e += CHOL_THREADS)
+        L[e] = A[e];
+    for (int j = tid; j < M1; j += CHOL_THREADS)
+        adiag[j] = A[(size_t) j * M1 + j];
     __syncthreads();
+    if (tid == 0)
+        chol_pivot(L, adiag, M1, 0, rinv, &bad, &ndrop);
     for (int j = 0; j < M1; j++) {
-        if (threadIdx.x == 0) {
-            const double d = L[(size_t) j * M1 + j], ajj = A[(size_t) j * M1 + j];
-            double r = 0.0;
-            if (!isfinite(d)) {
-                bad = 1;
-                L[(size_t) j * M1 + j] = 0.0;
-            } else if (!(d > CHOL_DROP * ajj)) {
-                ndrop++;
-                L[(size_t) j * M1 + j] = 0.0;  // marks a dropped unknown
-            } else {
-                r = rsqrt_nr(d);
-                L[(size_t) j * M1 + j] = d * r;
-            }
-            inv[j] = r;
-            rj = r;
+        __syncthreads();
+        const double rj = rinv[j], r2 = rj * rj;
+        for (int i = r0; i < M1; i += 64) {
+            if (i <= j)
+                continue;
+            const double aij = L[(size_t) i * M1 + j];
+            if (q == 0)
+                L[(size_t) j * M1 + i] = aij * rj;
+            const double ti = aij * r2;
+            for (int k = j + 1 + ((q - j - 1) & 3); k <= i; k += 4)
+                L[(size_t) i * M1 + k] = fma(-ti, L[(size_t) k * M1 + j], L[(size_t) i * M1 + k]);
+            if (i == j + 1 && q == ((j + 1) & 3))
+                chol_pivot(L, adiag, M1, j + 1, rinv, &bad, &ndrop);
         }
-        __syncthreads();
-        const double r = rj;
-        for (int i = j + 1 + threadIdx.x; i < M1; i += blockDim.x)
-            L[(size_t) i * M1 + j] *= r;
-        __syncthreads();
-        // L[i][k] -= L[i][j] L[k][j] for j < k <= i, packed over the triangle
-        const int n = M1 - 1 - j;
-        const int npair = n * (n + 1) / 2;
-        for (int t = threadIdx.x; t < npair; t += blockDim.x) {
-            // row offset ii with ii (ii + 1) / 2 <= t
-            int ii = (int) ((sqrtf(8.0f * (float) t + 1.0f) - 1.0f) * 0.5f);
-            while ((ii + 1) * (ii + 2) / 2 <= t)
-                ii++;
-            while (ii * (ii + 1) / 2 > t)
-                ii--;
-            const int kk = t - ii * (ii + 1) / 2;
-            const int i = j + 1 + ii, k = j + 1 + kk;
-            L[(size_t) i * M1 + k] -= L[(size_t) i * M1 + j] * L[(size_t) k * M1 + j];
-        }
-        __syncthreads();
     }
-    if (L != work)
-        for (int i = threadIdx.x; i < M1 * M1; i += blockDim.x)
-            work[i] = L[i];
-    if (threadIdx.x == 0) {
+    __syncthreads();
+    for (size_t e = tid; e < n2; e += CHOL_THREADS) {
+        const int i = (int) (e / M1), k = (int) (e % M1);
+        if (k < i)
+            work[e] = L[(size_t) k * M1 + i];
+        else if (k == i)
+            work[e] = L[e];
+    }
+    for (int j = tid; j < M1; j += CHOL_THREADS)
+        work[n2 + j] = rinv[j];
+    if (tid == 0) {
         flag[0] = bad ? DGTM_ENONFINITE : 0;
         flag[1] = ndrop;
     }
 }
 
 // Forward (L y = b) and back (L^T w = y) substitution, right-looking: one warp
-// per right-hand side (column of B), lane l holding entries l, l + 32, ...;
-// step i broadcasts the finished entry i and every lane updates its later
-// (forward) or earlier (back) entries with one FMA.  Many blocks, so the D
-// columns run on many SMs.
+// per right-hand side (column of B), lane l holding entries l, l + 32, ...
+// in NR = ceil(M1 / 32) registers; step i broadcasts the finished entry i and
+// every lane updates the registers that can still hold later (forward) or
+// earlier (back) entries with one FMA each.  Many blocks, so the D columns
+// run on many SMs.
 constexpr int TRI_WARPS = 4;
-constexpr int TRI_MAXR = 8;  // entries per lane: M1 <= 256
 
+template <int NR>
 __global__ void __launch_bounds__(TRI_WARPS * 32) tri_solve_kernel(const double *__restrict__ Lg,
                                                                   const double *__restrict__ B,
                                                                   int M1, int D, int l_in_smem,
@@ -297,7 +316,9 @@ __global__ void __launch_bounds__(TRI_WARPS * 32) tri_solve_kernel(const double 
     const double *L = Lg;
     const double *inv = Lg + (size_t) M1 * M1;
     if (l_in_smem) {
-        for (int i = threadIdx.x; i < M1 * M1 + M1; i += blockDim.x)
+        const size_t n = (size_t) M1 * M1 + M1;
+#pragma unroll 8
+        for (size_t i = threadIdx.x; i < n; i += blockDim.x)
             sh[i] = Lg[i];
         __syncthreads();
         L = sh;
@@ -307,24 +328,22 @@ __global__ void __launch_bounds__(TRI_WARPS * 32) tri_solve_kernel(const double 
     const int c = blockIdx.x * TRI_WARPS + warp;
     if (c >= D)
         return;
-    double x[TRI_MAXR];
+    double x[NR];
 #pragma unroll
-    for (int r = 0; r < TRI_MAXR; r++) {
+    for (int r = 0; r < NR; r++) {
         const int p = lane + 32 * r;
         x[r] = (p < M1) ? B[(size_t) p * D + c] : 0.0;
     }
     // forward: y_i = x_i / L_ii, then x_p -= L_pi y_i for p > i; entry i sits
-    // in register rb = i / 32 of lane i % 32 (rb a constant after unrolling)
+    // in register rb = i / 32 of lane i % 32, and only registers rb.. hold p > i
 #pragma unroll
-    for (int rb = 0; rb < TRI_MAXR; rb++) {
-        if (32 * rb >= M1)
-            break;
+    for (int rb = 0; rb < NR; rb++) {
         const int iend = min(32, M1 - 32 * rb);
         for (int il = 0; il < iend; il++) {
             const int i = 32 * rb + il;
             const double yi = __shfl_sync(0xffffffffu, x[rb], il) * inv[i];
 #pragma unroll
-            for (int r = 0; r < TRI_MAXR; r++) {
+            for (int r = rb; r < NR; r++) {
                 const int p = lane + 32 * r;
                 if (p == i)
                     x[r] = yi;
@@ -333,17 +352,15 @@ __global__ void __launch_bounds__(TRI_WARPS * 32) tri_solve_kernel(const double 
             }
         }
     }
-    // back: w_i = y_i / L_ii, then y_p -= L_ip w_i for p < i
+    // back: w_i = y_i / L_ii, then y_p -= L_ip w_i for p < i (registers ..rb)
 #pragma unroll
-    for (int rb = TRI_MAXR - 1; rb >= 0; rb--) {
-        if (32 * rb >= M1)
-            continue;
+    for (int rb = NR - 1; rb >= 0; rb--) {
         const int iend = min(32, M1 - 32 * rb);
         for (int il = iend - 1; il >= 0; il--) {
             const int i = 32 * rb + il;
             const double wi = __shfl_sync(0xffffffffu, x[rb], il) * inv[i];
 #pragma unroll
-            for (int r = 0; r < TRI_MAXR; r++) {
+            for (int r = 0; r <= rb; r++) {
                 const int p = lane + 32 * r;
                 if (p == i)
                     x[r] = wi;
@@ -353,10 +370,26 @@ __global__ void __launch_bounds__(TRI_WARPS * 32) tri_solve_kernel(const double 
         }
     }
 #pragma unroll
-    for (int r = 0; r < TRI_MAXR; r++) {
+    for (int r = 0; r < NR; r++) {
         const int p = lane + 32 * r;
         if (p < M1)
             W[(size_t) p * D + c] = x[r];
+    }
+}
+
+using TriKernel = void (*)(const double *, const double *, int, int, int, const int *, double *);
+
+TriKernel tri_solve_for(int nr)
+{
+    switch (nr) {
+    case 1: return tri_solve_kernel<1>;
+    case 2: return tri_solve_kernel<2>;
+    case 3: return tri_solve_kernel<3>;
+    case 4: return tri_solve_kernel<4>;
+    case 5: return tri_solve_kernel<5>;
+    case 6: return tri_solve_kernel<6>;
+    case 7: return tri_solve_kernel<7>;
+    default: return tri_solve_kernel<8>;
     }
 }
 
@@ -491,15 +524,15 @@ int launch_solve(const double *A, const double *B, int M1, int D, int solver, do
         DGTM_CUDA_TRY(cudaFuncSetAttribute(cholesky_kernel,
                                            cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int) (smem > 0 ? smem : 1)));
-        cholesky_kernel<<<1, SOLVE_THREADS, smem, s>>>(A, M1, work, flag);
+        cholesky_kernel<<<1, CHOL_THREADS, smem, s>>>(A, M1, work, flag);
         DGTM_CUDA_TRY(cudaGetLastError());
         const size_t lbytes = sizeof(double) * ((size_t) M1 * M1 + M1);
         const int l_in_smem = lbytes <= 96 * 1024;
         const size_t tsmem = l_in_smem ? lbytes : 16;
-        DGTM_CUDA_TRY(cudaFuncSetAttribute(tri_solve_kernel,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int) tsmem));
-        tri_solve_kernel<<<ceil_div(D, TRI_WARPS), TRI_WARPS * 32, tsmem, s>>>(work, B, M1, D,
-                                                                             l_in_smem, flag, W);
+        const TriKernel tri = tri_solve_for(ceil_div(M1, 32));
+        DGTM_CUDA_TRY(cudaFuncSetAttribute(tri, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int) tsmem));
+        tri<<<ceil_div(D, TRI_WARPS), TRI_WARPS * 32, tsmem, s>>>(work, B, M1, D, l_in_smem, flag, W);
     }
     DGTM_CUDA_TRY(cudaGetLastError());
     return DGTM_OK;
