@@ -34,7 +34,7 @@ ERRORS = {1: "EINVAL", 2: "ECUDA", 3: "ENOTSPD", 4: "ENONFINITE", 5: "ETIMEOUT",
 ABI_SYMBOLS = ("dgtm_version", "dgtm_last_error_string", "dgtm_ctx_create", "dgtm_ctx_destroy",
                "dgtm_set_solver", "dgtm_set_Y", "dgtm_get_Y", "dgtm_get_W", "dgtm_estep",
                "dgtm_mstep", "dgtm_get_stats", "dgtm_map", "dgtm_get_R_block", "dgtm_next_ctemp",
-               "dgtm_set_timing",
+               "dgtm_next_ctemp_k", "dgtm_set_timing",
                "dgtm_reset_timing", "dgtm_get_timing", "dgtm_get_stream", "dgtm_selftest",
                "dgtm_fe_workspace_size", "dgtm_fe_forward", "dgtm_fe_backward",
                "dgtm_fe_forward_noalloc")
@@ -77,6 +77,7 @@ def load_library(path: str = LIB_PATH):
         "dgtm_map": (i, [vp, _dp, i, _dp, i]),
         "dgtm_get_R_block": (i, [vp, i, i, i, i, _dp, i]),
         "dgtm_next_ctemp": (i, [vp, d, d, d, _dp, _dp]),
+        "dgtm_next_ctemp_k": (i, [vp, d, d, d, _dp, _dp, _dp]),
         "dgtm_set_timing": (i, [vp, i]),
         "dgtm_reset_timing": (i, [vp]),
         "dgtm_get_timing": (i, [vp, _dp, ctypes.POINTER(ctypes.c_longlong),
@@ -134,12 +135,31 @@ class Context:
         self.N, self.D = T.shape
         self.K, self.M1 = FI.shape
         self.precision = precision
+        self.solver = solver
+        self._create(T, FI)
+
+    def _create(self, T, FI):
         h = ctypes.c_void_p()
-        _check(lib.dgtm_ctx_create(self.N, self.D, self.K, self.M1, _p(T), self.D, _p(FI),
-                                   self.M1, PRECISIONS[precision], ctypes.byref(h)))
+        _check(load_library().dgtm_ctx_create(self.N, self.D, self.K, self.M1, _p(T), self.D,
+                                              _p(FI), self.M1, PRECISIONS[self.precision],
+                                              ctypes.byref(h)))
         self._h = h
-        if solver != "cholesky":
-            self.set_solver(solver)
+        if self.solver != "cholesky":
+            self.set_solver(self.solver)
+
+    def set_basis(self, T, FI, Y):
+        """A new latent basis FI (K' x M1, same M1) on the same data T, with
+        centres Y (K' x D): the context is rebuilt in place for K'.  This is
+        the hierarchical schedule's grid expansion (dagtm/dagtm.cxx:2110-2144:
+        new X and FI, K-sized buffers reallocated, Y = FI W)."""
+        T = _f64(T)
+        FI = _f64(FI)
+        if T.shape != (self.N, self.D) or FI.ndim != 2 or FI.shape[1] != self.M1:
+            raise ValueError("set_basis: T must be the context's data and FI K' x M1")
+        self.close()
+        self.K = FI.shape[0]
+        self._create(T, FI)
+        self.set_Y(Y)
 
     # life cycle
     def close(self):
@@ -235,18 +255,27 @@ class Context:
         _check(load_library().dgtm_get_R_block(self._h, k0, nk, n0, nn, _p(R), nn))
         return R
 
-    def next_ctemp(self, temp: float, beta: float, eps: float, gg=None) -> float:
+    def next_ctemp(self, temp: float, beta: float, eps: float, gg=None,
+                   per_centre: bool = False):
         """Next critical temperature (AUTO cooling) from the last E-step's R;
-        gg: per-centre weights (the G of the last M-step), None: row sums of R."""
+        gg: per-centre weights (the G of the last M-step), None: row sums of R.
+        per_centre: also return every centre's ctemp_k (the reference's vctemp)."""
         out = ctypes.c_double()
         g = None if gg is None else _f64(np.asarray(gg).reshape(self.K))
-        _check(load_library().dgtm_next_ctemp(self._h, float(temp), float(beta), float(eps),
-                                              _p(g) if g is not None else None,
-                                              ctypes.byref(out)))
-        return out.value
+        ck = np.empty(self.K) if per_centre else None
+        _check(load_library().dgtm_next_ctemp_k(self._h, float(temp), float(beta), float(eps),
+                                                _p(g) if g is not None else None,
+                                                _p(ck) if ck is not None else None,
+                                                ctypes.byref(out)))
+        return (out.value, ck) if per_centre else out.value
 
 
 QUEUE_SIZE = 50  # dagtm/dagtm.cxx:45 INIT_QUEUE_SIZE
+
+
+def _gtm_setup():
+    import importlib
+    return importlib.import_module(__name__ + ".gtm_setup")
 
 
 @dataclass
@@ -259,35 +288,57 @@ class RunResult:
     temp: float = 1.0
     nloop: int = 0
     W: np.ndarray | None = None
+    expansions: list = field(default_factory=list)  # HDA: (iteration, K before, K after)
 
 
 def anneal(ctx: Context, beta: float, temp: float, isDA: int = 1, schedule: str = "exp",
            alpha: float = 0.99, delta: float = 0.1, eps: float = 1e-6, iter0: int = 0,
-           maxloop: int = 0, log=None) -> RunResult:
-    """Temperature loop of dagtm/dagtm.cxx:1508-2206 (EXP / LINEAR / AUTO, no HDA).
+           maxloop: int = 0, log=None, hda: bool = False, T=None, L: int = 0,
+           Kmax: int = 32768, eps2: float = 1e-3, on_expand=None) -> RunResult:
+    """Temperature loop of dagtm/dagtm.cxx:1508-2206 (EXP / LINEAR / AUTO, HDA).
 
     AUTO (dagtm/dagtm.cxx:1919-1934): the next temperature is the critical
     temperature from ``Context.next_ctemp`` with the G of the last M-step as
     weights (the reference's vggsub), or temp * alpha when that is not below
     the current temperature.
 
+    HDA (``hda=True``, the -H option; EXP schedule; dagtm/dagtm.cxx:1912-2124):
+    at the end of a temperature with K < Kmax, a grid that is ready to expand
+    either expands, if the log-likelihood rose by at least eps2 over the
+    temperature, or stops being ready.  A grid that is not ready asks for the
+    next critical temperature and becomes ready when it is at least
+    temp * alpha.  Expanding doubles the latent grid per dimension,
+    K = (round(K^(1/L)) 2)^L, rebuilds X and FI with width factor 2 and the
+    same M, and sets Y = FI W (``Context.set_basis``; ``T`` must be the
+    context's data, ``L`` the latent dimension).  ``on_expand(ctx, info)``
+    runs before the expansion, with ``info`` holding the trace index, K, the
+    new K, W, beta and the per-centre critical temperatures of the last
+    ``next_ctemp`` call (the reference writes these, with the MAP, when it
+    logs progress).
+
     Starts from the centres already loaded into ``ctx`` (a fresh set-up or a
     restart, dagtm/dagtm.cxx:1161-1232) and mirrors the reference's order:
     E-step, qualities, |diff| < eps test (before the M-step), the 50-wide
     moving-average test once nloop > 50, M-step, beta, maxloop test.
     """
+    if hda and (schedule != "exp" or T is None or L < 1):
+        raise ValueError("HDA needs the EXP schedule, the data T and the latent dimension L")
     res = RunResult()
     nloop = iter0
     if maxloop:
         maxloop = iter0 + maxloop
     qual = 0.0
+    llh = 0.0
     isLast = False
     W = None
     G_last = None
+    ready = False  # HDA: bReadyToExpand
+    ctemp_k = None
     while True:
         if temp < 1.0:
             temp = 1.0
             isLast = True
+        qual_before_temp = llh
         queue = [np.finfo(np.float64).max] * QUEUE_SIZE
         qnext = 0
         if log:
@@ -321,7 +372,7 @@ def anneal(ctx: Context, beta: float, temp: float, isDA: int = 1, schedule: str 
                 if stalled:
                     break
             beta, W, _ = ctx.mstep(want_W=True)
-            if schedule == "auto":
+            if schedule == "auto" or hda:
                 G_last = ctx.get_stats()[0]
             if maxloop and nloop >= maxloop:
                 isLast = True
@@ -335,6 +386,31 @@ def anneal(ctx: Context, beta: float, temp: float, isDA: int = 1, schedule: str 
                     ctemp = temp * alpha  # no valid next critical temperature
                 temp = ctemp
             else:
+                if hda and ctx.K < Kmax:
+                    qual_diff = llh - qual_before_temp
+                    expand = False
+                    if ready:
+                        if qual_diff < eps2:
+                            ready = False  # nothing happened at this temperature
+                        else:
+                            expand = True
+                    if not ready:
+                        cmax, ctemp_k = ctx.next_ctemp(temp, beta, eps, gg=G_last,
+                                                       per_centre=True)
+                        if cmax >= temp * alpha:
+                            ready = True
+                    if expand:
+                        ready = False
+                        Knew = int(round(ctx.K ** (1.0 / L)) * 2) ** L
+                        if on_expand is not None:
+                            on_expand(ctx, dict(index=len(res.temp_trace) - 1, K=ctx.K,
+                                                K_new=Knew, W=W, beta=beta, ctemp=ctemp_k))
+                        if log:
+                            log(f"new K : {Knew}\n")
+                        _, FI = _gtm_setup().setup_grid(L, Knew, ctx.M1 - 1, 2.0)
+                        res.expansions.append((nloop, ctx.K, Knew))
+                        ctx.set_basis(T, FI, FI @ W)
+                        G_last = None
                 temp *= alpha
         else:
             break

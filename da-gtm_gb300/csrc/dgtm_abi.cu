@@ -646,6 +646,12 @@ int dgtm_map(dgtm_ctx *ctx, const double *X, int L, double *M, int ldM)
 int dgtm_next_ctemp(dgtm_ctx *ctx, double temp, double beta, double eps, const double *gg,
                     double *ctemp)
 {
+    return dgtm_next_ctemp_k(ctx, temp, beta, eps, gg, nullptr, ctemp);
+}
+
+int dgtm_next_ctemp_k(dgtm_ctx *ctx, double temp, double beta, double eps, const double *gg,
+                      double *ctemp_k, double *ctemp)
+{
     DGTM_TRY(check_ctx(ctx));
     if (!ctemp || !(beta > 0.0)) {
         set_error(DGTM_EINVAL, "dgtm_next_ctemp: bad arguments (beta=%g)", beta);
@@ -714,6 +720,8 @@ int dgtm_next_ctemp(dgtm_ctx *ctx, double temp, double beta, double eps, const d
                                                                               : out[(size_t) 2 * k + 1];
             ck = beta / 2 / g * lmax;
         }
+        if (ctemp_k)
+            ctemp_k[k] = ck;
         if (ck > cmax)
             cmax = ck;
     }

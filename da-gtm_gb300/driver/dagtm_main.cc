@@ -3,11 +3,11 @@
 //
 // It follows the control flow of dagtm/dagtm.cxx (main, :714-2633) for one
 // process: options (:719-891), reading T/id/lb (:1070-1101), random set-up or
-// restart (:1104-1213), the temperature loop with the EXP and LINEAR
-// schedules (:1508-2206), checkpoints (:1609-1687), interpolation (:1247-1295)
-// and the output file (:2342-2552).  The MPI grid (-z) has nothing to do on one
-// GPU; AUTO cooling and HDA (-c auto, -H) are not part of this build and are
-// refused.  Extra options: -F form (fp64 | fp32 | bf16x3, default fp64),
+// restart (:1104-1213), the temperature loop with the EXP, LINEAR and AUTO
+// schedules and the hierarchical expansion of EXP (-H, :1508-2206),
+// checkpoints (:1609-1687), interpolation (:1247-1295) and the output file
+// (:2342-2552).  The MPI grid (-z) has nothing to do on one GPU.  Extra
+// options: -F form (fp64 | fp32 | bf16x3, default fp64),
 // -G width (basis-function width factor, default 2 as the reference
 // hard-codes at :1119), -Q solver (cholesky | svd, default svd as the
 // reference's dagtm_solve2).
@@ -214,10 +214,10 @@ void setup_grid(int L, int K, int M, double s, std::vector<double> &X, std::vect
 }
 
 struct Opts {
-    int K = 125, L = 3, M = 8, maxloop = 0, period = 100, verbose = 0;
+    int K = 125, L = 3, M = 8, maxloop = 0, period = 100, verbose = 0, Kmax = 32768;
     double alpha = 0.99, delta = 0.1, eps = 1e-6, eps2 = 1e-3, start_temp = 1.0, width = 2.0;
     bool need_ctemp = true, isDA = true, checkpointing = true, log_progress = false,
-         save_R = false, log_file = false, interpolation = false;
+         save_R = false, log_file = false, interpolation = false, hda = false;
     int schedule = 0;  // 0 EXP, 1 LINEAR, 2 AUTO
     unsigned long seed = 0;
     std::string in = "INPUT.h5", out, restart, prefix = "ckp.";
@@ -235,13 +235,16 @@ void help()
         "-B name      : dataset name for label (default: lb)",
         "-c schedule  : cooling schedule [auto|exp|linear] (default : exp)",
         "-e number    : precision (default: 1e-6)",
+        "-E number    : log-likelihood gain that confirms an HDA expansion (default: 1e-3)",
         "-f dataset   : dataset name for FI (default: FI)",
         "-F form      : arithmetic [fp64|fp32|bf16x3] (default: fp64)",
         "-G number    : basis-function width factor (default: 2)",
         "-h           : show help",
+        "-H           : hierarchical DA (EXP schedule: grow K at critical temperatures)",
         "-i filename  : input HDF5 filename",
         "-I           : interpolation",
         "-j number    : maximum number of iterations",
+        "-k number    : largest K of the hierarchical DA (default: 32768)",
         "-K number    : number of latent data K (eg, 100, 1k, 1M)",
         "-l           : log to file",
         "-L number    : latent dimension",
@@ -307,11 +310,11 @@ Opts parse(int argc, char **argv)
             break;
         case 'G': o.width = atof(optarg); break;
         case 'h': help(); exit(EXIT_SUCCESS);
-        case 'H': die("hierarchical DA (-H) is not part of this build");
+        case 'H': o.hda = !o.hda; break;
         case 'i': o.in = optarg; break;
         case 'I': o.interpolation = true; break;
         case 'j': o.maxloop = atoi(optarg); break;
-        case 'k': break;  // Kmax: HDA only
+        case 'k': o.Kmax = atoi(optarg); break;
         case 'K': {
             float num = 0, unit = 1;
             char ch = 0;
@@ -613,16 +616,98 @@ int main(int argc, char **argv)
     std::vector<double> queue(QUEUE, DBL_MAX), tr_temp, tr_llh, tr_free;
     double llh = 0, nfree = 0, qual = 0, qual_old = 0, diff = DBL_MAX;
     bool isLast = false, stats_current = false;
-    std::vector<double> G_last;  // G of the last M-step (AUTO schedule)
+    std::vector<double> G_last;  // G of the last M-step (AUTO schedule, HDA)
     int lloop = 0;
+    // HDA (dagtm/dagtm.cxx:1504-1506, 1937-2124): the expansion state, the
+    // per-centre critical temperatures of the last next_ctemp call, and the
+    // snapshots written into the output file when progress is logged
+    bool ready = false;
+    int nexpanded = 0;
+    std::vector<double> ctemp_k;
+    struct Snap {
+        std::string name;
+        std::vector<uint64_t> dims;
+        std::vector<double> v;
+    };
+    std::vector<Snap> snaps;
+
     W.assign((size_t) (M + 1) * D, 0.0);
     bool have_W = false;
+    auto hda_step = [&](double qual_before_temp) {
+        const double qual_diff = llh - qual_before_temp;
+        bool expand = false;
+        if (ready) {
+            if (qual_diff < o.eps2) {
+                fprintf(g_log, "HDA: nothing happened at this temperature, not expanding\n");
+                ready = false;
+            } else {
+                expand = true;
+            }
+        }
+        if (!ready) {
+            double ct = 0.0;
+            ctemp_k.assign((size_t) K, 0.0);
+            check(dgtm_next_ctemp_k(ctx, temp, beta, o.eps,
+                                    G_last.empty() ? nullptr : G_last.data(), ctemp_k.data(),
+                                    &ct),
+                  "dgtm_next_ctemp_k");
+            fprintf(g_log, "HDA: ctemp_max : %f\n", ct);
+            if (ct >= temp * o.alpha) {
+                fprintf(g_log, "HDA: ready to expand\n");
+                ready = true;
+            }
+        }
+        if (!expand)
+            return;
+        ready = false;
+        nexpanded++;
+        if (!have_W)
+            check(dgtm_get_W(ctx, W.data(), D), "dgtm_get_W");
+        if (!o.out.empty() && o.log_progress) {
+            // dagtm/dagtm.cxx:1980-2096: MAP and the model at this temperature,
+            // indexed by the temperature collection's last entry
+            const long idx = (long) tr_temp.size() - 1;
+            auto name = [&](const std::string &base) { return base + "." + std::to_string(idx); };
+            std::vector<double> Mout((size_t) N * L);
+            check(dgtm_map(ctx, X.data(), L, Mout.data(), L), "dgtm_map");
+            check(dgtm_get_Y(ctx, Y.data(), D), "dgtm_get_Y");
+            snaps.push_back({name(o.dM), {(uint64_t) N, (uint64_t) L}, Mout});
+            snaps.push_back({name(o.dX), {(uint64_t) K, (uint64_t) L}, X});
+            snaps.push_back({name(o.dY), {(uint64_t) K, (uint64_t) D}, Y});
+            snaps.push_back({name(o.dFI), {(uint64_t) K, (uint64_t) M + 1}, FI});
+            snaps.push_back({name(o.dW), {(uint64_t) M + 1, (uint64_t) D}, W});
+            snaps.push_back({name("ctemp"), {(uint64_t) K}, ctemp_k});
+            snaps.push_back({name(o.dbeta), {1}, {beta}});
+        }
+        // dagtm/dagtm.cxx:2110-2144: the latent grid doubles per dimension, X
+        // and FI are rebuilt with width factor 2 and the same M, Y = FI W
+        const int g = (int) lround(pow((double) K, 1.0 / L)) * 2;
+        K = (int) lround(pow((double) g, (double) L));
+        fprintf(g_log, "HDA: new K : %d\n", K);
+        setup_grid(L, K, M, 2.0, X, FI);
+        Y.assign((size_t) K * D, 0.0);
+        for (int k = 0; k < K; k++)
+            for (int j = 0; j <= M; j++) {
+                const double f = FI[(size_t) k * (M + 1) + j];
+                for (int d = 0; d < D; d++)
+                    Y[(size_t) k * D + d] += f * W[(size_t) j * D + d];
+            }
+        dgtm_ctx_destroy(ctx);
+        ctx = nullptr;
+        check(dgtm_ctx_create(N, D, K, M + 1, T.data(), D, FI.data(), M + 1, o.form, &ctx),
+              "dgtm_ctx_create");
+        check(dgtm_set_solver(ctx, o.solver), "dgtm_set_solver");
+        check(dgtm_set_Y(ctx, Y.data(), D), "dgtm_set_Y");
+        G_last.clear();
+        stats_current = false;
+    };
     do {
         if (temp < 1.0) {
             temp = 1.0;
             isLast = true;
         }
         fprintf(g_log, "\nT= %.10g\n", temp);
+        const double qual_before_temp = llh;
         std::fill(queue.begin(), queue.end(), DBL_MAX);
         int qnext = 0;
         fprintf(g_log, ">>> %15s %15s %15s %15s %15s %15s\n", "GSEQ", "SEQ", "K", "TEMP", "NFREE", "LLH");
@@ -685,8 +770,8 @@ int main(int argc, char **argv)
             }
             check(dgtm_mstep(ctx, W.data(), D, nullptr, D, &beta), "dgtm_mstep");
             have_W = true;
-            if (o.schedule == 2) {
-                // the AUTO schedule weighs centres by the G of the last M-step
+            if (o.schedule == 2 || o.hda) {
+                // AUTO and HDA weigh centres by the G of the last M-step
                 G_last.resize(K);
                 check(dgtm_get_stats(ctx, G_last.data(), nullptr, D), "dgtm_get_stats");
             }
@@ -710,6 +795,8 @@ int main(int argc, char **argv)
                     ct = temp * o.alpha;  // no valid next critical temperature
                 temp = ct;
             } else {
+                if (o.hda && K < o.Kmax)
+                    hda_step(qual_before_temp);
                 temp *= o.alpha;
             }
         } else {
@@ -742,6 +829,8 @@ int main(int argc, char **argv)
         } else if (o.schedule == 0) {
             fprintf(g_log, "%20s = %s\n", "Cooling Schedule", "EXP");
             fprintf(g_log, "%20s = %g\n", "alpha", o.alpha);
+            if (o.hda)
+                fprintf(g_log, "%20s = %d (K = %d)\n", "HDA expansions", nexpanded, K);
         } else {
             fprintf(g_log, "%20s = %s\n", "Cooling Schedule", "LINEAR");
             fprintf(g_log, "%20s = %g\n", "delta", o.delta);
@@ -766,6 +855,8 @@ int main(int argc, char **argv)
         std::vector<double> Mout((size_t) N * L);
         check(dgtm_map(ctx, X.data(), L, Mout.data(), L), "dgtm_map");
         h5lite::Writer w = write_output(Mout, qual, o.save_R);
+        for (const Snap &sn : snaps)
+            w.add_f64(sn.name, sn.dims, sn.v.data());
         if (o.log_progress) {
             w.add_f64("Temp", {(uint64_t) tr_temp.size()}, tr_temp.data());
             w.add_f64("LLH", {(uint64_t) tr_llh.size()}, tr_llh.data());

@@ -150,6 +150,15 @@ int dgtm_next_ctemp(dgtm_ctx *ctx, double temp, double beta, double eps, const d
                     double *ctemp);
 
 /*
+ * dgtm_next_ctemp that also returns every centre's ctemp_k in ctemp_k[0..K)
+ * (host, may be NULL): the reference's vctemp, which the hierarchical (HDA)
+ * schedule writes as ctemp.<i> before it expands the latent grid
+ * (dagtm/dagtm.cxx:1958-2067).
+ */
+int dgtm_next_ctemp_k(dgtm_ctx *ctx, double temp, double beta, double eps, const double *gg,
+                      double *ctemp_k, double *ctemp);
+
+/*
  * Per-phase device timers, the counterpart of the reference's LOG_TICTOC
  * phase counters (comm/log.h:35-75, printed by logfullWithPID at
  * dagtm/dagtm.cxx:2286).  When enabled, CUDA events bracket each phase on the

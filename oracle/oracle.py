@@ -302,3 +302,98 @@ def run(T, FI, Y, beta, temp, isDA=1, schedule=0, alpha=0.99, delta=0.1, eps=1e-
     return {"ret": ret, "n": nout.value, "temp_trace": tt[:n], "nfree_trace": tn[:n],
             "llh_trace": tl[:n], "beta_trace": tb[:n], "Y": Y, "W": W, "beta": b.value,
             "temp": t.value, "R": R}
+
+
+def run_hda(T, FI, Y, beta, temp, L, alpha=0.99, eps=1e-6, eps2=1e-3, Kmax=32768,
+            iter0=0, maxloop=0):
+    """The annealing loop with the hierarchical schedule (-H, EXP cooling),
+    restated over the C primitives above: E-step and qualities
+    (dagtm/dagtm.cxx:1541-1605), the two stopping tests (:1690-1709), M-step
+    with the Cholesky solve and beta (:1715-1779), and at the end of each
+    temperature the expansion logic of :1912-2124 (ready / expand on the
+    log-likelihood gain over the temperature against eps2, the next critical
+    temperature against temp * alpha, K = (round(K^(1/L)) 2)^L, new FI from
+    dagtm_stp with width factor 2, Y = FI W).  The weights of next_ctemp are
+    the G of the last M-step at this K (the row sums of R before the first).
+    Python control flow: small cases only."""
+    T, FI = _c(T), _c(FI)
+    Y = _c(Y).copy()
+    N, D = T.shape
+    K, M1 = FI.shape
+    nloop = iter0
+    if maxloop:
+        maxloop = iter0 + maxloop
+    q = 0.0
+    llh = 0.0
+    isLast = False
+    ready = False
+    W = None
+    G = None
+    tr = {"temp": [], "nfree": [], "llh": [], "beta": [], "K": []}
+    expansions = []
+    Dm = dist(Y, T)
+    big = np.finfo(np.float64).max
+    while True:
+        if temp < 1.0:
+            temp = 1.0
+            isLast = True
+        queue = [big] * 50
+        qnext = 0
+        qual_before = llh
+        while True:
+            R, vgc, vgc2 = resp(Dm, beta, 1, temp)
+            q_old = q
+            nloop += 1
+            llh = qual(N, K, D, beta, vgc, 0, temp)
+            nfree = qual(N, K, D, beta, vgc2, 1, temp)
+            q = nfree
+            diff = q - q_old
+            for key, v in (("temp", temp), ("nfree", nfree), ("llh", llh), ("beta", beta),
+                           ("K", K)):
+                tr[key].append(v)
+            if abs(diff) < eps:
+                break
+            if nloop > 50:
+                with np.errstate(over="ignore", invalid="ignore"):
+                    avg_old = sum(queue) / 50
+                    queue[qnext] = q
+                    qnext = (qnext + 1) % 50
+                    avg = sum(queue) / 50
+                    stalled = abs(avg - avg_old) < eps
+                if stalled:
+                    break
+            G, A, B = mstep_stats(R, FI, T)
+            W = solve_chol(A, B)
+            Y = fiw(FI, W)
+            beta, _, Dm = beta_update(Y, T, R)
+            if maxloop and nloop >= maxloop:
+                isLast = True
+                break
+        if isLast:
+            break
+        if K < Kmax:
+            qual_diff = llh - qual_before
+            expand = False
+            if ready:
+                if qual_diff < eps2:
+                    ready = False
+                else:
+                    expand = True
+            if not ready:
+                gg = G if G is not None else R.sum(axis=1)
+                if next_ctemp(T, Y, R, gg, temp, beta, eps) >= temp * alpha:
+                    ready = True
+            if expand:
+                ready = False
+                Knew = int(round(K ** (1.0 / L)) * 2) ** L
+                _, FI = stp(L, Knew, M1 - 1, 2.0)
+                expansions.append((nloop, K, Knew))
+                K = Knew
+                Y = fiw(FI, W)
+                Dm = dist(Y, T)
+                G = None
+        temp *= alpha
+    return {"n": len(tr["temp"]), "temp_trace": np.array(tr["temp"]),
+            "nfree_trace": np.array(tr["nfree"]), "llh_trace": np.array(tr["llh"]),
+            "beta_trace": np.array(tr["beta"]), "K_trace": np.array(tr["K"]),
+            "expansions": expansions, "Y": Y, "W": W, "FI": FI, "beta": beta, "temp": temp}

@@ -24,11 +24,12 @@ def test_help_lists_reference_options(built_lib):
     out = subprocess.run([DRIVER, "-h"], capture_output=True, text=True)
     assert out.returncode == 0
     for flag in ("-K number", "-L number", "-M number", "-S number", "-c schedule", "-a number",
-                 "-e number", "-j number", "-s number", "-r filename", "-o filename"):
+                 "-e number", "-j number", "-s number", "-r filename", "-o filename", "-H ",
+                 "-k number", "-E number"):
         assert flag in out.stderr
 
 
 def test_unsupported_options_are_refused(built_lib):
-    for args in (["-H"], ["-g", "spacefilling"], ["-c", "fast"]):
+    for args in (["-g", "spacefilling"], ["-c", "fast"]):
         out = subprocess.run([DRIVER] + args, capture_output=True, text=True)
         assert out.returncode != 0

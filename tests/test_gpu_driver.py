@@ -123,3 +123,41 @@ def test_auto_schedule_matches_package_loop(tmp_path, pkg, golden):
     assert n >= 10
     assert np.allclose(tr[:n, 3], ref.temp_trace[:n], rtol=1e-6)
     assert np.allclose(tr[:n, 4], ref.nfree_trace[:n], rtol=1e-5, atol=1e-6)
+
+
+def test_hda_expands_and_writes_snapshots(tmp_path, pkg, golden):
+    # -H on the EXP schedule from K = 8 (L = 3), started below the first
+    # critical temperature: the grid doubles per dimension twice within 200
+    # iterations (8 -> 64 -> 512), as the package loop does from the same set-up
+    st = __import__("importlib").import_module(pkg.__name__ + ".gtm_setup")
+    T = golden["T_in"].astype(np.float64)
+    t0 = 0.6 * st.first_critical_temp(T)
+    out = run(["-i", OIL_IN, "-o", "hda.h5", "-K", "8", "-L", "3", "-M", "8", "-s", "3", "-H",
+               "-S", f"{float(t0):.17g}", "-j", "200", "-n", "-p", "-a", "0.9", "-e", "1e-6", "-F", "fp64",
+               "-Q", "cholesky"], tmp_path)
+    tr = trace(out)
+    Ks = tr[:, 2].astype(int)
+    assert Ks[0] == 8 and Ks[-1] == 512
+    grow = [int(tr[i, 0]) for i in range(1, len(tr)) if Ks[i] != Ks[i - 1]]
+    _, FI0, W0, beta0 = st.random_init(T, 3, 8, 8, 2.0, seed=3)
+    with pkg.Context(T, FI0, "fp64") as c:
+        c.set_Y(FI0 @ W0)
+        ref = pkg.anneal(c, beta0, t0, alpha=0.9, eps=1e-6, maxloop=200, hda=True, T=T, L=3)
+    assert [e[1:] for e in ref.expansions] == [(8, 64), (64, 512)]
+    # the first iteration at the new K follows the expansion's last one
+    assert grow == [e[0] + 1 for e in ref.expansions]
+    n = min(len(tr), len(ref.nfree_trace))
+    # the host products Y = FI W of the two loops round differently, and A is
+    # ill-conditioned on the oil basis: the tolerance of the other driver tests
+    assert np.allclose(tr[:n, 4], ref.nfree_trace[:n], rtol=1e-5, atol=1e-6)
+    f = H5File(str(tmp_path / "hda.h5"))
+    for (it, K, _), (Kx, Mx) in zip(ref.expansions, ((8, 8), (64, 8))):
+        idx = it - 1  # the temperature collection holds one entry per iteration
+        assert f.read(f"X.{idx}").shape == (K, 3)
+        assert f.read(f"FI.{idx}").shape == (K, Mx + 1)
+        assert f.read(f"Y.{idx}").shape == (K, 12)
+        assert f.read(f"W.{idx}").shape == (Mx + 1, 12)
+        assert f.read(f"M.{idx}").shape == (1000, 3)
+        assert f.read(f"ctemp.{idx}").shape == (K,)
+        assert f.read(f"beta.{idx}").shape == (1,)
+    assert f.read("X").shape == (512, 3) and f.read("Y").shape == (512, 12)

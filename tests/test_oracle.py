@@ -156,3 +156,25 @@ def test_run_loop_reference_order(orc, golden):
     assert tr[0] == 1.5 and np.all(np.diff(tr) <= 0)
     last = tr == 1.0
     assert np.allclose(out["nfree_trace"][last], out["llh_trace"][last], rtol=1e-13)
+
+
+def test_oracle_hda_loop_expands(orc):
+    """The oracle's HDA loop on a small mixture: the grid grows 4 -> 16 -> 64
+    -> 256 (L = 2), K in the trace follows the expansions, and the K formula
+    doubles the grid per dimension."""
+    import importlib
+    ds = importlib.import_module("da-gtm_gb300.datasets")
+    st = importlib.import_module("da-gtm_gb300.gtm_setup")
+    T = ds.gaussian_mixture(400, 5, 8, 0.2, seed=3)
+    _, FI, W, beta = st.random_init(T, 2, 4, 4, 2.0, seed=1)
+    out = orc.run_hda(T, FI, FI @ W, beta, st.first_critical_temp(T) * 0.8, 2, alpha=0.9,
+                      eps=1e-6, eps2=1e-3, Kmax=256, maxloop=1500)
+    assert [e[1:] for e in out["expansions"]] == [(4, 16), (16, 64), (64, 256)]
+    Ks = out["K_trace"]
+    for it, K, Knew in out["expansions"]:
+        assert Ks[it - 1] == K and Ks[it] == Knew
+    assert out["FI"].shape == (256, 5) and out["Y"].shape == (256, 5)
+    # Kmax stops the growth
+    out2 = orc.run_hda(T, FI, FI @ W, beta, st.first_critical_temp(T) * 0.8, 2, alpha=0.9,
+                       eps=1e-6, eps2=1e-3, Kmax=16, maxloop=1500)
+    assert [e[1:] for e in out2["expansions"]] == [(4, 16)]
