@@ -68,7 +68,7 @@ struct dgtm_ctx {
     double *Gpart, *RTpart;
     double *G, *RT, *A, *B, *work, *bterm, *abpart;
     double *scal;      // device scalars
-    int *flag;         // device status
+    int *flag;         // device status: [0..1] the solver's, [2] update_y's pair counter
     double *hscal;     // pinned host scalars
     int *hflag;
     // split-BF16 form
@@ -460,7 +460,9 @@ int dgtm_mstep(dgtm_ctx *ctx, double *W, int ldW, double *Y, int ldY, double *be
     }
     const int N = ctx->N, K = ctx->K, D = ctx->D, M1 = ctx->M1;
     const double c = ctx->isDA ? ctx->beta / (2.0 * ctx->temp) : ctx->beta / 2.0;
-    int npass = 1, nsmall = 5;
+    // kernels of the solve phase: form_ab (2), the solver (Cholesky and the
+    // substitution, or one eigen kernel), update_y, the beta sum, the reduction
+    int npass = 1, nsmall = 4 + ((ctx->solver == DGTM_SOLVE_SVD) ? 1 : 2);
     DGTM_TRY(phase_begin(ctx, DGTM_PHASE_MSTEP_PASS));
     if (ctx->precision == DGTM_FP64) {
         Pass2Args<double> a{ctx->T64, ctx->Y64, ctx->tt, ctx->yy, ctx->colstat, N, D, K, c,
@@ -488,13 +490,17 @@ int dgtm_mstep(dgtm_ctx *ctx, double *W, int ldW, double *Y, int ldY, double *be
                             ctx->stream));
     DGTM_TRY(launch_solve(ctx->A, ctx->B, M1, D, ctx->solver, ctx->W, ctx->work, ctx->flag,
                           ctx->stream));
+    // the E-step's copies of the new centres come out of the same kernel
+    YCopies cp;
+    if (ctx->precision == DGTM_FP32)
+        cp.Y32 = ctx->Y32;
+    else if (ctx->precision == DGTM_BF16X3)
+        tc_y_copies(ctx->tc, &cp);
     DGTM_TRY(launch_update_y(ctx->FI, ctx->W, ctx->G, ctx->RT, K, M1, D, ctx->Y64, ctx->yy,
-                             ctx->bterm, ctx->stream));
+                             ctx->bterm, cp, ctx->flag + 2, ctx->stream));
     DGTM_TRY(launch_sum_ratio(ctx->bterm, K, ctx->sum_tt, (double) ((long long) N * D),
                               ctx->scal, ctx->stream));
-    int ny = 0;
-    DGTM_TRY(refresh_y_copies(ctx, &ny));
-    DGTM_TRY(phase_end(ctx, DGTM_PHASE_MSTEP_SOLVE, nsmall + ny - 1));
+    DGTM_TRY(phase_end(ctx, DGTM_PHASE_MSTEP_SOLVE, nsmall));
     DGTM_CUDA_TRY(cudaMemcpyAsync(ctx->hscal, ctx->scal, 2 * sizeof(double),
                                   cudaMemcpyDeviceToHost, ctx->stream));
     DGTM_CUDA_TRY(cudaMemcpyAsync(ctx->hflag, ctx->flag, 2 * sizeof(int), cudaMemcpyDeviceToHost,

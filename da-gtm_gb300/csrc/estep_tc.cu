@@ -35,6 +35,7 @@
 // FP32 R T is written to its own slot; a fixed-order sum over the slots
 // (TwoSum, exact to FP64) gives RT and G.
 #include "common.cuh"
+#include "kernels.cuh"
 #include "sm100.cuh"
 #include "tc.cuh"
 
@@ -1293,6 +1294,14 @@ void tc_destroy(TcState *st)
     if (st->hstatus)
         cudaFreeHost(st->hstatus);
     delete st;
+}
+
+void tc_y_copies(TcState *st, YCopies *cp)
+{
+    cp->Y32 = st->Y32;
+    cp->Yb = reinterpret_cast<uint16_t *>(st->Yb);
+    cp->Dp = st->Dp;
+    cp->Kpad = st->Kpad;
 }
 
 int tc_prepare_y(TcState *st, const double *Y64, cudaStream_t s)

@@ -61,10 +61,20 @@ int launch_form_ab(const double *FI, const double *G, const double *RT, int K, i
 // work: M1*M1 + M1 doubles (+ M1*M1 for solver 1).  flag[0] != 0 on failure.
 int launch_solve(const double *A, const double *B, int M1, int D, int solver, double *W,
                  double *work, int *flag, cudaStream_t s);
-// Y = FI W, yy = |y|^2, bterm_k = G_k yy_k - 2 y_k.RT_k (G/RT may be null: no bterm).
+// Copies of the centres that the E-step of a form reads, written by
+// launch_update_y with Y (each may be null): the FP32 copy (K x D) and the
+// split-BF16 pieces (two planes of Kpad x Dp: hi with -|y_hi + y_lo|^2 / 2 in
+// three BF16 pieces at columns D .. D+2, then lo).
+struct YCopies {
+    float *Y32 = nullptr;
+    uint16_t *Yb = nullptr;  // BF16 bit patterns
+    int Dp = 0, Kpad = 0;
+};
+// Y = FI W, yy = |y|^2, bterm_k = G_k yy_k - 2 y_k.RT_k (G/RT may be null: no
+// bterm), and the copies in cp.  ticket: one device int of scratch.
 int launch_update_y(const double *FI, const double *W, const double *G, const double *RT,
                     int K, int M1, int D, double *Y, double *yy, double *bterm,
-                    cudaStream_t s);
+                    const YCopies &cp, int *ticket, cudaStream_t s);
 // AUTO cooling (ctemp.cu): scratch doubles per batch of kb centres and
 // whether the eigen kernel keeps its D x D block in shared memory.
 size_t ctemp_scratch_doubles(int D, int kb, bool *eig_in_smem);

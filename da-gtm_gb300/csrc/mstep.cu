@@ -18,6 +18,8 @@
 #include "common.cuh"
 #include "kernels.cuh"
 
+#include <cuda_bf16.h>
+
 #include <math.h>
 
 namespace dgtm {
@@ -539,66 +541,183 @@ int launch_solve(const double *A, const double *B, int M1, int D, int solver, do
 }
 
 // ---------------------------------------------------------------------------
-// Y = FI W and the per-centre terms of beta
+// Y = FI W, the per-centre terms of beta and the E-step's copies of Y
 // ---------------------------------------------------------------------------
-constexpr int WSMEM_MAX = 96 * 1024;
+// A warp computes two centres over all depths: lane l owns depths l + 32 c,
+// c < NC (passes of 32 NC depths when D > 256), with 2 NC FP64 accumulators.
+// Per basis function it loads the two FI values once (broadcast) and
+// W[m][l + 32 c] from shared memory, where W is padded with zeros to whole
+// passes so the loop has no guards.  The FP64 pipe (about 2 FMA per clock
+// per SM) bounds the kernel; each warp takes the next centre pair from a
+// counter (*ticket, zero at launch), so the pairs spread evenly over the SM
+// sub-partitions whatever the CTA placement.  The warp sums
+// |y|^2, y.RT and, for the split form, |y_hi + y_lo|^2 of each centre by
+// lane partials and shuffles in a fixed order.
+constexpr int UY_THREADS = 256;
+constexpr int UY_NCMAX = 8;
+constexpr size_t UY_WSMEM_MAX = 110 * 1024;  // two CTAs per SM
 
-__global__ void __launch_bounds__(256) update_y_kernel(const double *__restrict__ FI,
-                                                      const double *__restrict__ Wg,
-                                                      const double *__restrict__ G,
-                                                      const double *__restrict__ RT, int K,
-                                                      int M1, int D, int w_in_smem,
-                                                      double *__restrict__ Y,
-                                                      double *__restrict__ yy,
-                                                      double *__restrict__ bterm)
+__device__ __forceinline__ double uy_warp_sum(double v)
 {
-    extern __shared__ double Ws[];
-    const double *W = Wg;
-    if (w_in_smem) {
-        for (int i = threadIdx.x; i < M1 * D; i += blockDim.x)
-            Ws[i] = Wg[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+template <int NC, bool WS>
+__global__ void __launch_bounds__(UY_THREADS) update_y_kernel(
+    const double *__restrict__ FI, const double *__restrict__ Wg, const double *__restrict__ G,
+    const double *__restrict__ RT, int K, int M1, int D, int Dw, double *__restrict__ Y,
+    double *__restrict__ yy, double *__restrict__ bterm, YCopies cp, int *ticket)
+{
+    extern __shared__ double Ws[];  // M1 x Dw, zero past D
+    if (WS) {
+        const int n = M1 * Dw;
+#pragma unroll 4
+        for (int i = threadIdx.x; i < n; i += UY_THREADS) {
+            const int m = i / Dw, d = i - m * Dw;
+            Ws[i] = (d < D) ? Wg[(size_t) m * D + d] : 0.0;
+        }
         __syncthreads();
-        W = Ws;
     }
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int k = blockIdx.x * 8 + warp; k < K; k += gridDim.x * 8) {
-        double syy = 0.0, syrt = 0.0;
-        const double *fi = FI + (size_t) k * M1;
-        for (int d = lane; d < D; d += 32) {
-            double y = 0.0;
-            for (int m = 0; m < M1; m++)
-                y += fi[m] * W[(size_t) m * D + d];
-            Y[(size_t) k * D + d] = y;
-            syy += y * y;
-            if (RT)
-                syrt += y * RT[(size_t) k * D + d];
+    __nv_bfloat16 *const hi = reinterpret_cast<__nv_bfloat16 *>(cp.Yb);
+    __nv_bfloat16 *const lo = hi ? hi + (size_t) cp.Kpad * cp.Dp : nullptr;
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        int pair = 0;
+        if (lane == 0)
+            pair = atomicAdd(ticket, 1);
+        const int k0 = 2 * __shfl_sync(0xffffffffu, pair, 0);
+        if (k0 >= K)
+            break;
+        const int nr = (k0 + 1 < K) ? 2 : 1;
+        const double *f0 = FI + (size_t) k0 * M1;
+        const double *f1 = FI + (size_t) (k0 + nr - 1) * M1;
+        double syy[2] = {0.0, 0.0}, srt[2] = {0.0, 0.0}, sq[2] = {0.0, 0.0};
+        for (int db = 0; db < D; db += 32 * NC) {
+            double a0[NC], a1[NC];
+#pragma unroll
+            for (int c = 0; c < NC; c++)
+                a0[c] = a1[c] = 0.0;
+            for (int m = 0; m < M1; m++) {
+                const double x0 = __ldg(f0 + m), x1 = __ldg(f1 + m);
+#pragma unroll
+                for (int c = 0; c < NC; c++) {
+                    const int d = db + lane + 32 * c;
+                    const double w =
+                        WS ? Ws[m * Dw + d] : ((d < D) ? __ldg(Wg + (size_t) m * D + d) : 0.0);
+                    a0[c] = fma(x0, w, a0[c]);
+                    a1[c] = fma(x1, w, a1[c]);
+                }
+            }
+#pragma unroll
+            for (int c = 0; c < NC; c++) {
+                const int d = db + lane + 32 * c;
+                if (d >= D)
+                    continue;
+#pragma unroll
+                for (int r = 0; r < 2; r++) {
+                    if (r >= nr)
+                        break;
+                    const int k = k0 + r;
+                    const double y = r ? a1[c] : a0[c];
+                    const size_t e = (size_t) k * D + d;
+                    Y[e] = y;
+                    syy[r] = fma(y, y, syy[r]);
+                    if (RT)
+                        srt[r] = fma(y, RT[e], srt[r]);
+                    if (cp.Y32)
+                        cp.Y32[e] = (float) y;
+                    if (hi) {
+                        // BF16 hi + lo of y, as the split form's set-up does
+                        const __nv_bfloat16 h = __float2bfloat16_rn((float) y);
+                        const double hd = (double) __bfloat162float(h);
+                        const __nv_bfloat16 l = __float2bfloat16_rn((float) (y - hd));
+                        const double yh = hd + (double) __bfloat162float(l);
+                        hi[(size_t) k * cp.Dp + d] = h;
+                        lo[(size_t) k * cp.Dp + d] = l;
+                        sq[r] = fma(yh, yh, sq[r]);
+                    }
+                }
+            }
         }
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            syy += __shfl_xor_sync(0xffffffffu, syy, o);
-            syrt += __shfl_xor_sync(0xffffffffu, syrt, o);
-        }
-        if (lane == 0) {
-            yy[k] = syy;
-            if (bterm)
-                bterm[k] = G[k] * syy - 2.0 * syrt;
+        for (int r = 0; r < 2; r++) {
+            if (r >= nr)
+                break;
+            const int k = k0 + r;
+            const double s_yy = uy_warp_sum(syy[r]);
+            const double s_rt = RT ? uy_warp_sum(srt[r]) : 0.0;
+            const double s_q = hi ? uy_warp_sum(sq[r]) : 0.0;
+            if (lane == 0) {
+                yy[k] = s_yy;
+                if (bterm)
+                    bterm[k] = G[k] * s_yy - 2.0 * s_rt;
+            }
+            if (hi && lane < 3) {
+                // -q/2 in three BF16 pieces (24+ significant bits), columns D .. D+2
+                const double v = -0.5 * s_q;
+                const __nv_bfloat16 p1 = __float2bfloat16_rn((float) v);
+                const double r1 = v - (double) __bfloat162float(p1);
+                const __nv_bfloat16 p2 = __float2bfloat16_rn((float) r1);
+                const double r2 = r1 - (double) __bfloat162float(p2);
+                const __nv_bfloat16 p3 = __float2bfloat16_rn((float) r2);
+                hi[(size_t) k * cp.Dp + D + lane] = (lane == 0) ? p1 : (lane == 1) ? p2 : p3;
+            }
         }
     }
 }
 
-int launch_update_y(const double *FI, const double *W, const double *G, const double *RT, int K,
-                    int M1, int D, double *Y, double *yy, double *bterm, cudaStream_t s)
+template <bool WS>
+using UpdateYKernel = void (*)(const double *, const double *, const double *, const double *, int,
+                               int, int, int, double *, double *, double *, YCopies, int *);
+
+template <bool WS>
+UpdateYKernel<WS> update_y_for(int nc)
 {
-    const size_t wbytes = sizeof(double) * (size_t) M1 * D;
-    const int in_smem = wbytes <= WSMEM_MAX;
-    const size_t smem = in_smem ? wbytes : 0;
-    DGTM_CUDA_TRY(cudaFuncSetAttribute(update_y_kernel,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int) (smem > 0 ? smem : 1)));
-    int blocks = ceil_div(K, 8);
-    if (blocks > 1216)
-        blocks = 1216;
-    update_y_kernel<<<blocks, 256, smem, s>>>(FI, W, G, RT, K, M1, D, in_smem, Y, yy, bterm);
+    switch (nc) {
+    case 1: return update_y_kernel<1, WS>;
+    case 2: return update_y_kernel<2, WS>;
+    case 3: return update_y_kernel<3, WS>;
+    case 4: return update_y_kernel<4, WS>;
+    case 5: return update_y_kernel<5, WS>;
+    case 6: return update_y_kernel<6, WS>;
+    case 7: return update_y_kernel<7, WS>;
+    default: return update_y_kernel<8, WS>;
+    }
+}
+
+int launch_update_y(const double *FI, const double *W, const double *G, const double *RT, int K,
+                    int M1, int D, double *Y, double *yy, double *bterm, const YCopies &cp,
+                    int *ticket, cudaStream_t s)
+{
+    DGTM_CUDA_TRY(cudaMemsetAsync(ticket, 0, sizeof(int), s));
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        DGTM_CUDA_TRY(cudaGetDevice(&dev));
+        DGTM_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    }
+    int nc = ceil_div(D, 32);
+    if (nc > UY_NCMAX)
+        nc = UY_NCMAX;
+    const int Dw = ceil_div(D, 32 * nc) * 32 * nc;
+    const size_t wbytes = sizeof(double) * (size_t) M1 * Dw;
+    const bool ws = wbytes <= UY_WSMEM_MAX;
+    int blocks = ceil_div(K, 2 * (UY_THREADS / 32));
+    const int cap = sms * (ws ? 2 : 4);
+    if (blocks > cap)
+        blocks = cap;
+    if (ws) {
+        const UpdateYKernel<true> k = update_y_for<true>(nc);
+        DGTM_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int) wbytes));
+        k<<<blocks, UY_THREADS, wbytes, s>>>(FI, W, G, RT, K, M1, D, Dw, Y, yy, bterm, cp, ticket);
+    } else {
+        update_y_for<false>(nc)<<<blocks, UY_THREADS, 0, s>>>(FI, W, G, RT, K, M1, D, Dw, Y, yy,
+                                                             bterm, cp, ticket);
+    }
     DGTM_CUDA_TRY(cudaGetLastError());
     return DGTM_OK;
 }

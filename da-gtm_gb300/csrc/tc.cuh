@@ -14,6 +14,9 @@ int tc_create(TcState **out, int N, int D, int K, int sms, const double *T64, co
 void tc_destroy(TcState *st);
 // Split the FP64 centres into BF16 pieces (with the folded -|y|^2/2 column).
 int tc_prepare_y(TcState *st, const double *Y64, cudaStream_t s);
+// Where the M-step writes the BF16 pieces and the FP32 copy of new centres.
+struct YCopies;
+void tc_y_copies(TcState *st, YCopies *cp);
 // E-step: column statistics (exact-minimum shift, log s_n) and per-block
 // partial sums of the llh / nfree terms.
 int tc_estep(TcState *st, const double *Y64, double c1, double c2, int isDA, double2 *colstat,
