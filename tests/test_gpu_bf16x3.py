@@ -130,3 +130,36 @@ def test_reruns_are_bit_identical_bf16x3(pkg):
             outs.append((q, b, Yn))
     assert outs[0][0] == outs[1][0] and outs[0][1] == outs[1][1]
     assert np.array_equal(outs[0][2], outs[1][2])
+
+
+@pytest.mark.parametrize("N,D,K,M1", [(1, 1, 1, 1), (5, 2, 3, 2), (129, 3, 129, 4),
+                                      (255, 31, 7, 3), (513, 64, 257, 9), (300, 189, 130, 5)])
+def test_tiny_and_ragged_shapes_bf16x3(pkg, orc, N, D, K, M1):
+    """Shapes below one tile and one past a tile boundary (pass-1 tiles of 128
+    points, pass-2 tiles of 64 points, 128-centre tiles, D at both ends of the
+    supported range), real-valued data (two T pieces), against the oracle at
+    the split form's tolerances."""
+    rng = np.random.default_rng(N + D + K)
+    T = rng.random((N, D))
+    Y = rng.random((K, D))
+    FI = np.concatenate([rng.random((K, M1 - 1)), np.ones((K, 1))], axis=1)
+    beta, temp = 3.0, 1.3
+    Dm = orc.dist(Y, T)
+    R, vgc, vgc2 = orc.resp(Dm, beta, 1, temp)
+    ollh = orc.qual(N, K, D, beta, vgc, 0, temp)
+    onfree = orc.qual(N, K, D, beta, vgc2, 1, temp)
+    with pkg.Context(T, FI, "bf16x3") as c:
+        c.set_Y(Y)
+        llh, nfree = c.estep(beta, 1, temp)
+        Rg = c.R_block(0, K, 0, N)
+        assert llh == pytest.approx(ollh, rel=1e-4, abs=1e-6)
+        assert nfree == pytest.approx(onfree, rel=1e-4, abs=1e-6)
+        assert np.max(np.abs(Rg - R)) <= 1e-4
+        try:
+            c.mstep()
+        except pkg.DgtmError as e:  # a degenerate exact fit gives beta = inf
+            assert e.code == 4
+            return
+        G, RT = c.get_stats()
+    assert rel(G, R.sum(1)) <= 1e-4
+    assert rel(RT, R @ T) <= 1e-4
