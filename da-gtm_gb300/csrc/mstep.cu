@@ -693,12 +693,9 @@ int launch_update_y(const double *FI, const double *W, const double *G, const do
                     int *ticket, cudaStream_t s)
 {
     DGTM_CUDA_TRY(cudaMemsetAsync(ticket, 0, sizeof(int), s));
-    static int sms = 0;
-    if (!sms) {
-        int dev = 0;
-        DGTM_CUDA_TRY(cudaGetDevice(&dev));
-        DGTM_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    }
+    int dev = 0, sms = 0;
+    DGTM_CUDA_TRY(cudaGetDevice(&dev));
+    DGTM_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     int nc = ceil_div(D, 32);
     if (nc > UY_NCMAX)
         nc = UY_NCMAX;
