@@ -37,7 +37,7 @@ ABI_SYMBOLS = ("dgtm_version", "dgtm_last_error_string", "dgtm_ctx_create", "dgt
                "dgtm_next_ctemp_k", "dgtm_set_timing",
                "dgtm_reset_timing", "dgtm_get_timing", "dgtm_get_stream", "dgtm_selftest",
                "dgtm_fe_workspace_size", "dgtm_fe_forward", "dgtm_fe_backward",
-               "dgtm_fe_forward_noalloc")
+               "dgtm_fe_forward_noalloc", "dgtm_wait_probe")
 PHASES = ("estep", "estep_reduce", "mstep_pass", "mstep_solve")
 
 
@@ -89,6 +89,7 @@ def load_library(path: str = LIB_PATH):
         "dgtm_fe_backward": (i, [vp, vp, i, i, i, d, d, vp, ctypes.c_size_t, vp, vp, vp, vp,
                                  vp]),
         "dgtm_fe_forward_noalloc": (i, [vp, vp, i, i, i, d, d, vp, vp]),
+        "dgtm_wait_probe": (i, [ctypes.c_uint, ctypes.POINTER(i), _dp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -117,6 +118,15 @@ def selftest():
     errs = (ctypes.c_double * 3)()
     _check(load_library().dgtm_selftest(errs, 3))
     return list(errs)
+
+
+def wait_probe(limit_ms: int = 50):
+    """One bounded wait that runs out (see dgtm_wait_probe): returns the status
+    code, the site the kernel recorded and the milliseconds it waited."""
+    site = ctypes.c_int()
+    ms = ctypes.c_double()
+    code = load_library().dgtm_wait_probe(int(limit_ms), ctypes.byref(site), ctypes.byref(ms))
+    return code, site.value, ms.value
 
 
 class Context:

@@ -171,6 +171,26 @@ int make_tmap_bf16(CUtensorMap *map, const void *ptr, uint64_t rows, uint64_t co
     return DGTM_OK;
 }
 
+// The failure path of every bounded wait: one thread waits, with the given
+// limit, on an mbarrier that nothing arrives at, exactly as the tensor-core
+// kernels wait (mbar_wait: hardware-suspended try_wait, wall-clock limit),
+// records the probe's site code in the status word when it gives up, and the
+// kernel returns normally.
+constexpr int WAIT_PROBE_SITE = 90;
+
+__global__ void wait_probe_kernel(int *status, unsigned long long limit_ns,
+                                  unsigned long long *waited_ns)
+{
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_barrier_init();
+        const uint64_t t0 = globaltimer_ns();
+        mbar_wait(&bar, 0, status, WAIT_PROBE_SITE, limit_ns);
+        *waited_ns = globaltimer_ns() - t0;
+    }
+}
+
 static uint16_t f2bf(float f)
 {
     uint32_t u;
@@ -289,4 +309,44 @@ done:
     cudaFree(dSt);
     return rc;
 #undef ST_CK
+}
+
+extern "C" int dgtm_wait_probe(unsigned limit_ms, int *site, double *waited_ms)
+{
+    if (!site || !waited_ms || limit_ms == 0 || limit_ms > 10000) {
+        set_error(DGTM_EINVAL, "dgtm_wait_probe: bad arguments (limit %u ms)", limit_ms);
+        return DGTM_EINVAL;
+    }
+    int *dSt = nullptr;
+    unsigned long long *dW = nullptr;
+    int st = 0;
+    unsigned long long w = 0;
+    cudaError_t e = cudaMalloc((void **) &dSt, sizeof(int));
+    if (e == cudaSuccess)
+        e = cudaMalloc((void **) &dW, sizeof(unsigned long long));
+    if (e == cudaSuccess)
+        e = cudaMemset(dSt, 0, sizeof(int));
+    if (e == cudaSuccess) {
+        wait_probe_kernel<<<1, 32>>>(dSt, (unsigned long long) limit_ms * 1000000ull, dW);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess)
+        e = cudaDeviceSynchronize();
+    if (e == cudaSuccess)
+        e = cudaMemcpy(&st, dSt, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(&w, dW, sizeof(w), cudaMemcpyDeviceToHost);
+    cudaFree(dSt);
+    cudaFree(dW);
+    if (e != cudaSuccess) {
+        set_error(DGTM_ECUDA, "dgtm_wait_probe: %s", cudaGetErrorString(e));
+        return DGTM_ECUDA;
+    }
+    *site = st;
+    *waited_ms = (double) w * 1e-6;
+    if (st != 0) {
+        set_error(DGTM_ETIMEOUT, "a wait gave up (site %d) after %.1f ms", st, *waited_ms);
+        return DGTM_ETIMEOUT;
+    }
+    return DGTM_OK;
 }

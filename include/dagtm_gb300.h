@@ -235,6 +235,16 @@ int dgtm_fe_forward_noalloc(const float *Y, const float *T, int N, int K, int D,
  */
 int dgtm_selftest(double *errs, int nerrs);
 
+/*
+ * Diagnostic of the failure path: every wait in the tensor-core kernels is
+ * bounded and, when it gives up, records a site code that the host turns into
+ * DGTM_ETIMEOUT while the device stays usable.  This runs one such wait, with
+ * limit_ms (1 .. 10000), on a barrier that nothing arrives at.  Returns
+ * DGTM_ETIMEOUT with *site = 90 and the time the wait took in *waited_ms.
+ * No reference counterpart (the reference has no GPU code).
+ */
+int dgtm_wait_probe(unsigned limit_ms, int *site, double *waited_ms);
+
 #ifdef __cplusplus
 }
 #endif
