@@ -189,7 +189,7 @@ int launch_form_ab(const double *FI, const double *G, const double *RT, int K, i
 // ---------------------------------------------------------------------------
 constexpr int SOLVE_THREADS = 512;
 constexpr int SMEM_SOLVE_MAX = 110;  // M1 up to which L lives in shared memory
-constexpr int TRI_MAXR = 8;  // registers per lane in the substitution: M1 <= 256
+constexpr int TRI_MAXR = 32;  // registers per lane in the substitution: M1 <= 1024
 
 // 1/sqrt(d) for a positive normal d: an FP32 estimate refined by two
 // Newton-Raphson steps for f(r) = 1/r^2 - d, r <- r (3 - d r^2) / 2 (each
@@ -247,9 +247,11 @@ __global__ void __launch_bounds__(CHOL_THREADS) cholesky_kernel(const double *__
                                                                int M1, double *__restrict__ work,
                                                                int *flag)
 {
+    // shared: the pivots' reciprocal square roots and A's diagonal (M1 each),
+    // then L itself when it fits (M1 <= SMEM_SOLVE_MAX), else L is in work
     extern __shared__ double sh[];
-    double *L = (M1 <= SMEM_SOLVE_MAX) ? sh : work;
-    __shared__ double rinv[32 * TRI_MAXR], adiag[32 * TRI_MAXR];  // pivots: 1/sqrt, A's diagonal
+    double *rinv = sh, *adiag = sh + M1;
+    double *L = (M1 <= SMEM_SOLVE_MAX) ? sh + 2 * M1 : work;
     __shared__ int bad, ndrop;
     const int tid = threadIdx.x, q = tid & 3, r0 = tid >> 2;
     const size_t n2 = (size_t) M1 * M1;
@@ -381,6 +383,8 @@ __global__ void __launch_bounds__(TRI_WARPS * 32) tri_solve_kernel(const double 
 
 using TriKernel = void (*)(const double *, const double *, int, int, int, const int *, double *);
 
+// exact register counts up to 8, then buckets (the registers past M1 hold 0
+// and take no steps)
 TriKernel tri_solve_for(int nr)
 {
     switch (nr) {
@@ -391,7 +395,11 @@ TriKernel tri_solve_for(int nr)
     case 5: return tri_solve_kernel<5>;
     case 6: return tri_solve_kernel<6>;
     case 7: return tri_solve_kernel<7>;
-    default: return tri_solve_kernel<8>;
+    case 8: return tri_solve_kernel<8>;
+    default:
+        return nr <= 12 ? tri_solve_kernel<12>
+                        : nr <= 16 ? tri_solve_kernel<16>
+                                   : nr <= 24 ? tri_solve_kernel<24> : tri_solve_kernel<32>;
     }
 }
 
@@ -522,10 +530,10 @@ int launch_solve(const double *A, const double *B, int M1, int D, int solver, do
     if (solver == DGTM_SOLVE_SVD) {
         jacobi_solve_kernel<<<1, SOLVE_THREADS, 0, s>>>(A, B, M1, D, W, work, flag);
     } else {
-        const size_t smem = (M1 <= SMEM_SOLVE_MAX) ? sizeof(double) * (size_t) M1 * M1 : 0;
+        const size_t smem = sizeof(double) * (2 * (size_t) M1 +
+                                              ((M1 <= SMEM_SOLVE_MAX) ? (size_t) M1 * M1 : 0));
         DGTM_CUDA_TRY(cudaFuncSetAttribute(cholesky_kernel,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int) (smem > 0 ? smem : 1)));
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem));
         cholesky_kernel<<<1, CHOL_THREADS, smem, s>>>(A, M1, work, flag);
         DGTM_CUDA_TRY(cudaGetLastError());
         const size_t lbytes = sizeof(double) * ((size_t) M1 * M1 + M1);

@@ -71,7 +71,9 @@ int dgtm_ctx_create(int N, int D, int K, int M1, const double *T, int ldT,
 int dgtm_ctx_destroy(dgtm_ctx *ctx);
 
 /* Choose the M-step solver (DGTM_SOLVE_*); Cholesky is the default.
- * The reference solves with a GSL SVD: comm/comm.c:1299-1348 (dagtm_solve2). */
+ * The reference solves with a GSL SVD: comm/comm.c:1299-1348 (dagtm_solve2).
+ * Limits on M1 (basis functions + bias): Cholesky 1024, SVD 1022; beyond
+ * them dgtm_mstep returns DGTM_ENOTSUP. */
 int dgtm_set_solver(dgtm_ctx *ctx, int solver);
 
 /* Load the centres Y (K x D).  Replaces the distance pass that follows a
@@ -168,7 +170,7 @@ int dgtm_next_ctemp_k(dgtm_ctx *ctx, double temp, double beta, double eps, const
 #define DGTM_PHASE_ESTEP 0        /* distance + column log-sum-exp kernel      */
 #define DGTM_PHASE_ESTEP_REDUCE 1 /* quality reductions                        */
 #define DGTM_PHASE_MSTEP_PASS 2   /* responsibility pass: G, RT                */
-#define DGTM_PHASE_MSTEP_SOLVE 3  /* slice sums, A, B, solve, Y, beta, Y split */
+#define DGTM_PHASE_MSTEP_SOLVE 3  /* slice sums, A, B, solve, Y (and its copies), beta */
 #define DGTM_NPHASES 4
 int dgtm_set_timing(dgtm_ctx *ctx, int on);
 int dgtm_reset_timing(dgtm_ctx *ctx);

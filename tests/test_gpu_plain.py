@@ -222,3 +222,29 @@ def test_reruns_are_bit_identical(pkg, oil):
             outs.append((q, b, Yn))
     assert outs[0][0] == outs[1][0] and outs[0][1] == outs[1][1]
     assert np.array_equal(outs[0][2], outs[1][2])
+
+
+@pytest.mark.parametrize("form,tol", [("fp64", 1e-8), ("bf16x3", 1e-4)])
+def test_large_basis_cholesky(pkg, orc, form, tol):
+    """M = 512 basis functions + bias (M1 = 513, the large split-precision
+    configuration's basis) on a 9^3 latent grid: the Cholesky factor lives in
+    global memory and the substitution uses 24 registers per lane.  Width
+    factor 0.5 keeps A regular (cond 2.4e7, no pivot dropped), so two FP64
+    solvers agree to cond x eps: 1e-8 on the new centres against the oracle's
+    Cholesky solve of its own A and B; the split form to its stated 1e-4."""
+    ds = pkg_mod(pkg, "datasets")
+    st = pkg_mod(pkg, "gtm_setup")
+    T = ds.gaussian_mixture(3000, 12, 6, 0.2, seed=5)
+    X, FI = st.setup_grid(3, 729, 512, 0.5)
+    rng = np.random.default_rng(5)
+    Y = T[rng.integers(0, 3000, 729)] * 0.8 + 0.1
+    beta, temp = 8.0, 1.5
+    R, _, _ = oracle_estep(orc, T, Y, beta, 1, temp)
+    G, A, B = orc.mstep_stats(R, FI, T)
+    Yo = orc.fiw(FI, orc.solve_chol(A, B))
+    with pkg.Context(T, FI, form) as c:
+        c.set_Y(Y)
+        c.estep(beta, 1, temp)
+        b, W, Yn = c.mstep(want_Y=True)
+    assert FI.shape[1] == 513
+    assert rel(Yn, Yo) <= tol
