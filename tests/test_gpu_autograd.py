@@ -112,3 +112,40 @@ def test_projection_moves_points_onto_the_map(pkg, problem):
 
     assert nearest(P) < 0.5 * nearest(Tn)
     assert torch.isfinite(P).all()
+
+
+def test_differentiation_configuration_full_size(pkg):
+    """The differentiation configuration at its full size: N = 65,536 points
+    in D = 64 from a 16-component mixture (sd 0.2), K = 4096 (64 x 64).  The
+    dense FP64 oracle is too slow here, so the FP32 forward/backward is
+    checked against the library's FP64 form on the same inputs (itself
+    parity-tested against the oracle): F = N nfree; dF/dY = -beta (G Y - R T);
+    dF/dT = -beta (T - R^T Y) with R^T Y from dgtm_map in 8-column slices;
+    dF/dbeta against FP64 central differences of N nfree.  Tolerances as for
+    the small problem: 1e-5 on F, 1e-3 on the gradients."""
+    ds = sub(pkg, "datasets")
+    st = sub(pkg, "gtm_setup")
+    N, D, K = 65536, 64, 4096
+    T = ds.gaussian_mixture(N, D, 16, 0.2, seed=0).astype(np.float32).astype(np.float64)
+    X, FI = st.setup_grid(2, K, 16, 1.0)
+    rng = np.random.default_rng(0)
+    Y = (T[rng.integers(0, N, K)] + 0.05 * rng.standard_normal((K, D))).astype(np.float32)
+    Y = Y.astype(np.float64)
+    beta, temp = 4.0, 2.0
+    F, dY, dT, db = run_fe(pkg, Y, T, beta, temp)
+    h = 1e-4 * beta
+    with pkg.Context(T, FI, "fp64") as c:
+        c.set_Y(Y)
+        fp = N * c.estep(beta + h, 1, temp)[1]
+        fm = N * c.estep(beta - h, 1, temp)[1]
+        Fref = N * c.estep(beta, 1, temp)[1]
+        RtY = np.concatenate([c.map(np.ascontiguousarray(Y[:, s:s + 8])) for s in range(0, D, 8)],
+                             axis=1)
+        c.mstep(want_W=False)
+        G, RT = c.get_stats()
+    assert F == pytest.approx(Fref, rel=1e-5)
+    dY_ref = -beta * (G[:, None] * Y - RT)
+    dT_ref = -beta * (T - RtY)
+    assert np.max(np.abs(dY - dY_ref)) <= 1e-3 * np.max(np.abs(dY_ref))
+    assert np.max(np.abs(dT - dT_ref)) <= 1e-3 * np.max(np.abs(dT_ref))
+    assert db == pytest.approx((fp - fm) / (2 * h), rel=1e-3)
