@@ -78,3 +78,37 @@ def test_headline_size_identities_and_forms(pkg, headline, beta):
     bsplit = beta_from_stats(a["G"], a["RT"], b["Y"], N, D, t2)
     print(f"beta from split statistics: {bsplit / b64 - 1:.2e}")
     assert bsplit == pytest.approx(b64, rel=2e-5)
+
+
+def test_fingerprint_shape_fp64_and_fp32(pkg):
+    """The FP64 / FP32 configuration at its own size: N = 100,000 binary
+    vectors, D = 166, K = 8000, M = 64.  One EM step in each form: the FP64
+    form's column-sum identities at 1e-12; the FP32 form against the FP64
+    form at its stated tolerances (qualities 1e-5, G and RT 1e-4, beta and the
+    new centres 1e-4).  Width 1 (cond(FI^T FI) = 1e10, no pivot dropped)
+    keeps the new centres determined; at width 2 with M = 64 they are not."""
+    ds = importlib.import_module(pkg.__name__ + ".datasets")
+    st = importlib.import_module(pkg.__name__ + ".gtm_setup")
+    N = 100_000
+    T = ds.fingerprints(N, 166, 20, seed=6)
+    X, FI = st.setup_grid(3, 8000, 64, 1.0)
+    rng = np.random.default_rng(6)
+    Y = T[rng.integers(0, N, 8000)] * 0.7 + 0.15 + 0.05 * rng.standard_normal((8000, 166))
+    temp, beta = st.start_temp(T, 0.99), 4.0
+    out = {}
+    for form in ("fp64", "fp32"):
+        with pkg.Context(T, FI, form) as c:
+            c.set_Y(Y)
+            llh, nfree = c.estep(beta, 1, temp)
+            b, _, Yn = c.mstep(want_W=False, want_Y=True)
+            G, RT = c.get_stats()
+        out[form] = dict(llh=llh, nfree=nfree, beta=b, Y=Yn, G=G, RT=RT)
+    f64, f32 = out["fp64"], out["fp32"]
+    assert abs(f64["G"].sum() - N) / N <= 1e-12
+    assert rel(f64["RT"].sum(axis=0), T.sum(axis=0)) <= 1e-12
+    assert f32["llh"] == pytest.approx(f64["llh"], rel=1e-5)
+    assert f32["nfree"] == pytest.approx(f64["nfree"], rel=1e-5)
+    assert rel(f32["G"], f64["G"]) <= 1e-4
+    assert rel(f32["RT"], f64["RT"]) <= 1e-4
+    assert f32["beta"] == pytest.approx(f64["beta"], rel=1e-4)
+    assert rel(f32["Y"], f64["Y"]) <= 1e-4
