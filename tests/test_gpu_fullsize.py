@@ -10,7 +10,8 @@ time (each MMA's FP32 sum is rounded down a little, so a longer run drifts
 low) and then moved to FP32 slots; the identities bound what that loses.
 Tolerances: identities 1e-12 (FP64 form) and 2e-5 (split form, relative);
 split form against FP64 form as stated for the split form (qualities 1e-5,
-G and RT 1e-4).  W and Y are not compared: at width 2 with M = 64 the matrix
+G and RT 1e-4; R 1e-4 absolute on three 256-point blocks).  W and Y are not
+compared: at width 2 with M = 64 the matrix
 A is numerically singular, pivots are dropped, and the new centres depend on
 rounding in any two implementations.  Beta is compared through the split
 form's statistics with the FP64 form's new centres (beta = N D / (sum_k G_k
@@ -41,13 +42,17 @@ def headline(pkg):
     return T, FI, Y, temp
 
 
+R_COLS = (0, 499_776, 999_744)  # 256-point blocks at the start, middle and end
+
+
 def one_step(pkg, form, T, FI, Y, beta, temp):
     with pkg.Context(T, FI, form) as c:
         c.set_Y(Y)
         llh, nfree = c.estep(beta, 1, temp)
+        R = [c.R_block(0, c.K, n0, 256) for n0 in R_COLS]
         b, _, Yn = c.mstep(want_W=False, want_Y=True)
         G, RT = c.get_stats()
-    return dict(llh=llh, nfree=nfree, G=G, RT=RT, beta=b, Y=Yn)
+    return dict(llh=llh, nfree=nfree, G=G, RT=RT, beta=b, Y=Yn, R=R)
 
 
 def beta_from_stats(G, RT, Y, N, D, sum_t2):
@@ -72,6 +77,9 @@ def test_headline_size_identities_and_forms(pkg, headline, beta):
     assert a["nfree"] == pytest.approx(b["nfree"], rel=1e-5)
     assert rel(a["G"], b["G"]) <= 1e-4
     assert rel(a["RT"], b["RT"]) <= 1e-4
+    # responsibilities (the split form's stated 1e-4, absolute)
+    for Ra, Rb in zip(a["R"], b["R"]):
+        assert np.max(np.abs(Ra - Rb)) <= 1e-4
     D, t2 = T.shape[1], float((T * T).sum())
     b64 = beta_from_stats(b["G"], b["RT"], b["Y"], N, D, t2)
     assert b64 == pytest.approx(b["beta"], rel=1e-12)
