@@ -411,6 +411,8 @@ def anneal(ctx: Context, beta: float, temp: float, isDA: int = 1, schedule: str 
                             ready = True
                     if expand:
                         ready = False
+                        if W is None:  # no M-step in this call: the context's last W
+                            W = ctx.get_W()
                         Knew = int(round(ctx.K ** (1.0 / L)) * 2) ** L
                         if on_expand is not None:
                             on_expand(ctx, dict(index=len(res.temp_trace) - 1, K=ctx.K,

@@ -661,8 +661,10 @@ int main(int argc, char **argv)
             return;
         ready = false;
         nexpanded++;
-        if (!have_W)
+        if (!have_W) {
             check(dgtm_get_W(ctx, W.data(), D), "dgtm_get_W");
+            have_W = true;
+        }
         if (!o.out.empty() && o.log_progress) {
             // dagtm/dagtm.cxx:1980-2096: MAP and the model at this temperature,
             // indexed by the temperature collection's last entry
