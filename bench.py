@@ -9,12 +9,22 @@ with the data resident in HBM; the data (>= 332 MB in BF16, 1.3 GB in FP64)
 is larger than L2, so no flush is needed between iterations.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+  python bench.py --anneal [--form bf16x3|fp32|fp64] [--anneal-maxloop J]
 
 Under torchrun each rank runs an independent replica (the path is one GPU
 per problem; no data-path collective); rank 0 prints one JSON line.
 ``--impl reference`` times the CPU restatement of the reference's algorithm
 (the oracle: the reference itself needs MPI/GSL/HDF5, which are absent) on
 all host cores, on a bounded sample of the same workload.
+
+``--anneal`` is a separate measurement, not the per-iteration contract: the
+wall time of a whole annealing run of the workload through the package's
+temperature loop (EXP cooling, alpha 0.99, eps 1e-6, from the start
+temperature down to 1, as the reference's dagtm runs by default), host loop
+and per-iteration synchronisation included.  Give it a cap: a temperature
+ends only when the quality changes by less than eps (or its 50-iteration
+average settles), and at the start temperature the EM keeps drifting for
+thousands of iterations (an uncapped run did not finish in 15 minutes).
 """
 from __future__ import annotations
 
@@ -51,6 +61,10 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=1024,
                     help="points in the bounded CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--anneal", action="store_true",
+                    help="time a whole annealing run instead of single iterations")
+    ap.add_argument("--anneal-maxloop", type=int, default=2000,
+                    help="iteration cap of the annealing run (0: none; see above)")
     return ap.parse_args()
 
 
@@ -354,6 +368,36 @@ def main_gb300(args):
         torch.distributed.destroy_process_group()
 
 
+def main_anneal(args):
+    """Wall time of a whole annealing run (rank 0 of one GPU)."""
+    import torch
+    pkg = importlib.import_module("da-gtm_gb300")
+    T, X, FI, Y0, beta0, temp0 = make_problem(args.n)
+    ctx = pkg.Context(T, FI, args.form)
+    ctx.set_Y(Y0)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    run = pkg.anneal(ctx, beta0, temp0, alpha=0.99, eps=1e-6, maxloop=args.anneal_maxloop)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    temps = len(set(run.temp_trace))
+    w = WORKLOAD
+    print(json.dumps({
+        "mode": "anneal",
+        "metric": "wall seconds of a whole DA-GTM annealing run (EXP, alpha 0.99, eps 1e-6)",
+        "value": wall, "unit": "s", "higher_is_better": False,
+        "iterations": run.nloop, "temperatures": temps, "iters_per_s": run.nloop / wall,
+        "final": {"temp": run.temp, "beta": run.beta, "llh": run.llh_trace[-1],
+                  "nfree": run.nfree_trace[-1]},
+        "start": {"temp": temp0, "beta": beta0},
+        "dtype": args.form, "data": "synthetic (seeded binary fingerprints)",
+        "config": {"workload": f"DA-GTM annealing run, N={args.n}, D={w['D']}, K={w['K']} "
+                               f"(20^3), M={w['M']} (4^3) + bias, {args.form} form",
+                   "N": args.n, "D": w["D"], "K": w["K"], "M": w["M"], "L": w["L"],
+                   "maxloop": args.anneal_maxloop}}), flush=True)
+    ctx.close()
+
+
 def main_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -391,7 +435,10 @@ def main_reference(args):
 
 if __name__ == "__main__":
     a = parse()
-    if a.impl == "reference":
+    if a.anneal:
+        if dist_env()[0] == 0:
+            main_anneal(a)
+    elif a.impl == "reference":
         main_reference(a)
     else:
         main_gb300(a)
