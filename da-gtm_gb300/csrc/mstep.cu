@@ -8,7 +8,8 @@
 //                   or symmetric-eigen pseudo-inverse
 //                   with exactly-zero eigenvalues dropped (the semantics of
 //                   gsl_linalg_SV_solve used by dagtm_solve2, comm/comm.c:1299-1348)
-//   update_y      : Y = FI W (dagtm/dagtm.cxx:1769), |y_k|^2 and the beta terms
+//   update_y      : Y = FI W (dagtm/dagtm.cxx:1769), |y_k|^2, the beta terms, and
+//                   the copies of Y the E-step of the FP32 / split form reads
 //   sum_ratio     : beta = N D / (sum_k G_k|y_k|^2 - 2 y_k.RT_k + sum_n |t_n|^2)
 //                   = N D / sum_kn R_kn |y_k - t_n|^2 (comm/mpicomm.c:276-302
 //                   evaluates the same sum over an explicit K x N distance matrix;
