@@ -161,3 +161,25 @@ def test_hda_expands_and_writes_snapshots(tmp_path, pkg, golden):
         assert f.read(f"ctemp.{idx}").shape == (K,)
         assert f.read(f"beta.{idx}").shape == (1,)
     assert f.read("X").shape == (512, 3) and f.read("Y").shape == (512, 12)
+
+
+def test_split_form_with_linear_cooling(tmp_path, pkg, golden):
+    # -F bf16x3 -c linear: the driver's loop over the split form agrees with
+    # the package's loop from the same set-up (one library, two host loops)
+    out = run(["-i", OIL_IN, "-o", "lin.h5", "-K", "125", "-L", "3", "-M", "8", "-s", "4",
+               "-j", "40", "-n", "-c", "linear", "-e", "1e-3", "-F", "bf16x3"], tmp_path)
+    assert "Cooling Schedule = LINEAR" in " ".join(out.split())
+    tr = trace(out)
+    st = __import__("importlib").import_module(pkg.__name__ + ".gtm_setup")
+    T = golden["T_in"].astype(np.float64)
+    _, FI0, W0, beta0 = st.random_init(T, 3, 125, 8, 2.0, seed=4)
+    with pkg.Context(T, FI0, "bf16x3", solver="svd") as c:
+        c.set_Y(FI0 @ W0)
+        ref = pkg.anneal(c, beta0, st.start_temp(T, 0.99), schedule="linear", delta=0.1,
+                         eps=1e-3, maxloop=40)
+    n = min(len(tr), len(ref.nfree_trace))
+    assert n >= 10
+    assert np.allclose(tr[:n, 3], ref.temp_trace[:n], rtol=1e-6)
+    assert np.allclose(tr[:n, 4], ref.nfree_trace[:n], rtol=1e-5, atol=1e-6)
+    f = H5File(str(tmp_path / "lin.h5"))
+    assert f.read("Y").shape == (125, 12) and np.all(np.isfinite(f.read("Y")))

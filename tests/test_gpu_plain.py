@@ -248,3 +248,19 @@ def test_large_basis_cholesky(pkg, orc, form, tol):
         b, W, Yn = c.mstep(want_Y=True)
     assert FI.shape[1] == 513
     assert rel(Yn, Yo) <= tol
+
+
+def test_linear_schedule_trajectory_fp64(pkg, orc):
+    """LINEAR cooling (temp -= delta after each temperature, -c linear,
+    dagtm/dagtm.cxx:2168-2171) on the CPU-sized mixture: the trace matches the
+    oracle's loop at 1e-9."""
+    T, FI, Y0, beta, temp0 = gmm_problem(pkg)
+    kw = dict(isDA=1, delta=0.1, eps=1e-6, maxloop=30)
+    ref = orc.run(T, FI, Y0, beta, temp0, schedule=1, solver=1, **kw)
+    with pkg.Context(T, FI, "fp64") as c:
+        c.set_Y(Y0)
+        out = pkg.anneal(c, beta, temp0, schedule="linear", **kw)
+    assert len(out.nfree_trace) == ref["n"]
+    assert np.array_equal(out.temp_trace, ref["temp_trace"])
+    assert rel(out.nfree_trace, ref["nfree_trace"]) <= 1e-9
+    assert rel(out.beta_trace, ref["beta_trace"]) <= 1e-9
