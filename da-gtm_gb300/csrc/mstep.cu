@@ -207,7 +207,8 @@ __device__ __forceinline__ double rsqrt_nr(double d)
     return r;
 }
 
-// Right-looking Cholesky in one block, one barrier per column.  Thread t
+// Right-looking Cholesky in one block for M1 > SMEM_SOLVE_MAX (L factorised in
+// place in global memory), one barrier per column.  Thread t
 // owns rows i = t/4, t/4 + 64, ... and in each the columns k = t (mod 4).
 // Column j stays unscaled while it is in use: after the barrier of step j
 // every thread reads the pivot's reciprocal square root r_j, updates its
@@ -248,11 +249,11 @@ __global__ void __launch_bounds__(CHOL_THREADS) cholesky_kernel(const double *__
                                                                int M1, double *__restrict__ work,
                                                                int *flag)
 {
-    // shared: the pivots' reciprocal square roots and A's diagonal (M1 each),
-    // then L itself when it fits (M1 <= SMEM_SOLVE_MAX), else L is in work
+    // shared: the pivots' reciprocal square roots and A's diagonal (M1 each);
+    // L is factorised in place in work (M1 > SMEM_SOLVE_MAX)
     extern __shared__ double sh[];
     double *rinv = sh, *adiag = sh + M1;
-    double *L = (M1 <= SMEM_SOLVE_MAX) ? sh + 2 * M1 : work;
+    double *L = work;
     __shared__ int bad, ndrop;
     const int tid = threadIdx.x, q = tid & 3, r0 = tid >> 2;
     const size_t n2 = (size_t) M1 * M1;
@@ -289,6 +290,85 @@ __global__ void __launch_bounds__(CHOL_THREADS) cholesky_kernel(const double *__
         const int i = (int) (e / M1), k = (int) (e % M1);
         if (k < i)
             work[e] = L[(size_t) k * M1 + i];
+        else if (k == i)
+            work[e] = L[e];
+    }
+    for (int j = tid; j < M1; j += CHOL_THREADS)
+        work[n2 + j] = rinv[j];
+    if (tid == 0) {
+        flag[0] = bad ? DGTM_ENONFINITE : 0;
+        flag[1] = ndrop;
+    }
+}
+
+// The same factorisation with L in shared memory (M1 <= SMEM_SOLVE_MAX),
+// balanced over the threads.  The trailing triangle of step j, the (i, k) with
+// j < k <= i < M1, is the first n_j (n_j + 1) / 2 entries of a table ordered by
+// k, then i, both descending (entry a (a + 1) / 2 + b holds k = M1 - 1 - a,
+// i = M1 - 1 - b), so each step's elements spread evenly.  Per column j: the
+// scaled column u_i = a_ij r_j goes to a shared vector (and to the free upper
+// triangle), then every element takes one FMA, L[i][k] -= u_i u_k.  The next
+// pivot (j+1, j+1) is the last entry of step j; its thread walks its entries
+// in reverse, so it updates the pivot first and takes its reciprocal square
+// root while the other threads work.
+__global__ void __launch_bounds__(CHOL_THREADS) cholesky_small_kernel(const double *__restrict__ A,
+                                                                     int M1,
+                                                                     double *__restrict__ work,
+                                                                     int *flag)
+{
+    extern __shared__ double sh[];
+    double *rinv = sh, *adiag = sh + M1, *u = sh + 2 * M1, *L = sh + 3 * M1;
+    uint32_t *tab = (uint32_t *) (L + M1 * M1);
+    __shared__ int bad, ndrop;
+    const int tid = threadIdx.x;
+    const int n2 = M1 * M1, npair0 = M1 * (M1 - 1) / 2;
+    if (tid == 0) {
+        bad = 0;
+        ndrop = 0;
+    }
+#pragma unroll 4
+    for (int e = tid; e < n2; e += CHOL_THREADS)
+        L[e] = A[e];
+    for (int j = tid; j < M1; j += CHOL_THREADS)
+        adiag[j] = A[j * M1 + j];
+    for (int t = tid; t < npair0; t += CHOL_THREADS) {
+        int a = (int) ((sqrtf(8.0f * (float) t + 1.0f) - 1.0f) * 0.5f);
+        while ((a + 1) * (a + 2) / 2 <= t)
+            a++;
+        while (a * (a + 1) / 2 > t)
+            a--;
+        const int b = t - a * (a + 1) / 2;
+        tab[t] = ((uint32_t) (M1 - 1 - b) << 16) | (uint32_t) (M1 - 1 - a);
+    }
+    __syncthreads();
+    if (tid == 0)
+        chol_pivot(L, adiag, M1, 0, rinv, &bad, &ndrop);
+    for (int j = 0; j < M1; j++) {
+        __syncthreads();  // r_j published, step j-1's updates done
+        const double rj = rinv[j];
+        for (int i = j + 1 + tid; i < M1; i += CHOL_THREADS) {
+            const double ui = L[i * M1 + j] * rj;
+            u[i] = ui;
+            L[j * M1 + i] = ui;
+        }
+        __syncthreads();
+        const int nj = M1 - 1 - j, npair = nj * (nj + 1) / 2;
+        if (tid < npair) {
+            for (int t = tid + (npair - 1 - tid) / CHOL_THREADS * CHOL_THREADS; t >= tid;
+                 t -= CHOL_THREADS) {
+                const uint32_t ik = tab[t];
+                const int i = (int) (ik >> 16), k = (int) (ik & 0xFFFFu);
+                L[i * M1 + k] = fma(-u[i], u[k], L[i * M1 + k]);
+                if (t == npair - 1)
+                    chol_pivot(L, adiag, M1, j + 1, rinv, &bad, &ndrop);
+            }
+        }
+    }
+    __syncthreads();
+    for (int e = tid; e < n2; e += CHOL_THREADS) {
+        const int i = e / M1, k = e - i * M1;
+        if (k < i)
+            work[e] = L[k * M1 + i];
         else if (k == i)
             work[e] = L[e];
     }
@@ -531,11 +611,20 @@ int launch_solve(const double *A, const double *B, int M1, int D, int solver, do
     if (solver == DGTM_SOLVE_SVD) {
         jacobi_solve_kernel<<<1, SOLVE_THREADS, 0, s>>>(A, B, M1, D, W, work, flag);
     } else {
-        const size_t smem = sizeof(double) * (2 * (size_t) M1 +
-                                              ((M1 <= SMEM_SOLVE_MAX) ? (size_t) M1 * M1 : 0));
-        DGTM_CUDA_TRY(cudaFuncSetAttribute(cholesky_kernel,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem));
-        cholesky_kernel<<<1, CHOL_THREADS, smem, s>>>(A, M1, work, flag);
+        if (M1 <= SMEM_SOLVE_MAX) {
+            const size_t smem = sizeof(double) * (3 * (size_t) M1 + (size_t) M1 * M1) +
+                                sizeof(uint32_t) * ((size_t) M1 * (M1 - 1) / 2);
+            DGTM_CUDA_TRY(cudaFuncSetAttribute(cholesky_small_kernel,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int) smem));
+            cholesky_small_kernel<<<1, CHOL_THREADS, smem, s>>>(A, M1, work, flag);
+        } else {
+            const size_t smem = sizeof(double) * 2 * (size_t) M1;
+            DGTM_CUDA_TRY(cudaFuncSetAttribute(cholesky_kernel,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int) smem));
+            cholesky_kernel<<<1, CHOL_THREADS, smem, s>>>(A, M1, work, flag);
+        }
         DGTM_CUDA_TRY(cudaGetLastError());
         const size_t lbytes = sizeof(double) * ((size_t) M1 * M1 + M1);
         const int l_in_smem = lbytes <= 96 * 1024;
