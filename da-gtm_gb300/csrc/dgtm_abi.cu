@@ -55,6 +55,7 @@ struct dgtm_ctx {
     double *tt;        // N
     double sum_tt;
     double *FI;        // K x M1
+    float2 *FIp;       // K x M1 FP32 (hi, lo) pairs for update_y (FP32 / split forms)
     double *Y64;       // K x D (master copy of the centres)
     float *Y32;        // K x D (FP32 form)
     double *yy;        // K
@@ -177,7 +178,7 @@ void free_ctx(dgtm_ctx *c)
 {
     if (!c)
         return;
-    void *ptrs[] = {c->T64, c->T32, c->tt, c->FI, c->Y64, c->Y32, c->yy, c->W, c->colstat,
+    void *ptrs[] = {c->T64, c->T32, c->tt, c->FI, c->FIp, c->Y64, c->Y32, c->yy, c->W, c->colstat,
                     c->part, c->Gpart, c->RTpart, c->G, c->RT, c->A, c->B, c->work, c->bterm, c->abpart,
                     c->scal, c->flag};
     for (void *p : ptrs)
@@ -289,6 +290,10 @@ int dgtm_ctx_create(int N, int D, int K, int M1, const double *T, int ldT, const
                           sizeof(double) * D, N, cudaMemcpyHostToDevice, c->stream));
     CKC(copy_rows(c->FI, sizeof(double) * M1, FI, sizeof(double) * (size_t) ldFI,
                           sizeof(double) * M1, K, cudaMemcpyHostToDevice, c->stream));
+    if (precision != DGTM_FP64) {
+        CK(dev_alloc(&c->FIp, (size_t) K * M1));
+        CK(launch_to_pairs(c->FI, (size_t) K * M1, c->FIp, c->stream));
+    }
     CK(launch_norms(c->T64, N, D, c->tt, c->stream));
     CK(launch_sum_ratio(c->tt, N, 0.0, 1.0, c->scal, c->stream));
     CKC(cudaMemcpyAsync(c->hscal, c->scal, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
@@ -496,8 +501,8 @@ int dgtm_mstep(dgtm_ctx *ctx, double *W, int ldW, double *Y, int ldY, double *be
         cp.Y32 = ctx->Y32;
     else if (ctx->precision == DGTM_BF16X3)
         tc_y_copies(ctx->tc, &cp);
-    DGTM_TRY(launch_update_y(ctx->FI, ctx->W, ctx->G, ctx->RT, K, M1, D, ctx->Y64, ctx->yy,
-                             ctx->bterm, cp, ctx->flag + 2, ctx->stream));
+    DGTM_TRY(launch_update_y(ctx->FI, ctx->FIp, ctx->W, ctx->G, ctx->RT, K, M1, D, ctx->Y64,
+                             ctx->yy, ctx->bterm, cp, ctx->flag + 2, ctx->stream));
     DGTM_TRY(launch_sum_ratio(ctx->bterm, K, ctx->sum_tt, (double) ((long long) N * D),
                               ctx->scal, ctx->stream));
     DGTM_TRY(phase_end(ctx, DGTM_PHASE_MSTEP_SOLVE, nsmall));

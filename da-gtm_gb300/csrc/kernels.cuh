@@ -71,10 +71,14 @@ struct YCopies {
     int Dp = 0, Kpad = 0;
 };
 // Y = FI W, yy = |y|^2, bterm_k = G_k yy_k - 2 y_k.RT_k (G/RT may be null: no
-// bterm), and the copies in cp.  ticket: one device int of scratch.
-int launch_update_y(const double *FI, const double *W, const double *G, const double *RT,
-                    int K, int M1, int D, double *Y, double *yy, double *bterm,
-                    const YCopies &cp, int *ticket, cudaStream_t s);
+// bterm), and the copies in cp.  FIp: FI as (hi, lo) FP32 pairs for the
+// compensated FP32 product (FP32 and split forms), or null for FP64 FMAs.
+// ticket: one device int of scratch.
+int launch_update_y(const double *FI, const float2 *FIp, const double *W, const double *G,
+                    const double *RT, int K, int M1, int D, double *Y, double *yy,
+                    double *bterm, const YCopies &cp, int *ticket, cudaStream_t s);
+// dst[i] = src[i] as an unevaluated sum of two FP32 (hi, lo).
+int launch_to_pairs(const double *src, size_t n, float2 *dst, cudaStream_t s);
 // AUTO cooling (ctemp.cu): scratch doubles per batch of kb centres and
 // whether the eigen kernel keeps its D x D block in shared memory.
 size_t ctemp_scratch_doubles(int D, int kb, bool *eig_in_smem);

@@ -642,15 +642,25 @@ int launch_solve(const double *A, const double *B, int M1, int D, int solver, do
 // Y = FI W, the per-centre terms of beta and the E-step's copies of Y
 // ---------------------------------------------------------------------------
 // A warp computes two centres over all depths: lane l owns depths l + 32 c,
-// c < NC (passes of 32 NC depths when D > 256), with 2 NC FP64 accumulators.
-// Per basis function it loads the two FI values once (broadcast) and
-// W[m][l + 32 c] from shared memory, where W is padded with zeros to whole
-// passes so the loop has no guards.  The FP64 pipe (about 2 FMA per clock
-// per SM) bounds the kernel; each warp takes the next centre pair from a
-// counter (*ticket, zero at launch), so the pairs spread evenly over the SM
-// sub-partitions whatever the CTA placement.  The warp sums
-// |y|^2, y.RT and, for the split form, |y_hi + y_lo|^2 of each centre by
-// lane partials and shuffles in a fixed order.
+// c < NC (passes of 32 NC depths when D > 256).  Per basis function it loads
+// the two FI values once (broadcast) and W[m][l + 32 c] from shared memory,
+// where W is padded with zeros to whole passes so the loop has no guards.
+// Each warp takes the next centre pair from a counter (*ticket, zero at
+// launch), so the pairs spread evenly over the SM sub-partitions whatever the
+// CTA placement.  The warp sums |y|^2, y.RT and, for the split form,
+// |y_hi + y_lo|^2 of each centre by lane partials and shuffles in a fixed
+// order (FP64).
+//
+// Two arithmetics.  DF = false (the FP64 form): 2 NC FP64 accumulators per
+// lane; the FP64 pipe (about 2 FMA per clock per SM) bounds the kernel.
+// DF = true (the FP32 and split-BF16 forms): FI and W as unevaluated sums of
+// two FP32 (hi + lo, 48 bits) and each product accumulated by Dot2 of Ogita,
+// Rump and Oishi ("Accurate sum and dot product", SIAM J. Sci. Comput. 26,
+// 2005): the high parts' product split exactly by an FMA, the cross terms
+// added to its error, the running sum kept exact by Knuth's TwoSum.  The
+// result is as accurate as a product in twice FP32's precision (~1e-14
+// relative), far inside those forms' 1e-4, on the FP32 pipe, which is 64
+// times as wide as the FP64 one.
 constexpr int UY_THREADS = 256;
 constexpr int UY_NCMAX = 8;
 constexpr size_t UY_WSMEM_MAX = 110 * 1024;  // two CTAs per SM
@@ -663,19 +673,64 @@ __device__ __forceinline__ double uy_warp_sum(double v)
     return v;
 }
 
-template <int NC, bool WS>
-__global__ void __launch_bounds__(UY_THREADS) update_y_kernel(
-    const double *__restrict__ FI, const double *__restrict__ Wg, const double *__restrict__ G,
-    const double *__restrict__ RT, int K, int M1, int D, int Dw, double *__restrict__ Y,
-    double *__restrict__ yy, double *__restrict__ bterm, YCopies cp, int *ticket)
+// p + s += (a.x + a.y) (w.x + w.y); the _rn intrinsics keep each rounding
+// where Dot2 needs it (no contraction into an FMA)
+__device__ __forceinline__ void dot2_step(float &p, float &s, float2 a, float2 w)
 {
-    extern __shared__ double Ws[];  // M1 x Dw, zero past D
+    const float h = __fmul_rn(a.x, w.x);
+    float r = fmaf(a.x, w.x, -h);
+    r = fmaf(a.x, w.y, r);
+    r = fmaf(a.y, w.x, r);
+    const float t = __fadd_rn(p, h);
+    const float z = __fsub_rn(t, p);
+    const float q = __fadd_rn(__fsub_rn(p, __fsub_rn(t, z)), __fsub_rn(h, z));
+    p = t;
+    s = __fadd_rn(s, __fadd_rn(q, r));
+}
+
+__device__ __forceinline__ float2 f64_to_pair(double x)
+{
+    const float hi = (float) x;
+    return make_float2(hi, (float) (x - (double) hi));
+}
+
+__global__ void to_pairs_kernel(const double *__restrict__ src, size_t n, float2 *__restrict__ dst)
+{
+    for (size_t i = blockIdx.x * (size_t) blockDim.x + threadIdx.x; i < n;
+         i += (size_t) gridDim.x * blockDim.x)
+        dst[i] = f64_to_pair(src[i]);
+}
+
+int launch_to_pairs(const double *src, size_t n, float2 *dst, cudaStream_t s)
+{
+    size_t blocks = (n + 255) / 256;
+    if (blocks > 4096)
+        blocks = 4096;
+    to_pairs_kernel<<<(int) blocks, 256, 0, s>>>(src, n, dst);
+    DGTM_CUDA_TRY(cudaGetLastError());
+    return DGTM_OK;
+}
+
+template <int NC, bool WS, bool DF>
+__global__ void __launch_bounds__(UY_THREADS) update_y_kernel(
+    const double *__restrict__ FI, const float2 *__restrict__ FIp, const double *__restrict__ Wg,
+    const double *__restrict__ G, const double *__restrict__ RT, int K, int M1, int D, int Dw,
+    double *__restrict__ Y, double *__restrict__ yy, double *__restrict__ bterm, YCopies cp,
+    int *ticket)
+{
+    // M1 x Dw, zero past D: FP64 values, or (hi, lo) pairs of the same size
+    extern __shared__ double Ws[];
+    float2 *const Wp = reinterpret_cast<float2 *>(Ws);
     if (WS) {
         const int n = M1 * Dw;
 #pragma unroll 4
         for (int i = threadIdx.x; i < n; i += UY_THREADS) {
             const int m = i / Dw, d = i - m * Dw;
-            Ws[i] = (d < D) ? Wg[(size_t) m * D + d] : 0.0;
+            const double w = (d < D) ? Wg[(size_t) m * D + d] : 0.0;
+            if constexpr (DF)
+                Wp[i] = f64_to_pair(w);
+            else
+                Ws[i] = w;
         }
         __syncthreads();
     }
@@ -690,23 +745,48 @@ __global__ void __launch_bounds__(UY_THREADS) update_y_kernel(
         if (k0 >= K)
             break;
         const int nr = (k0 + 1 < K) ? 2 : 1;
-        const double *f0 = FI + (size_t) k0 * M1;
-        const double *f1 = FI + (size_t) (k0 + nr - 1) * M1;
+        const int k1 = k0 + nr - 1;
         double syy[2] = {0.0, 0.0}, srt[2] = {0.0, 0.0}, sq[2] = {0.0, 0.0};
         for (int db = 0; db < D; db += 32 * NC) {
-            double a0[NC], a1[NC];
+            double y0[NC], y1[NC];
+            if constexpr (DF) {
+                float p0[NC], s0[NC], p1[NC], s1[NC];
 #pragma unroll
-            for (int c = 0; c < NC; c++)
-                a0[c] = a1[c] = 0.0;
-            for (int m = 0; m < M1; m++) {
-                const double x0 = __ldg(f0 + m), x1 = __ldg(f1 + m);
+                for (int c = 0; c < NC; c++)
+                    p0[c] = s0[c] = p1[c] = s1[c] = 0.f;
+                const float2 *f0 = FIp + (size_t) k0 * M1, *f1 = FIp + (size_t) k1 * M1;
+                for (int m = 0; m < M1; m++) {
+                    const float2 x0 = f0[m], x1 = f1[m];
+#pragma unroll
+                    for (int c = 0; c < NC; c++) {
+                        const int d = db + lane + 32 * c;
+                        const float2 w = WS ? Wp[m * Dw + d]
+                                            : ((d < D) ? f64_to_pair(Wg[(size_t) m * D + d])
+                                                       : make_float2(0.f, 0.f));
+                        dot2_step(p0[c], s0[c], x0, w);
+                        dot2_step(p1[c], s1[c], x1, w);
+                    }
+                }
 #pragma unroll
                 for (int c = 0; c < NC; c++) {
-                    const int d = db + lane + 32 * c;
-                    const double w =
-                        WS ? Ws[m * Dw + d] : ((d < D) ? __ldg(Wg + (size_t) m * D + d) : 0.0);
-                    a0[c] = fma(x0, w, a0[c]);
-                    a1[c] = fma(x1, w, a1[c]);
+                    y0[c] = (double) p0[c] + (double) s0[c];
+                    y1[c] = (double) p1[c] + (double) s1[c];
+                }
+            } else {
+#pragma unroll
+                for (int c = 0; c < NC; c++)
+                    y0[c] = y1[c] = 0.0;
+                const double *f0 = FI + (size_t) k0 * M1, *f1 = FI + (size_t) k1 * M1;
+                for (int m = 0; m < M1; m++) {
+                    const double x0 = __ldg(f0 + m), x1 = __ldg(f1 + m);
+#pragma unroll
+                    for (int c = 0; c < NC; c++) {
+                        const int d = db + lane + 32 * c;
+                        const double w =
+                            WS ? Ws[m * Dw + d] : ((d < D) ? __ldg(Wg + (size_t) m * D + d) : 0.0);
+                        y0[c] = fma(x0, w, y0[c]);
+                        y1[c] = fma(x1, w, y1[c]);
+                    }
                 }
             }
 #pragma unroll
@@ -719,7 +799,7 @@ __global__ void __launch_bounds__(UY_THREADS) update_y_kernel(
                     if (r >= nr)
                         break;
                     const int k = k0 + r;
-                    const double y = r ? a1[c] : a0[c];
+                    const double y = r ? y1[c] : y0[c];
                     const size_t e = (size_t) k * D + d;
                     Y[e] = y;
                     syy[r] = fma(y, y, syy[r]);
@@ -767,28 +847,28 @@ __global__ void __launch_bounds__(UY_THREADS) update_y_kernel(
     }
 }
 
-template <bool WS>
-using UpdateYKernel = void (*)(const double *, const double *, const double *, const double *, int,
-                               int, int, int, double *, double *, double *, YCopies, int *);
+using UpdateYKernel = void (*)(const double *, const float2 *, const double *, const double *,
+                               const double *, int, int, int, int, double *, double *, double *,
+                               YCopies, int *);
 
-template <bool WS>
-UpdateYKernel<WS> update_y_for(int nc)
+template <bool WS, bool DF>
+UpdateYKernel update_y_for(int nc)
 {
     switch (nc) {
-    case 1: return update_y_kernel<1, WS>;
-    case 2: return update_y_kernel<2, WS>;
-    case 3: return update_y_kernel<3, WS>;
-    case 4: return update_y_kernel<4, WS>;
-    case 5: return update_y_kernel<5, WS>;
-    case 6: return update_y_kernel<6, WS>;
-    case 7: return update_y_kernel<7, WS>;
-    default: return update_y_kernel<8, WS>;
+    case 1: return update_y_kernel<1, WS, DF>;
+    case 2: return update_y_kernel<2, WS, DF>;
+    case 3: return update_y_kernel<3, WS, DF>;
+    case 4: return update_y_kernel<4, WS, DF>;
+    case 5: return update_y_kernel<5, WS, DF>;
+    case 6: return update_y_kernel<6, WS, DF>;
+    case 7: return update_y_kernel<7, WS, DF>;
+    default: return update_y_kernel<8, WS, DF>;
     }
 }
 
-int launch_update_y(const double *FI, const double *W, const double *G, const double *RT, int K,
-                    int M1, int D, double *Y, double *yy, double *bterm, const YCopies &cp,
-                    int *ticket, cudaStream_t s)
+int launch_update_y(const double *FI, const float2 *FIp, const double *W, const double *G,
+                    const double *RT, int K, int M1, int D, double *Y, double *yy, double *bterm,
+                    const YCopies &cp, int *ticket, cudaStream_t s)
 {
     DGTM_CUDA_TRY(cudaMemsetAsync(ticket, 0, sizeof(int), s));
     int dev = 0, sms = 0;
@@ -798,21 +878,20 @@ int launch_update_y(const double *FI, const double *W, const double *G, const do
     if (nc > UY_NCMAX)
         nc = UY_NCMAX;
     const int Dw = ceil_div(D, 32 * nc) * 32 * nc;
-    const size_t wbytes = sizeof(double) * (size_t) M1 * Dw;
+    const size_t wbytes = sizeof(double) * (size_t) M1 * Dw;  // = pairs of FP32
     const bool ws = wbytes <= UY_WSMEM_MAX;
+    const bool df = FIp != nullptr;
     int blocks = ceil_div(K, 2 * (UY_THREADS / 32));
     const int cap = sms * (ws ? 2 : 4);
     if (blocks > cap)
         blocks = cap;
-    if (ws) {
-        const UpdateYKernel<true> k = update_y_for<true>(nc);
+    const UpdateYKernel k = ws ? (df ? update_y_for<true, true>(nc) : update_y_for<true, false>(nc))
+                               : (df ? update_y_for<false, true>(nc) : update_y_for<false, false>(nc));
+    if (ws)
         DGTM_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int) wbytes));
-        k<<<blocks, UY_THREADS, wbytes, s>>>(FI, W, G, RT, K, M1, D, Dw, Y, yy, bterm, cp, ticket);
-    } else {
-        update_y_for<false>(nc)<<<blocks, UY_THREADS, 0, s>>>(FI, W, G, RT, K, M1, D, Dw, Y, yy,
-                                                             bterm, cp, ticket);
-    }
+    k<<<blocks, UY_THREADS, ws ? wbytes : 0, s>>>(FI, FIp, W, G, RT, K, M1, D, Dw, Y, yy, bterm, cp,
+                                                 ticket);
     DGTM_CUDA_TRY(cudaGetLastError());
     return DGTM_OK;
 }

@@ -163,3 +163,22 @@ def test_tiny_and_ragged_shapes_bf16x3(pkg, orc, N, D, K, M1):
         G, RT = c.get_stats()
     assert rel(G, R.sum(1)) <= 1e-4
     assert rel(RT, R @ T) <= 1e-4
+
+
+@pytest.mark.parametrize("form", ["bf16x3", "fp32"])
+def test_centre_product_is_compensated(pkg, form):
+    """The FP32 and split forms form Y = FI W from FP32 pairs (hi + lo) with the
+    compensated dot product Dot2 (Ogita, Rump and Oishi, 2005): the new centres
+    match a host FP64 product of the returned W to 1e-10, far inside the
+    forms' 1e-4 (plain FP32 products would give ~1e-7)."""
+    ds = sub(pkg, "datasets")
+    st = sub(pkg, "gtm_setup")
+    T = ds.gaussian_mixture(4000, 40, 8, 0.2, seed=12)
+    X, FI = st.setup_grid(3, 512, 64, 1.0)
+    rng = np.random.default_rng(12)
+    Y = T[rng.integers(0, 4000, 512)] * 0.8 + 0.1
+    with pkg.Context(T, FI, form) as c:
+        c.set_Y(Y)
+        c.estep(3.0, 1, 2.0)
+        b, W, Yn = c.mstep(want_W=True, want_Y=True)
+    assert rel(Yn, FI @ W) <= 1e-10
