@@ -929,10 +929,8 @@ __global__ void __launch_bounds__(1024) sum_ratio_kernel(const double *__restric
                                                         double add, double num, double *out)
 {
     __shared__ double red[32];
-    const int per = (n + blockDim.x - 1) / blockDim.x;
-    const int b = threadIdx.x * per, e = min(n, b + per);
     double s = 0.0;
-    for (int i = b; i < e; i++)
+    for (int i = threadIdx.x; i < n; i += blockDim.x)  // coalesced, fixed order
         s += v[i];
     s = block_sum_fixed(s, red);
     if (threadIdx.x == 0) {
@@ -953,10 +951,8 @@ __global__ void __launch_bounds__(1024) sum_dev_kernel(const double *__restrict_
                                                       const double *__restrict__ add, double *out)
 {
     __shared__ double red[32];
-    const int per = (n + blockDim.x - 1) / blockDim.x;
-    const int b = threadIdx.x * per, e = min(n, b + per);
     double s = 0.0;
-    for (int i = b; i < e; i++)
+    for (int i = threadIdx.x; i < n; i += blockDim.x)  // coalesced, fixed order
         s += v[i];
     s = block_sum_fixed(s, red);
     if (threadIdx.x == 0)
@@ -975,10 +971,8 @@ __global__ void __launch_bounds__(1024) sum_pairs_kernel(const double *__restric
                                                         int nb, double *out)
 {
     __shared__ double red[32];
-    const int per = (nb + blockDim.x - 1) / blockDim.x;
-    const int b = threadIdx.x * per, e = min(nb, b + per);
     double s0 = 0.0, s1 = 0.0;
-    for (int i = b; i < e; i++) {
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) {  // coalesced, fixed order
         s0 += part[2 * i];
         s1 += part[2 * i + 1];
     }
