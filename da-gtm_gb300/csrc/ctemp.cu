@@ -1,6 +1,6 @@
 // ctemp.cu -- the next critical temperature of the AUTO cooling schedule
 // (comm/mpicomm.c:562-674, dagtm_mpi_next_ctemp and its helper; the limit
-// filter of dagtm_vector_max, comm/comm.c:2149-2161), FP64.
+// filter of dagtm_vector_max, comm/comm.c:2149-2161).
 //
 // For centre k, with x_n = t_n - y_k and R_kn the responsibilities of the last
 // E-step, the reference forms
@@ -13,35 +13,58 @@
 // limit_k = (temp - eps) gg_k 2 / beta count as 0 (as dagtm_vector_max sets
 // them), the largest remaining value gives ctemp_k = beta / (2 gg_k) lambda.
 //
-//   scatter_kernel : one CTA per (centre, 32 x 32 tile of the upper triangle);
-//                    recomputes R_kn as the R-block kernel does and sums S1, S2
-//                    over all points in a fixed order
-//   eig_kernel     : one CTA per (centre, block); parallel cyclic Jacobi
-//                    (round-robin pairing) on the D x D block, then the filter
+// Centres go in batches; inside a batch the points go in chunks small enough
+// that the chunk's data and responsibilities stay in L2:
+//   r_block_kernel  : R of the batch's centres over the chunk (FP64, once)
+//   scatter_kernel  : one CTA per (centre, 64 x 64 tile of the upper
+//                     triangle), 4 x 4 entries of S1 and of S2 per thread,
+//                     added over the chunk's points in a fixed order and into
+//                     the running sums of the earlier chunks
+//   eig_kernel      : one CTA per (centre, block); parallel cyclic Jacobi
+//                     (round-robin pairing) on the D x D block, then the filter
+// Arithmetic type F: FP64 for the FP64 form.  The FP32 and split forms form
+// x and the products in FP32 (partial sums over 128 points go into FP64) and
+// run the Jacobi sweeps in FP32: their stated error is 1e-4, and GB300's FP32
+// pipe is about 64 times its FP64 pipe.
 #include "common.cuh"
 #include "kernels.cuh"
 
 #include <float.h>
 #include <math.h>
+#include <type_traits>
 
 namespace dgtm {
 
 namespace {
 
-constexpr int SC_THREADS = 256;
-constexpr int SC_TILE = 32;   // output tile (rows x cols of S)
-constexpr int SC_PTS = 32;    // points per staged chunk
-constexpr int EIG_THREADS = 256;
+constexpr int SC_THREADS = 256;  // 16 x 16 threads, 4 x 4 entries each
+constexpr int SC_TILE = 64;      // output tile (rows x cols of S)
+constexpr int SC_PTS = 32;       // points per staged sub-chunk
+constexpr int SC_FLUSH = 4;      // FP32 partial sums go into FP64 every 4 sub-chunks
+// threads of the eigen kernel: 256 for small matrices (several blocks per SM);
+// above that 1024 (FP64, the matrix fills shared memory: one block per SM) or
+// 512 (FP32: two blocks per SM)
+constexpr int EIG_SMALL_D = 96;
+// largest dynamic shared memory a block may opt into on sm_10x (227 KB), less
+// room for the kernel's static arrays
+constexpr size_t EIG_SMEM_MAX = 232448 - 1024;
 constexpr double GG_MIN = 1e-250;  // comm/mpicomm.c:601-612
+constexpr size_t ALIGN = 256;
 
-__global__ void __launch_bounds__(SC_THREADS) scatter_kernel(
-    const double *__restrict__ T, const double *__restrict__ Y, const double *__restrict__ tt,
-    const double *__restrict__ yy, const double2 *__restrict__ colstat, int N, int D, int K,
-    double c, int k0, double *__restrict__ S, double *__restrict__ gsum)
+size_t align_up(size_t b) { return (b + ALIGN - 1) / ALIGN * ALIGN; }
+
+// blockIdx.x = centre in the batch, blockIdx.y = tile pair (ti <= tj).
+// Tc: the chunk's points (nn x D, row-major); Rb: kb x nn responsibilities.
+// S (per centre: S1 then S2, D x D) holds the entries i <= j only.
+template <typename F>
+__global__ void __launch_bounds__(SC_THREADS, 2) scatter_kernel(
+    const F *__restrict__ Tc, const double *__restrict__ Y, const double *__restrict__ Rb, int nn,
+    int D, int k0, int first, double *__restrict__ S, double *__restrict__ gsum)
 {
-    __shared__ double xr[SC_PTS][SC_TILE], xc[SC_PTS][SC_TILE], w[SC_PTS];
+    __shared__ __align__(16) F xr[SC_PTS][SC_TILE];
+    __shared__ __align__(16) F xc[SC_PTS][SC_TILE];
+    __shared__ F yr[SC_TILE], yc[SC_TILE], w1[SC_PTS], w2[SC_PTS];
     const int kl = blockIdx.x, k = k0 + kl;
-    // upper-triangle tile (ti <= tj) from the linear tile index
     int ti = 0, rem = blockIdx.y;
     const int nb = (D + SC_TILE - 1) / SC_TILE;
     while (rem >= nb - ti) {
@@ -49,104 +72,129 @@ __global__ void __launch_bounds__(SC_THREADS) scatter_kernel(
         ti++;
     }
     const int tj = ti + rem;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int r = threadIdx.x >> 3, c0 = (threadIdx.x & 7) * 4;  // this thread's 1 x 4 entries
+    const int i0 = ti * SC_TILE, j0 = tj * SC_TILE;
+    const int tr = threadIdx.x >> 4, tc = threadIdx.x & 15;
     const double *yk = Y + (size_t) k * D;
-    double s1[4] = {0.0, 0.0, 0.0, 0.0}, s2[4] = {0.0, 0.0, 0.0, 0.0}, g = 0.0;
-    for (int nb0 = 0; nb0 < N; nb0 += SC_PTS) {
-        __syncthreads();
-        // responsibilities of the chunk's points for centre k (warp per point)
-        for (int p = warp; p < SC_PTS; p += SC_THREADS / 32) {
-            const int n = nb0 + p;
-            double rv = 0.0;
-            if (n < N) {
-                const double2 cs = colstat[n];
-                if (isnan(cs.y)) {
-                    rv = 1.0 / (double) K;
-                } else {
-                    double dot = 0.0;
-                    for (int d = lane; d < D; d += 32)
-                        dot += yk[d] * T[(size_t) n * D + d];
+    if (threadIdx.x < SC_TILE) {
+        const int d = i0 + threadIdx.x;
+        yr[threadIdx.x] = d < D ? (F) yk[d] : F(0);
+    } else if (threadIdx.x < 2 * SC_TILE) {
+        const int d = j0 + threadIdx.x - SC_TILE;
+        yc[threadIdx.x - SC_TILE] = d < D ? (F) yk[d] : F(0);
+    }
+    constexpr bool F32 = std::is_same<F, float>::value;
+    F a1[4][4], a2[4][4];
+    double d1[4][4], d2[4][4];
 #pragma unroll
-                    for (int o = 16; o > 0; o >>= 1)
-                        dot += __shfl_down_sync(0xffffffffu, dot, o);
-                    dot = __shfl_sync(0xffffffffu, dot, 0);
-                    const double dd = ((-2.0 * dot) + yy[k]) + tt[n];
-                    rv = exp(-c * (dd - cs.x) - cs.y);
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+            a1[i][j] = a2[i][j] = F(0), d1[i][j] = d2[i][j] = 0.0;
+    const double *rk = Rb + (size_t) kl * nn;
+    double g = 0.0;  // lanes of warp 0: every 32nd point, summed at the end
+    int sub = 0;
+    for (int p0 = 0; p0 < nn; p0 += SC_PTS) {
+        __syncthreads();
+        if (threadIdx.x < SC_PTS) {
+            const int p = p0 + threadIdx.x;
+            const double r = p < nn ? rk[p] : 0.0;
+            g += r;
+            const F wf = (F) r;
+            w1[threadIdx.x] = wf;
+            w2[threadIdx.x] = wf * wf;
+        }
+        for (int e = threadIdx.x; e < SC_PTS * SC_TILE; e += SC_THREADS) {
+            const int p = e / SC_TILE, j = e % SC_TILE;
+            const bool ok = p0 + p < nn;
+            const F *tp = Tc + (size_t) (ok ? p0 + p : 0) * D;
+            xr[p][j] = (ok && i0 + j < D) ? tp[i0 + j] - yr[j] : F(0);
+            xc[p][j] = (ok && j0 + j < D) ? tp[j0 + j] - yc[j] : F(0);
+        }
+        __syncthreads();
+#pragma unroll 4
+        for (int p = 0; p < SC_PTS; p++) {
+            F a[4], b[4];
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                a[i] = xr[p][tr * 4 + i];
+                b[i] = xc[p][tc * 4 + i];
+            }
+            const F u = w1[p], v = w2[p];
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                const F ua = u * a[i], va = v * a[i];
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    a1[i][j] = fma(ua, b[j], a1[i][j]);
+                    a2[i][j] = fma(va, b[j], a2[i][j]);
                 }
             }
-            if (lane == 0)
-                w[p] = rv;
         }
-        // x = t - y over the tile's row and column ranges
-        for (int e = threadIdx.x; e < SC_PTS * SC_TILE; e += SC_THREADS) {
-            const int p = e / SC_TILE, j = e % SC_TILE, n = nb0 + p;
-            const int di = ti * SC_TILE + j, dj = tj * SC_TILE + j;
-            xr[p][j] = (n < N && di < D) ? T[(size_t) n * D + di] - yk[di] : 0.0;
-            xc[p][j] = (n < N && dj < D) ? T[(size_t) n * D + dj] - yk[dj] : 0.0;
-        }
-        __syncthreads();
-        for (int p = 0; p < SC_PTS; p++) {
-            const double wp = w[p], w2 = wp * wp, a = xr[p][r];
-            if (threadIdx.x == 0)
-                g += wp;
+        if (F32 && ++sub == SC_FLUSH) {
+            sub = 0;
 #pragma unroll
-            for (int e = 0; e < 4; e++) {
-                const double v = a * xc[p][c0 + e];
-                s1[e] = fma(wp, v, s1[e]);
-                s2[e] = fma(w2, v, s2[e]);
+            for (int i = 0; i < 4; i++)
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    d1[i][j] += (double) a1[i][j];
+                    d2[i][j] += (double) a2[i][j];
+                    a1[i][j] = a2[i][j] = F(0);
+                }
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            d1[i][j] += (double) a1[i][j];
+            d2[i][j] += (double) a2[i][j];
+        }
+    if (blockIdx.y == 0 && threadIdx.x < 32) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            g += __shfl_down_sync(0xffffffffu, g, o);
+        if (threadIdx.x == 0)
+            gsum[kl] = first ? g : gsum[kl] + g;
+    }
+    double *S1 = S + (size_t) kl * 2 * D * D, *S2 = S1 + (size_t) D * D;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const int row = i0 + tr * 4 + i;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const int col = j0 + tc * 4 + j;
+            if (row < D && col < D && row <= col) {
+                const size_t at = (size_t) row * D + col;
+                S1[at] = first ? d1[i][j] : S1[at] + d1[i][j];
+                S2[at] = first ? d2[i][j] : S2[at] + d2[i][j];
             }
         }
     }
-    // both triangles of S1 (block 0) and S2 (block 1) of this centre
-    double *S1 = S + (size_t) kl * 2 * D * D, *S2 = S1 + (size_t) D * D;
-    const int i = ti * SC_TILE + r;
-#pragma unroll
-    for (int e = 0; e < 4; e++) {
-        const int j = tj * SC_TILE + c0 + e;
-        if (i < D && j < D) {
-            S1[(size_t) i * D + j] = s1[e];
-            S2[(size_t) i * D + j] = s2[e];
-            S1[(size_t) j * D + i] = s1[e];
-            S2[(size_t) j * D + i] = s2[e];
-        }
-    }
-    if (blockIdx.y == 0 && threadIdx.x == 0)
-        gsum[kl] = g;
 }
 
-// fixed-order block sum (every thread gets the result)
-__device__ double block_sum(double v, double *red)
+template <typename F>
+size_t eig_smem_bytes(int D)
 {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1)
-        v += __shfl_down_sync(0xffffffffu, v, o);
-    __syncthreads();
-    if (lane == 0)
-        red[warp] = v;
-    __syncthreads();
-    double t = 0.0;
-    for (int i = 0; i < EIG_THREADS / 32; i++)
-        t += red[i];
-    return t;
+    const size_t npair = (size_t) (D + 1) / 2;
+    return sizeof(F) * ((size_t) D * D + 2 * npair) + sizeof(int) * 2 * npair;
 }
 
 // blockIdx.x = centre in the batch, blockIdx.y = 0: 2 S1, 1: 2 (S1 - S2)
+template <int EIG_THREADS, typename F>
 __global__ void __launch_bounds__(EIG_THREADS) eig_kernel(const double *__restrict__ S, int D,
-                                                          int in_smem, double *__restrict__ Mg,
+                                                          int in_smem, F *__restrict__ Mg,
                                                           const double *__restrict__ gg,
                                                           double lim_scale, double *__restrict__ out)
 {
-    extern __shared__ double sh[];
+    extern __shared__ __align__(16) unsigned char sh_raw[];
+    F *sh = reinterpret_cast<F *>(sh_raw);
     const int kl = blockIdx.x, which = blockIdx.y;
     const int npair = (D + 1) / 2, nslot = 2 * npair;  // slot D (odd D) is a dummy
-    double *M = in_smem ? sh : Mg + ((size_t) kl * 2 + which) * D * D;
-    double *cs = in_smem ? sh + (size_t) D * D : sh;
-    double *sn = cs + npair;
+    F *M = in_smem ? sh : Mg + ((size_t) kl * 2 + which) * D * D;
+    F *cs = in_smem ? sh + (size_t) D * D : sh;
+    F *sn = cs + npair;
     int *pp = (int *) (sn + npair), *qq = pp + npair;
-    __shared__ double red[EIG_THREADS / 32];
-    __shared__ int done;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const double *S1 = S + (size_t) kl * 2 * D * D, *S2 = S1 + (size_t) D * D;
     const double gk = gg[kl];
     if (gk == 0.0) {
@@ -156,40 +204,43 @@ __global__ void __launch_bounds__(EIG_THREADS) eig_kernel(const double *__restri
         return;
     }
     // gg < GG_MIN: the reference scales H by 1 / GG_MIN before gsl_eigen_symm
-    const double sc = (gk < GG_MIN) ? 1.0 / GG_MIN : 1.0;
-    for (int e = threadIdx.x; e < D * D; e += EIG_THREADS)
-        M[e] = (which == 0 ? 2.0 * S1[e] : 2.0 * (S1[e] - S2[e])) * sc;
+    // and the eigenvalues back.  The FP32 sweeps take H / gg (1e250 is outside
+    // FP32) and multiply the eigenvalues by gg.
+    double sc = 1.0, back = 1.0;
+    if (sizeof(F) == 8) {
+        if (gk < GG_MIN)
+            sc = 1.0 / GG_MIN, back = GG_MIN;
+    } else {
+        sc = 1.0 / gk, back = gk;
+    }
+    for (int e = threadIdx.x; e < D * D; e += EIG_THREADS) {
+        const int i = e / D, j = e - i * D;
+        const size_t at = i <= j ? (size_t) i * D + j : (size_t) j * D + i;
+        M[e] = (F) ((which == 0 ? 2.0 * S1[at] : 2.0 * (S1[at] - S2[at])) * sc);
+    }
     __syncthreads();
+    // A rotation is skipped when |a_pq| <= eps sqrt|a_pp a_qq| (the threshold
+    // of Demmel and Veselic's Jacobi, SIAM J. Matrix Anal. Appl. 13, 1992);
+    // the sweeps end when one rotates nothing.
+    const F eps = sizeof(F) == 8 ? (F) DBL_EPSILON : (F) FLT_EPSILON;
     for (int sweep = 0; sweep < 100; sweep++) {
-        double off = 0.0, tot = 0.0;
-        for (int e = threadIdx.x; e < D * D; e += EIG_THREADS) {
-            const double v = M[e] * M[e];
-            tot += v;
-            if (e / D != e % D)
-                off += v;
-        }
-        off = block_sum(off, red);
-        tot = block_sum(tot, red);
-        if (threadIdx.x == 0)
-            done = (off <= DBL_EPSILON * DBL_EPSILON * tot);
-        __syncthreads();
-        if (done)
-            break;
+        int rotated = 0;
         for (int step = 0; step < nslot - 1; step++) {
             for (int t = threadIdx.x; t < npair; t += EIG_THREADS) {
                 // round-robin pairing: slot 0 fixed, the others rotate
                 const int a = (t == 0) ? 0 : 1 + ((t - 1 + step) % (nslot - 1));
                 const int b = 1 + ((nslot - 2 - t + step) % (nslot - 1));
                 const int p = min(a, b), q = max(a, b);
-                double cc = 1.0, ss = 0.0;
+                F cc = F(1), ss = F(0);
                 if (q < D) {
-                    const double apq = M[(size_t) p * D + q];
-                    if (apq != 0.0) {
-                        const double app = M[(size_t) p * D + p], aqq = M[(size_t) q * D + q];
-                        const double th = (aqq - app) / (2.0 * apq);
-                        const double tn = (th >= 0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
-                        cc = 1.0 / sqrt(tn * tn + 1.0);
+                    const F apq = M[(size_t) p * D + q];
+                    const F app = M[(size_t) p * D + p], aqq = M[(size_t) q * D + q];
+                    if (fabs(apq) > eps * (sqrt(fabs(app)) * sqrt(fabs(aqq)))) {
+                        const F th = (aqq - app) / (F(2) * apq);
+                        const F tn = (th >= F(0) ? F(1) : F(-1)) / (fabs(th) + sqrt(th * th + F(1)));
+                        cc = F(1) / sqrt(tn * tn + F(1));
                         ss = tn * cc;
+                        rotated |= (ss != F(0));  // 0 when th * th overflows
                     }
                 }
                 pp[t] = p;
@@ -198,36 +249,46 @@ __global__ void __launch_bounds__(EIG_THREADS) eig_kernel(const double *__restri
                 sn[t] = ss;
             }
             __syncthreads();
-            for (int idx = threadIdx.x; idx < npair * D; idx += EIG_THREADS) {
-                const int t = idx / D, j = idx % D;
-                if (qq[t] >= D || sn[t] == 0.0)
-                    continue;
+            // rows p and q of every rotation, one warp per pair
+            for (int t = warp; t < npair; t += EIG_THREADS / 32) {
+                const F ct = cs[t], st = sn[t];
                 const int p = pp[t], q = qq[t];
-                const double mp = M[(size_t) p * D + j], mq = M[(size_t) q * D + j];
-                M[(size_t) p * D + j] = cs[t] * mp - sn[t] * mq;
-                M[(size_t) q * D + j] = sn[t] * mp + cs[t] * mq;
+                if (q >= D || st == F(0))
+                    continue;
+                F *rp = M + (size_t) p * D, *rq = M + (size_t) q * D;
+                for (int j = lane; j < D; j += 32) {
+                    const F mp = rp[j], mq = rq[j];
+                    rp[j] = ct * mp - st * mq;
+                    rq[j] = st * mp + ct * mq;
+                }
             }
             __syncthreads();
-            for (int idx = threadIdx.x; idx < npair * D; idx += EIG_THREADS) {
-                const int t = idx / D, j = idx % D;
-                if (qq[t] >= D || sn[t] == 0.0)
-                    continue;
+            // then columns p and q
+            for (int t = warp; t < npair; t += EIG_THREADS / 32) {
+                const F ct = cs[t], st = sn[t];
                 const int p = pp[t], q = qq[t];
-                const double mp = M[(size_t) j * D + p], mq = M[(size_t) j * D + q];
-                M[(size_t) j * D + p] = cs[t] * mp - sn[t] * mq;
-                M[(size_t) j * D + q] = sn[t] * mp + cs[t] * mq;
+                if (q >= D || st == F(0))
+                    continue;
+                for (int j = lane; j < D; j += 32) {
+                    F *r = M + (size_t) j * D;
+                    const F mp = r[p], mq = r[q];
+                    r[p] = ct * mp - st * mq;
+                    r[q] = st * mp + ct * mq;
+                }
             }
             __syncthreads();
         }
+        if (!__syncthreads_or(rotated))
+            break;
     }
     if (threadIdx.x == 0) {
         // eigenvalues at or above the limit count as 0, then the largest
         const double limit = lim_scale * gk;
         double mx = -INFINITY;
         for (int i = 0; i < D; i++) {
-            double l = M[(size_t) i * D + i];
-            if (gk < GG_MIN)
-                l *= GG_MIN;
+            double l = (double) M[(size_t) i * D + i];
+            if (back != 1.0)
+                l *= back;
             if (l >= limit)
                 l = 0.0;
             mx = fmax(mx, l);
@@ -236,40 +297,100 @@ __global__ void __launch_bounds__(EIG_THREADS) eig_kernel(const double *__restri
     }
 }
 
-}  // namespace
-
-size_t ctemp_scratch_doubles(int D, int kb, bool *eig_in_smem)
+template <int NT, typename F>
+int launch_eig(int kb, int D, bool in_smem, const double *S, F *Mg, const double *gg,
+               double lim_scale, double *out, cudaStream_t s)
 {
-    const size_t dd = (size_t) D * D;
-    const size_t smem = sizeof(double) * (dd + (size_t) 2 * ((D + 1) / 2)) +
-                        sizeof(int) * (size_t) 2 * ((D + 1) / 2);
-    *eig_in_smem = smem <= (size_t) 200 * 1024;
-    return (size_t) kb * 2 * dd * (*eig_in_smem ? 1 : 2) + (size_t) 4 * kb;
-}
-
-int launch_ctemp_batch(const double *T, const double *Y, const double *tt, const double *yy,
-                       const double2 *colstat, int N, int D, int K, double c, int k0, int kb,
-                       const double *gg_dev, double lim_scale, double *scratch, double *gsum_dev,
-                       double *out_dev, cudaStream_t s)
-{
-    bool in_smem = false;
-    ctemp_scratch_doubles(D, kb, &in_smem);
-    double *S = scratch;
-    double *Mg = scratch + (size_t) kb * 2 * D * D;
-    const int nb = (D + SC_TILE - 1) / SC_TILE;
-    scatter_kernel<<<dim3(kb, nb * (nb + 1) / 2), SC_THREADS, 0, s>>>(T, Y, tt, yy, colstat, N, D,
-                                                                      K, c, k0, S, gsum_dev);
-    DGTM_CUDA_TRY(cudaGetLastError());
-    const int npair = (D + 1) / 2;
-    const size_t small = sizeof(double) * 2 * npair + sizeof(int) * 2 * npair;
-    const size_t smem = (in_smem ? sizeof(double) * (size_t) D * D : 0) + small;
-    DGTM_CUDA_TRY(cudaFuncSetAttribute(eig_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int) smem));
-    eig_kernel<<<dim3(kb, 2), EIG_THREADS, smem, s>>>(S, D, in_smem ? 1 : 0, Mg,
-                                                      gg_dev ? gg_dev : gsum_dev, lim_scale,
-                                                      out_dev);
+    const size_t smem = in_smem ? eig_smem_bytes<F>(D)
+                                : eig_smem_bytes<F>(D) - sizeof(F) * (size_t) D * D;
+    DGTM_CUDA_TRY(cudaFuncSetAttribute(eig_kernel<NT, F>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem));
+    eig_kernel<NT, F><<<dim3(kb, 2), NT, smem, s>>>(S, D, in_smem ? 1 : 0, Mg, gg, lim_scale, out);
     DGTM_CUDA_TRY(cudaGetLastError());
     return DGTM_OK;
+}
+
+template <typename F>
+int run_batch(const CtempPlan &pl, const double *T64, const float *T32, const double *Y,
+              const double *tt, const double *yy, const double2 *colstat, int N, int D, int K,
+              double c, int k0, int kb, const double *gg_dev, double lim_scale, void *scratch,
+              double *gsum_dev, double *out_dev, cudaStream_t s)
+{
+    unsigned char *base = (unsigned char *) scratch;
+    double *S = (double *) base;
+    base += align_up(sizeof(double) * (size_t) pl.kb * 2 * D * D);
+    F *Mg = nullptr;
+    if (!pl.eig_in_smem) {
+        Mg = (F *) base;
+        base += align_up(sizeof(F) * (size_t) pl.kb * 2 * D * D);
+    }
+    double *Rb = (double *) base;
+    base += align_up(sizeof(double) * (size_t) pl.kb * pl.nn);
+    float *Tbuf = (float *) base;  // FP32 copy of a chunk when the context has none
+    const int ntp = ((D + SC_TILE - 1) / SC_TILE) * ((D + SC_TILE - 1) / SC_TILE + 1) / 2;
+    for (int n0 = 0; n0 < N; n0 += pl.nn) {
+        const int nn = (N - n0 < pl.nn) ? N - n0 : pl.nn;
+        int r = launch_r_block(T64, Y, tt, yy, colstat, D, K, c, k0, kb, n0, nn, Rb, s);
+        if (r != DGTM_OK)
+            return r;
+        const F *Tc;
+        if constexpr (std::is_same<F, double>::value) {
+            Tc = T64 + (size_t) n0 * D;
+        } else if (T32) {
+            Tc = T32 + (size_t) n0 * D;
+        } else {
+            r = launch_to_f32(T64 + (size_t) n0 * D, (size_t) nn * D, Tbuf, s);
+            if (r != DGTM_OK)
+                return r;
+            Tc = Tbuf;
+        }
+        scatter_kernel<F><<<dim3(kb, ntp), SC_THREADS, 0, s>>>(Tc, Y, Rb, nn, D, k0, n0 == 0 ? 1 : 0,
+                                                                S, gsum_dev);
+        DGTM_CUDA_TRY(cudaGetLastError());
+    }
+    const double *gg = gg_dev ? gg_dev : gsum_dev;
+    if (D <= EIG_SMALL_D)
+        return launch_eig<256, F>(kb, D, pl.eig_in_smem, S, Mg, gg, lim_scale, out_dev, s);
+    if (sizeof(F) == 8)
+        return launch_eig<1024, F>(kb, D, pl.eig_in_smem, S, Mg, gg, lim_scale, out_dev, s);
+    return launch_eig<512, F>(kb, D, pl.eig_in_smem, S, Mg, gg, lim_scale, out_dev, s);
+}
+
+}  // namespace
+
+CtempPlan ctemp_plan(int N, int D, int K, bool f32, bool have_t32, size_t budget, int nn_max)
+{
+    CtempPlan pl;
+    pl.f32 = f32;
+    pl.nn = N < nn_max ? N : nn_max;
+    if (pl.nn < 1)
+        pl.nn = 1;
+    const size_t fsz = f32 ? sizeof(float) : sizeof(double);
+    pl.eig_in_smem = (f32 ? eig_smem_bytes<float>(D) : eig_smem_bytes<double>(D)) <= EIG_SMEM_MAX;
+    const size_t dd = (size_t) D * D;
+    const size_t per = sizeof(double) * 2 * dd + (pl.eig_in_smem ? 0 : fsz * 2 * dd) +
+                       sizeof(double) * (size_t) pl.nn;
+    const size_t fixed = (f32 && !have_t32) ? sizeof(float) * (size_t) pl.nn * D : 0;
+    size_t kb = budget > fixed + per ? (budget - fixed) / per : 1;
+    if (kb > (size_t) K)
+        kb = (size_t) K;
+    pl.kb = (int) kb;
+    pl.scratch_bytes = align_up(sizeof(double) * (size_t) pl.kb * 2 * dd) +
+                       (pl.eig_in_smem ? 0 : align_up(fsz * (size_t) pl.kb * 2 * dd)) +
+                       align_up(sizeof(double) * (size_t) pl.kb * pl.nn) + align_up(fixed) + ALIGN;
+    return pl;
+}
+
+int launch_ctemp_batch(const CtempPlan &pl, const double *T64, const float *T32, const double *Y,
+                       const double *tt, const double *yy, const double2 *colstat, int N, int D,
+                       int K, double c, int k0, int kb, const double *gg_dev, double lim_scale,
+                       void *scratch, double *gsum_dev, double *out_dev, cudaStream_t s)
+{
+    if (pl.f32)
+        return run_batch<float>(pl, T64, T32, Y, tt, yy, colstat, N, D, K, c, k0, kb, gg_dev,
+                                lim_scale, scratch, gsum_dev, out_dev, s);
+    return run_batch<double>(pl, T64, T32, Y, tt, yy, colstat, N, D, K, c, k0, kb, gg_dev,
+                             lim_scale, scratch, gsum_dev, out_dev, s);
 }
 
 }  // namespace dgtm

@@ -114,6 +114,19 @@ int dev_alloc(P **p, size_t count)
             return _r;              \
     } while (0)
 
+// an integer from the environment, or dflt when unset or out of [lo, hi]
+int env_int(const char *name, int dflt, int lo, int hi)
+{
+    const char *v = getenv(name);
+    if (!v || !*v)
+        return dflt;
+    char *end = nullptr;
+    const long x = strtol(v, &end, 10);
+    if (*end || x < lo || x > hi)
+        return dflt;
+    return (int) x;
+}
+
 int check_ctx(dgtm_ctx *c)
 {
     if (!c) {
@@ -674,16 +687,16 @@ int dgtm_next_ctemp_k(dgtm_ctx *ctx, double temp, double beta, double eps, const
     }
     const int N = ctx->N, D = ctx->D, K = ctx->K;
     const double c = ctx->isDA ? ctx->beta / (2.0 * ctx->temp) : ctx->beta / 2.0;
-    bool in_smem = false;
-    const size_t per = ctemp_scratch_doubles(D, 1, &in_smem);
-    int kb = (int) ((size_t) (256u << 20) / (per * sizeof(double)));
-    if (kb < 1)
-        kb = 1;
-    if (kb > K)
-        kb = K;
+    // scratch budget and points per chunk: DGTM_CTEMP_SCRATCH_MB (default 256)
+    // and DGTM_CTEMP_CHUNK (default 16384) override them
+    const size_t budget = (size_t) env_int("DGTM_CTEMP_SCRATCH_MB", 256, 1, 1 << 20) << 20;
+    const int nn_max = env_int("DGTM_CTEMP_CHUNK", 16384, 1, 1 << 30);
+    const CtempPlan pl = ctemp_plan(N, D, K, ctx->precision != DGTM_FP64, ctx->T32 != nullptr,
+                                    budget, nn_max);
+    const int kb = pl.kb;
     double *scratch = nullptr, *dgg = nullptr, *dgsum = nullptr, *dout = nullptr;
     std::vector<double> out((size_t) 2 * K), gsum(K);
-    int rc = dev_alloc(&scratch, ctemp_scratch_doubles(D, kb, &in_smem));
+    int rc = dev_alloc(&scratch, (pl.scratch_bytes + sizeof(double) - 1) / sizeof(double));
     if (rc == DGTM_OK)
         rc = dev_alloc(&dgsum, K);
     if (rc == DGTM_OK)
@@ -697,9 +710,9 @@ int dgtm_next_ctemp_k(dgtm_ctx *ctx, double temp, double beta, double eps, const
     const double lim_scale = (temp - eps) * 2.0 / beta;
     for (int k0 = 0; rc == DGTM_OK && e == cudaSuccess && k0 < K; k0 += kb) {
         const int nb = (K - k0 < kb) ? K - k0 : kb;
-        rc = launch_ctemp_batch(ctx->T64, ctx->Y64, ctx->tt, ctx->yy, ctx->colstat, N, D, K, c,
-                                k0, nb, gg ? dgg + k0 : nullptr, lim_scale, scratch, dgsum + k0,
-                                dout + (size_t) 2 * k0, ctx->stream);
+        rc = launch_ctemp_batch(pl, ctx->T64, ctx->T32, ctx->Y64, ctx->tt, ctx->yy, ctx->colstat,
+                                N, D, K, c, k0, nb, gg ? dgg + k0 : nullptr, lim_scale, scratch,
+                                dgsum + k0, dout + (size_t) 2 * k0, ctx->stream);
     }
     if (rc == DGTM_OK && e == cudaSuccess)
         e = cudaMemcpyAsync(out.data(), dout, sizeof(double) * 2 * K, cudaMemcpyDeviceToHost,

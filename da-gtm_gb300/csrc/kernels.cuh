@@ -79,16 +79,23 @@ int launch_update_y(const double *FI, const float2 *FIp, const double *W, const 
                     double *bterm, const YCopies &cp, int *ticket, cudaStream_t s);
 // dst[i] = src[i] as an unevaluated sum of two FP32 (hi, lo).
 int launch_to_pairs(const double *src, size_t n, float2 *dst, cudaStream_t s);
-// AUTO cooling (ctemp.cu): scratch doubles per batch of kb centres and
-// whether the eigen kernel keeps its D x D block in shared memory.
-size_t ctemp_scratch_doubles(int D, int kb, bool *eig_in_smem);
+// AUTO cooling (ctemp.cu).  A plan fixes the batch of centres (kb), the chunk
+// of points (nn), the arithmetic (FP32 for the FP32 and split forms) and the
+// scratch bytes one batch needs, within a budget of scratch bytes.
+struct CtempPlan {
+    int kb = 1, nn = 1;
+    bool f32 = false, eig_in_smem = true;
+    size_t scratch_bytes = 0;
+};
+CtempPlan ctemp_plan(int N, int D, int K, bool f32, bool have_t32, size_t budget, int nn_max);
 // For centres k0 .. k0+kb-1: gsum = row sums of R, out[2 i + w] = largest
 // eigenvalue of 2 S1 (w = 0) / 2 (S1 - S2) (w = 1) below lim_scale * gg_i
-// (eigenvalues at or above it count as 0).  gg_dev null: gg = gsum.
-int launch_ctemp_batch(const double *T, const double *Y, const double *tt, const double *yy,
-                       const double2 *colstat, int N, int D, int K, double c, int k0, int kb,
-                       const double *gg_dev, double lim_scale, double *scratch, double *gsum_dev,
-                       double *out_dev, cudaStream_t s);
+// (eigenvalues at or above it count as 0).  gg_dev null: gg = gsum.  T32: the
+// context's FP32 copy of T, or null (an FP32 plan then converts each chunk).
+int launch_ctemp_batch(const CtempPlan &pl, const double *T64, const float *T32, const double *Y,
+                       const double *tt, const double *yy, const double2 *colstat, int N, int D,
+                       int K, double c, int k0, int kb, const double *gg_dev, double lim_scale,
+                       void *scratch, double *gsum_dev, double *out_dev, cudaStream_t s);
 // yy = |y|^2 for a given Y.
 int launch_norms(const double *X, int rows, int D, double *out, cudaStream_t s);
 // out[0] = sum_i v[i] (fixed order) + add; out[1] = num / out[0].

@@ -5,8 +5,9 @@ The oracle builds each centre's 2D x 2D H and takes all its eigenvalues, as
 the reference does; the library takes the two D x D diagonal blocks of H
 after the orthogonal block transform.  The same responsibilities go into both
 (the FP64 form reproduces the oracle's R to ~1e-12), so the critical
-temperatures agree to FP64 eigenvalue accuracy: 1e-9 relative.  The split-BF16
-form's R carries its stated 1e-4 error.
+temperatures agree to FP64 eigenvalue accuracy: 1e-9 relative.  The FP32 and
+split-BF16 forms form the scatter matrices and run the eigen sweeps in FP32,
+and the split form's R carries its stated error: 1e-4 relative.
 """
 import importlib
 
@@ -44,8 +45,12 @@ def oracle_ctemp(orc, T, Y, beta, temp, eps, gg=None):
 @pytest.mark.parametrize("kind,N,D,K,form,tol", [
     ("binary", 600, 20, 64, "fp64", 1e-9),
     ("real", 500, 13, 49, "fp64", 1e-9),
+    ("binary", 400, 166, 9, "fp64", 1e-9),   # D x D block just inside shared memory
     ("real", 300, 170, 9, "fp64", 1e-9),     # D x D block beyond shared memory
     ("binary", 600, 20, 64, "bf16x3", 1e-4),
+    ("binary", 400, 166, 9, "bf16x3", 1e-4),  # FP32 sweeps, 512 threads
+    ("real", 500, 13, 49, "fp32", 1e-4),
+    ("real", 300, 250, 4, "fp32", 1e-4),      # FP32 block beyond shared memory
 ])
 def test_next_ctemp_matches_oracle(pkg, orc, kind, N, D, K, form, tol):
     T, FI, Y = problem(pkg, kind, N, D, K)
@@ -59,6 +64,26 @@ def test_next_ctemp_matches_oracle(pkg, orc, kind, N, D, K, form, tol):
     assert np.isfinite(ref) and ref < temp
     assert got == pytest.approx(ref, rel=tol)
     assert got_w == pytest.approx(ref, rel=tol)
+
+
+@pytest.mark.parametrize("form,tol", [("fp64", 1e-9), ("bf16x3", 1e-4)])
+def test_next_ctemp_in_chunks_and_batches(pkg, orc, monkeypatch, form, tol):
+    """Points in chunks of 96 (5 chunks, the last one ragged) and centres in
+    batches of 2 (1 MB of scratch at D = 166): the running sums over the
+    chunks and the batch offsets give the single-pass result."""
+    T, FI, Y = problem(pkg, "binary", 450, 166, 9)
+    beta, temp, eps = 30.0 / 166, 4.0, 1e-6
+    ref, R = oracle_ctemp(orc, T, Y, beta, temp, eps)
+    with pkg.Context(T, FI, form) as c:
+        c.set_Y(Y)
+        c.estep(beta, 1, temp)
+        whole, whole_k = c.next_ctemp(temp, beta, eps, per_centre=True)
+        monkeypatch.setenv("DGTM_CTEMP_CHUNK", "96")
+        monkeypatch.setenv("DGTM_CTEMP_SCRATCH_MB", "1")
+        parts, parts_k = c.next_ctemp(temp, beta, eps, per_centre=True)
+    assert whole == pytest.approx(ref, rel=tol)
+    assert parts == pytest.approx(ref, rel=tol)
+    np.testing.assert_allclose(parts_k, whole_k, rtol=1e-12 if form == "fp64" else 1e-4)
 
 
 def test_next_ctemp_oil(pkg, orc, golden):
