@@ -142,9 +142,12 @@ int dgtm_get_R_block(dgtm_ctx *ctx, int k0, int nk, int n0, int nn, double *R,
  * above (temp - eps) gg_k 2 / beta count as 0, ctemp_k = beta / 2 / gg_k
  * times the largest (HUGE_VAL when gg_k = 0), and *ctemp = max_k ctemp_k.
  * gg: K weights on the host (the reference passes its G of the last M-step),
- * or NULL for the row sums of the current R.  FP64.  The work is about
- * K N D^2 FMA plus K eigenproblems of size D: meant for the problem sizes
- * the reference runs AUTO on.
+ * or NULL for the row sums of the current R.  The work is about K N D^2 FMA
+ * plus 2K symmetric eigenproblems of size D.  The FP64 form computes in
+ * FP64; the FP32 and split forms build S1 and S2 from FP32 products (sums
+ * in FP64) and take the eigenvalues in FP32, within their stated 1e-4.
+ * Scratch: DGTM_CTEMP_SCRATCH_MB (default 256) bounds the device memory of
+ * one batch of centres, DGTM_CTEMP_CHUNK (default 16384) the points per chunk.
  * Replaces dagtm_mpi_next_ctemp and its helper (comm/mpicomm.c:562-674) with
  * dagtm_vector_max (comm/comm.c:2149-2161), called at dagtm/dagtm.cxx:1919-1934.
  */
