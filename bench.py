@@ -10,6 +10,7 @@ is larger than L2, so no flush is needed between iterations.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
   python bench.py --anneal [--form bf16x3|fp32|fp64] [--anneal-maxloop J]
+  python bench.py --ctemp [--form bf16x3|fp32|fp64] [--n N] [--ctemp-calls C]
 
 Under torchrun each rank runs an independent replica (the path is one GPU
 per problem; no data-path collective); rank 0 prints one JSON line.
@@ -25,6 +26,10 @@ and per-iteration synchronisation included.  Give it a cap: a temperature
 ends only when the quality changes by less than eps (or its 50-iteration
 average settles), and at the start temperature the EM keeps drifting for
 thousands of iterations (an uncapped run did not finish in 15 minutes).
+
+``--ctemp`` is another separate measurement: the wall time of the AUTO
+schedule's critical-temperature call (dgtm_next_ctemp) on the workload, after
+one E-step at the start temperature.
 """
 from __future__ import annotations
 
@@ -65,6 +70,9 @@ def parse():
                     help="time a whole annealing run instead of single iterations")
     ap.add_argument("--anneal-maxloop", type=int, default=2000,
                     help="iteration cap of the annealing run (0: none; see above)")
+    ap.add_argument("--ctemp", action="store_true",
+                    help="time the AUTO schedule's critical-temperature call instead")
+    ap.add_argument("--ctemp-calls", type=int, default=1)
     return ap.parse_args()
 
 
@@ -398,6 +406,33 @@ def main_anneal(args):
     ctx.close()
 
 
+def main_ctemp(args):
+    """Wall time of dgtm_next_ctemp on the workload (rank 0 of one GPU)."""
+    import torch
+    pkg = importlib.import_module("da-gtm_gb300")
+    T, X, FI, Y0, beta0, temp0 = make_problem(args.n)
+    times = []
+    with pkg.Context(T, FI, args.form) as ctx:
+        ctx.set_Y(Y0)
+        ctx.estep(beta0, 1, temp0)
+        torch.cuda.synchronize()
+        for _ in range(max(1, args.ctemp_calls)):
+            t0 = time.perf_counter()
+            ct = ctx.next_ctemp(temp0, beta0, 1e-6)
+            times.append(time.perf_counter() - t0)
+    w = WORKLOAD
+    print(json.dumps({
+        "mode": "ctemp",
+        "metric": "wall seconds of one AUTO critical-temperature call (dgtm_next_ctemp)",
+        "value": times[-1], "unit": "s", "higher_is_better": False, "calls_s": times,
+        "ctemp": ct, "temp": temp0, "beta": beta0,
+        "dtype": args.form, "data": "synthetic (seeded binary fingerprints)",
+        "config": {"workload": f"AUTO critical temperature, N={args.n}, D={w['D']}, K={w['K']} "
+                               f"(20^3), {args.form} form, after one E-step at the start "
+                               "temperature",
+                   "N": args.n, "D": w["D"], "K": w["K"]}}), flush=True)
+
+
 def main_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -438,6 +473,9 @@ if __name__ == "__main__":
     if a.anneal:
         if dist_env()[0] == 0:
             main_anneal(a)
+    elif a.ctemp:
+        if dist_env()[0] == 0:
+            main_ctemp(a)
     elif a.impl == "reference":
         main_reference(a)
     else:
