@@ -123,6 +123,32 @@ def test_ctemp_and_eig(orc, golden):
     assert orc.ctemp(T) == pytest.approx(ref, rel=1e-12)
 
 
+def test_next_ctemp_block_form(orc, golden):
+    """The GPU takes the spectrum of H = [[2 S1 - S2, -S2], [-S2, 2 S1 - S2]]
+    as that of 2 S1 together with that of 2 (S1 - S2): the orthogonal
+    (1/sqrt 2)[[I, I], [I, -I]] block-diagonalises H.  A numpy restatement in
+    that form gives the oracle's ctemp, which builds the 2D x 2D H as
+    comm/mpicomm.c:562-674 does.  Oil data, its stored centres, beta at temp 2.5."""
+    T, Y, beta = golden["T"], golden["Y"], golden["beta"][0]
+    temp, eps = 2.5, 1e-6
+    R, _, _ = orc.resp(orc.dist(Y, T), beta, 1, temp)
+    gg = R.sum(axis=1)
+    ref = orc.next_ctemp(T, Y, R, gg, temp, beta, eps)
+    best = -np.inf
+    for k in range(Y.shape[0]):
+        X = T - Y[k]
+        S1 = (R[k][:, None] * X).T @ X
+        S2 = ((R[k] ** 2)[:, None] * X).T @ X
+        lam = np.concatenate([np.linalg.eigvalsh(2 * S1), np.linalg.eigvalsh(2 * (S1 - S2))])
+        H = np.block([[2 * S1 - S2, -S2], [-S2, 2 * S1 - S2]])
+        np.testing.assert_allclose(np.sort(lam), np.linalg.eigvalsh(H), rtol=0,
+                                   atol=1e-12 * np.abs(lam).max())
+        lam = np.where(lam >= (temp - eps) * gg[k] * 2 / beta, 0.0, lam)
+        best = max(best, beta / 2 / gg[k] * lam.max())
+    assert np.isfinite(ref) and ref < temp
+    assert best == pytest.approx(ref, rel=1e-9)
+
+
 def test_mstep_stats_against_numpy(orc, golden):
     Dm = orc.dist(golden["Y"], golden["T"])
     R, _, _ = orc.resp(Dm, golden["beta"][0], 1, 1.0)
