@@ -4,7 +4,8 @@ Python side of the C ABI declared in ``include/dagtm_gb300.h``: the context
 that owns the device buffers of one GTM problem, the E-step and M-step that
 replace ``dagtm_mpi_resp``/``dagtm_mpi_qual``/``dagtm_mpi_beta`` and the inline
 M-step of ``dagtm/dagtm.cxx``, and the temperature loop of
-``dagtm/dagtm.cxx:1508-2206`` (EXP and LINEAR schedules) driving them.
+``dagtm/dagtm.cxx:1508-2206`` (EXP, LINEAR and AUTO schedules, and the
+hierarchical expansion) driving them.
 
 The package directory is named ``da-gtm_gb300``; import it with
 ``importlib.import_module("da-gtm_gb300")``.  There is no CPU fallback: the
@@ -142,6 +143,10 @@ class Context:
         FI = _f64(FI)
         if T.ndim != 2 or FI.ndim != 2:
             raise ValueError("T and FI must be 2-D")
+        if precision not in PRECISIONS:
+            raise ValueError(f"precision must be one of {sorted(PRECISIONS)}, not {precision!r}")
+        if solver not in SOLVERS:
+            raise ValueError(f"solver must be one of {sorted(SOLVERS)}, not {solver!r}")
         self.N, self.D = T.shape
         self.K, self.M1 = FI.shape
         self.precision = precision
@@ -191,7 +196,11 @@ class Context:
 
     # calls
     def set_solver(self, solver: str):
+        """"cholesky" or "svd"; kept across set_basis."""
+        if solver not in SOLVERS:
+            raise ValueError(f"solver must be one of {sorted(SOLVERS)}, not {solver!r}")
         _check(load_library().dgtm_set_solver(self._h, SOLVERS[solver]))
+        self.solver = solver
 
     def set_Y(self, Y):
         Y = _f64(Y)
