@@ -102,3 +102,42 @@ def test_driver_hda_matches_anneal(cpu_driver, tmp_path, pkg, orc, golden):
     # (a C++ loop, numpy), and A is ill-conditioned on the oil basis: the
     # tolerance of the GPU driver tests
     np.testing.assert_allclose(nf, run.nfree_trace, rtol=1e-5, atol=1e-5)
+
+
+def test_driver_checkpoint_restart_and_outputs(cpu_driver, tmp_path, golden):
+    """Checkpoints every 5 iterations, restart, -R, -I and the output layout
+    (dagtm/dagtm.cxx:1609-1687, 1161-1232, 2342-2414).  A checkpoint is taken
+    after an iteration's E-step, before its M-step, as the reference takes it:
+    a restart from the 10th therefore repeats the E-step of iteration 10 (its
+    iterations 11..16 are 10..15 of an uninterrupted run) and ends on the same
+    centres as an uninterrupted run of 15.  Started below the first critical
+    temperature, so that the trace moves from one iteration to the next."""
+    common = ["-i", OIL_IN, "-K", "125", "-L", "3", "-M", "8", "-s", "3", "-a", "0.9",
+              "-e", "0", "-S", "1.5", "-Q", "cholesky"]
+    drive(cpu_driver, common + ["-j", "15", "-n", "-p", "-o", "full.h5"], tmp_path)
+    drive(cpu_driver, common + ["-j", "10", "-P", "5", "-w", "ck."], tmp_path)
+    assert (tmp_path / "ck.5.h5").exists() and (tmp_path / "ck.10.h5").exists()
+    ck = H5File(str(tmp_path / "ck.10.h5"))
+    for name in ("X", "FI", "Y", "beta", "temp", "iter", "seed", "qual"):
+        assert name in ck.datasets, name
+    assert int(ck.read("iter")[0]) == 10
+    drive(cpu_driver, ["-i", OIL_IN, "-r", "ck.10.h5", "-j", "6", "-n", "-p", "-R",
+                       "-Q", "cholesky", "-e", "0", "-o", "rest.h5"], tmp_path)
+    full, rest = H5File(str(tmp_path / "full.h5")), H5File(str(tmp_path / "rest.h5"))
+    nf = full.read("NFree")
+    assert np.min(np.abs(np.diff(nf[9:15]))) > 1e-6 * np.max(np.abs(nf))  # the trace moves
+    np.testing.assert_allclose(rest.read("NFree"), nf[9:15], rtol=1e-13)
+    np.testing.assert_allclose(rest.read("LLH"), full.read("LLH")[9:15], rtol=1e-13)
+    np.testing.assert_allclose(rest.read("Y"), full.read("Y"), rtol=1e-12, atol=1e-15)
+    assert int(rest.read("iter")[0]) == 16
+    for name in ("T", "M", "X", "FI", "Y", "W", "beta", "temp", "iter", "seed", "qual", "id", "lb",
+                 "Temp", "LLH", "NFree"):
+        assert name in full.datasets, name
+    assert np.array_equal(full.read("T"), golden["T_in"].astype(np.float64))
+    R = rest.read("R")
+    assert R.shape == (125, 1000) and np.allclose(R.sum(axis=0), 1.0, atol=1e-12)
+    M = full.read("M")
+    assert M.shape == (1000, 3) and np.all(np.abs(M) <= 1.0 + 1e-12)
+    drive(cpu_driver, ["-i", OIL_IN, "-I", "-r", "ck.10.h5", "-o", "interp.h5"], tmp_path)
+    Mi = H5File(str(tmp_path / "interp.h5")).read("M")
+    assert Mi.shape == (1000, 3) and np.all(np.isfinite(Mi))

