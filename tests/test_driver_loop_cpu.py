@@ -72,6 +72,7 @@ def test_driver_loop_matches_anneal(cpu_driver, tmp_path, pkg, orc, golden, sche
     # one more E-step, in both loops
     assert len(temps) == len(run.temp_trace) >= 150
     assert len(set(temps.tolist())) >= 2  # the run crosses temperatures
+    assert np.ptp(f.read("NFree")) > 1.0  # and the centres leave the trivial solution
     np.testing.assert_allclose(temps, run.temp_trace, rtol=1e-12)
     np.testing.assert_allclose(f.read("LLH"), run.llh_trace, rtol=1e-9)
     np.testing.assert_allclose(f.read("NFree"), run.nfree_trace, rtol=1e-9)
