@@ -142,3 +142,21 @@ def test_driver_checkpoint_restart_and_outputs(cpu_driver, tmp_path, golden):
     drive(cpu_driver, ["-i", OIL_IN, "-I", "-r", "ck.10.h5", "-o", "interp.h5"], tmp_path)
     Mi = H5File(str(tmp_path / "interp.h5")).read("M")
     assert Mi.shape == (1000, 3) and np.all(np.isfinite(Mi))
+
+
+def test_driver_signal_forces_a_checkpoint_and_exit(cpu_driver, tmp_path):
+    """SIGCHLD makes the driver write a checkpoint at the next iteration and
+    exit 0 (dagtm/dagtm.cxx:978, 1609-1687)."""
+    import signal
+    import time
+    p = subprocess.Popen([cpu_driver, "-i", OIL_IN, "-K", "125", "-L", "3", "-M", "8", "-s", "5",
+                          "-e", "0", "-j", "1000000", "-n", "-w", "sig."], cwd=tmp_path,
+                         stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True)
+    time.sleep(2.0)
+    p.send_signal(signal.SIGCHLD)
+    out, err = p.communicate(timeout=120)
+    assert p.returncode == 0, err
+    files = list(tmp_path.glob("sig.*.h5"))
+    assert len(files) == 1
+    n = int(H5File(str(files[0])).read("iter")[0])
+    assert n > 1 and str(files[0]).endswith(f"sig.{n}.h5")
