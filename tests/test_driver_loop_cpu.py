@@ -160,3 +160,25 @@ def test_driver_signal_forces_a_checkpoint_and_exit(cpu_driver, tmp_path):
     assert len(files) == 1
     n = int(H5File(str(files[0])).read("iter")[0])
     assert n > 1 and str(files[0]).endswith(f"sig.{n}.h5")
+
+
+def test_driver_setup_matches_package_setup(cpu_driver, tmp_path, pkg, golden):
+    """The driver's set-up (C++) against the package's (numpy), both restating
+    the reference's (dagtm/dagtm.cxx:1104-1160; comm/comm.c:1118-1185,
+    1401-1448; comm/mpicomm.c:511-559).  A checkpoint at iteration 1 holds the
+    state before the first M-step: the initial centres, beta and the start
+    temperature.  Both solve the least-squares fit of W through the normal
+    equations FI^T FI, whose conditioning on the oil basis bounds the centres'
+    agreement (1e-6); grid, basis, beta and temperature agree to rounding."""
+    st = __import__("importlib").import_module(pkg.__name__ + ".gtm_setup")
+    drive(cpu_driver, ["-i", OIL_IN, "-K", "125", "-L", "3", "-M", "8", "-s", "7", "-a", "0.95",
+                       "-j", "1", "-P", "1", "-w", "init.", "-Q", "cholesky"], tmp_path)
+    f = H5File(str(tmp_path / "init.1.h5"))
+    T = golden["T_in"].astype(np.float64)
+    X, FI, W0, beta0 = st.random_init(T, 3, 125, 8, 2.0, seed=7)
+    assert np.array_equal(f.read("X"), X)
+    np.testing.assert_allclose(f.read("FI"), FI, rtol=0, atol=1e-15)
+    assert float(f.read("beta")[0]) == pytest.approx(beta0, rel=1e-13)
+    assert float(f.read("temp")[0]) == pytest.approx(st.start_temp(T, 0.95), rel=1e-13)
+    Y0 = FI @ W0
+    assert np.max(np.abs(f.read("Y") - Y0)) <= 1e-6 * np.max(np.abs(Y0))
