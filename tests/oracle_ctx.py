@@ -47,7 +47,11 @@ class OracleCtx:
         w = self.R.sum(axis=1) if gg is None else np.asarray(gg)
         c = self.orc.next_ctemp(self.T, self.Y, self.R, w, temp, beta, eps)
         self.calls.append(("ctemp", temp, c, None if gg is None else w.copy()))
-        return (c, np.full(self.K, np.nan)) if per_centre else c
+        if not per_centre:
+            return c
+        ck = np.array([self.orc.next_ctemp(self.T, self.Y[k:k + 1], self.R[k:k + 1], w[k:k + 1],
+                                           temp, beta, eps) for k in range(self.K)])
+        return c, ck
 
     def set_basis(self, T, FI, Y):
         self.calls.append(("basis", FI.shape[0]))

@@ -90,11 +90,21 @@ def test_driver_hda_matches_anneal(cpu_driver, tmp_path, pkg, orc, golden):
     drive(cpu_driver, ["-i", OIL_IN, "-r", "s0.h5", "-o", "s1.h5", "-j", "200", "-n", "-p", "-H",
                        "-Q", "cholesky", "-a", "0.9", "-e", "1e-6"], tmp_path)
     ctx = OracleCtx(orc, T, FI, Y)
+    seen = []
     run = pkg.anneal(ctx, beta, temp, alpha=0.9, eps=1e-6, iter0=it, maxloop=200, hda=True,
-                     T=T, L=3)
+                     T=T, L=3, on_expand=lambda c, info: seen.append(info))
     assert [e[1:] for e in run.expansions] == [(8, 64), (64, 512)]
     f = H5File(str(tmp_path / "s1.h5"))
     assert f.read("Y").shape == (512, 12)
+    # the snapshots written before each expansion (dagtm/dagtm.cxx:1980-2096),
+    # under the index of the temperature trace, against the package loop's
+    for info, tol in zip(seen, (1e-9, 1e-4)):
+        i, K = info["index"], info["K"]
+        assert f.read(f"X.{i}").shape == (K, 3) and f.read(f"M.{i}").shape == (1000, 3)
+        assert f.read(f"FI.{i}").shape == (K, 9) and f.read(f"Y.{i}").shape == (K, 12)
+        np.testing.assert_allclose(f.read(f"W.{i}"), info["W"], rtol=tol, atol=tol)
+        np.testing.assert_allclose(f.read(f"ctemp.{i}"), info["ctemp"], rtol=tol)
+        assert float(f.read(f"beta.{i}")[0]) == pytest.approx(info["beta"], rel=tol)
     np.testing.assert_allclose(f.read("Temp"), run.temp_trace, rtol=1e-12)
     nf = f.read("NFree")
     first = run.expansions[0][0] - it  # trace entries before the first expansion
