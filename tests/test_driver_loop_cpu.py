@@ -164,7 +164,12 @@ def test_driver_signal_forces_a_checkpoint_and_exit(cpu_driver, tmp_path):
                          stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True)
     time.sleep(2.0)
     p.send_signal(signal.SIGCHLD)
-    out, err = p.communicate(timeout=120)
+    try:
+        out, err = p.communicate(timeout=120)
+    except subprocess.TimeoutExpired:
+        p.kill()  # this test's own child
+        p.communicate()
+        raise
     assert p.returncode == 0, err
     files = list(tmp_path.glob("sig.*.h5"))
     assert len(files) == 1
