@@ -49,6 +49,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "EM iters/sec at N=1M,K=8k,D=166: FP64 plain vs BF16x3 form at stated error"
+DTYPES = {
+    "bf16x3": "bf16x3 (split BF16 products, fp32 accumulate; per point the log-sum-exp over "
+              "128-centre chunks in fp32, across chunks in fp64; fp64 M-step and beta)",
+    "fp64": "f64", "fp32": "f32 (fp64 reductions and M-step)"}
 WORKLOAD = dict(N=1_000_000, D=166, K=8000, L=3, M=64, s=2.0, nproto=20, seed=0)
 
 
@@ -63,8 +67,8 @@ def parse():
     ap.add_argument("--fp64-steps", type=int, default=2,
                     help="timed EM iterations of the FP64 form beside the headline (0: skip)")
     ap.add_argument("--e2e-steps", type=int, default=20)
-    ap.add_argument("--cpu-sample", type=int, default=1024,
-                    help="points in the bounded CPU-baseline sample")
+    ap.add_argument("--ref-sample", type=int, default=8192,
+                    help="points per step of the reference arm's bounded sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--anneal", action="store_true",
                     help="time a whole annealing run instead of single iterations")
@@ -202,13 +206,34 @@ def time_steps(torch, ctx, n, beta, temp, stream):
     return ev0.elapsed_time(ev1), beta
 
 
+R_COLS = (0, 499_776, 999_744)  # three 256-point blocks of sampled responsibilities
+
+
+def probe_step(ctx, beta, temp):
+    """One EM iteration from the loaded centres that also keeps what the error
+    report compares: qualities, R on three 256-point blocks, G, RT, beta, Y."""
+    llh, nfree = ctx.estep(beta, 1, temp)
+    cols = [min(c, max(0, ctx.N - 256)) for c in R_COLS]
+    R = [ctx.R_block(0, ctx.K, c, min(256, ctx.N)) for c in cols]
+    b, _, Y = ctx.mstep(want_W=False, want_Y=True)
+    G, RT = ctx.get_stats()
+    return dict(llh=llh, nfree=nfree, R=R, beta=b, Y=Y, G=G, RT=RT)
+
+
 def run_form(torch, pkg, form, T, FI, Y0, beta0, temp0, steps, warmup, rank, world, stream_cls,
-             clocks=False):
+             clocks=False, probe=False):
+    """Warm-up, then `steps` timed EM iterations.  With probe, the first warm-up
+    iteration is probe_step (it starts from Y0, beta0) and its record is returned."""
     ctx = pkg.Context(T, FI, form)
     ctx.set_Y(Y0)
     stream = stream_cls(ctx.stream())
     beta = beta0
-    for _ in range(warmup):
+    rec = None
+    for i in range(warmup):
+        if probe and i == 0:
+            rec = probe_step(ctx, beta, temp0)
+            beta = rec["beta"]
+            continue
         ctx.estep(beta, 1, temp0)
         beta, _, _ = ctx.mstep(want_W=False)
     ctx.set_timing(True)
@@ -224,7 +249,38 @@ def run_form(torch, pkg, form, T, FI, Y0, beta0, temp0, steps, warmup, rank, wor
     ms = max_over_ranks(ms, world)
     phases = ctx.timing()
     ctx.set_timing(False)
-    return ctx, ms, phases, (sampler.summary() if sampler else None), beta
+    return ctx, ms, phases, (sampler.summary() if sampler else None), beta, rec
+
+
+def rel_err(a, b):
+    a, b = np.asarray(a, float), np.asarray(b, float)
+    return float(np.max(np.abs(a - b)) / max(float(np.max(np.abs(b))), 1e-300))
+
+
+def form_errors(split, ref, N, D, sum_t2):
+    """The split form's first EM iteration against the FP64 form's, from the
+    same centres, beta and temperature."""
+    def beta_from(G, RT, Y):
+        return N * D / (float((G * (Y * Y).sum(axis=1)).sum()) - 2.0 * float((Y * RT).sum())
+                        + sum_t2)
+    b_stats = beta_from(split["G"], split["RT"], ref["Y"])
+    return {
+        "beta_stats_rel": abs(b_stats / ref["beta"] - 1.0),
+        "F_rel": abs(split["nfree"] - ref["nfree"]) / abs(ref["nfree"]),
+        "llh_rel": abs(split["llh"] - ref["llh"]) / abs(ref["llh"]),
+        "beta_rel": abs(split["beta"] - ref["beta"]) / abs(ref["beta"]),
+        "R_max_abs": max(float(np.max(np.abs(a - b))) for a, b in zip(split["R"], ref["R"])),
+        "G_rel": rel_err(split["G"], ref["G"]),
+        "RT_rel": rel_err(split["RT"], ref["RT"]),
+        "Y_rel": rel_err(split["Y"], ref["Y"]),
+        "what": "first EM iteration of each form from the same Y, beta, temp: F = N nfree "
+                "(the annealed free energy), llh, the new beta, R on three 256-point blocks "
+                f"(points 0, mid, end of {N}), G, RT and the new Y (max-abs / max).  At this "
+                "width A = FI^T G FI is numerically singular, pivots are dropped and W, Y are "
+                "not determined by the data (any two solvers differ); beta_stats_rel is the "
+                "determined part: beta from the split form's G and RT with the FP64 form's "
+                "new centres, against the FP64 form's beta",
+    }
 
 
 def e2e_steps(torch, pkg, ctx, steps, beta, temp, stream_cls):
@@ -258,37 +314,95 @@ def e2e_steps(torch, pkg, ctx, steps, beta, temp, stream_cls):
     return ms, h2d, d2h
 
 
-def algorithmic_flops(form, phase, N, K, D):
-    """Tensor-core / FMA work the algorithm needs per launch (unpadded shapes)."""
+def bf16_exact(T):
+    """Whether every value of T is exactly a BF16 number (the split form then
+    keeps T in one piece)."""
+    t32 = T.astype(np.float32)
+    return bool(np.array_equal(t32.astype(np.float64), T)
+                and not np.any(t32.view(np.uint32) & np.uint32(0xFFFF)))
+
+
+def canonical_flops(phase, N, K, D):
+    """The kernel's share of the canonical work of one EM iteration: the
+    distance product 2KND for the E-step and the R T product 2KND for the
+    responsibility pass (its distance recompute is not counted)."""
+    return 2.0 * K * N * D if phase in ("estep", "mstep_pass") else None
+
+
+def issued_flops(form, phase, nT, N, K, D):
+    """Products the kernel issues on unpadded shapes: the split form's E-step
+    runs Y_hi T and Y_lo T (plus Y_hi T_lo when T is split); its
+    responsibility pass recomputes those and runs R_hi T, R_lo T (and R_hi T_lo)."""
     kdn = 2.0 * K * N * D
+    per = (1 + nT) if form == "bf16x3" else 1
     if phase == "estep":
-        return (2 if form == "bf16x3" else 1) * kdn
+        return per * kdn
     if phase == "mstep_pass":
-        return (4 if form == "bf16x3" else 2) * kdn
+        return 2 * per * kdn
     return None
 
 
-def cpu_baseline(T, FI, Y0, beta0, temp0, sample, N_full):
-    from oracle import oracle as O  # the checker: CPU restatement of the reference
-    O.build()
-    threads = os.cpu_count() or 1
-    O.set_threads(threads)
-    ws = O.Workspace(T[:sample], FI, Y0, beta0)
-    ws.iteration(1, temp0)  # warm-up
+def canonical_step_flops(N, K, D, M1):
+    """Canonical work of one EM iteration: distances, the cheaper route to B,
+    A and Y = FI W."""
+    return (2.0 * K * N * D + min(2.0 * M1 * K * N + 2.0 * M1 * N * D,
+                                  2.0 * K * N * D + 2.0 * K * M1 * D)
+            + 2.0 * K * M1 * M1 + 2.0 * K * M1 * D)
+
+
+def _time_iters(ws, iters, temp, budget_s, **kw):
+    ws.iteration(1, temp, **kw)  # warm-up
     times = []
-    t_end = time.perf_counter() + 20.0
+    t_end = time.perf_counter() + budget_s
     while True:
         t0 = time.perf_counter()
-        ws.iteration(1, temp0)
+        ws.iteration(1, temp, **kw)
         times.append(time.perf_counter() - t0)
-        if len(times) >= 3 or time.perf_counter() > t_end:
+        if len(times) >= iters or time.perf_counter() > t_end:
             break
-    t = statistics.median(times)
-    return {"value": (1.0 / t) * (sample / N_full), "unit": "EM iters/s", "cores": threads,
-            "kind": "port",
-            "sample": f"{sample} of the {N_full} points (K, D, M unchanged), {len(times)} timed "
-                      f"iterations of the reference-semantics CPU restatement (dense K x N "
-                      f"matrices), scaled linearly in N; median {t:.3f} s per iteration"}
+    return statistics.median(times), len(times)
+
+
+def cpu_variants(T, FI, Y0, beta0, temp0, N_full, samples=(256, 1024, 8192), budget_s=10.0):
+    """The reference's EM iteration on the host cores, on the first points of
+    the same data and from the same initial state, in three variants:
+    faithful (the C restatement, one thread: the reference as built by default
+    against GSL's reference cblas, one MPI rank), port_omp (the same code with
+    OpenMP on every core), blas (numpy/OpenBLAS dgemm, element loops split
+    over every core).  Work is linear in N, so each rate is scaled from its
+    sample to N_full: these are extrapolations."""
+    from oracle import oracle as O  # the checker: CPU restatement of the reference
+    from oracle import oracle_blas as OB
+    O.build()
+    threads = os.cpu_count() or 1
+    out = {}
+    n_f, n_o, n_b = (min(s, T.shape[0]) for s in samples)
+    O.set_threads(1)
+    t, it = _time_iters(O.Workspace(T[:n_f], FI, Y0, beta0), 1, temp0, budget_s)
+    out["faithful"] = {"value": (1.0 / t) * (n_f / N_full), "cores": 1, "sample_points": n_f,
+                       "iters": it, "s_per_iter": t}
+    O.set_threads(threads)
+    t, it = _time_iters(O.Workspace(T[:n_o], FI, Y0, beta0), 2, temp0, budget_s)
+    out["port_omp"] = {"value": (1.0 / t) * (n_o / N_full), "cores": threads,
+                       "sample_points": n_o, "iters": it, "s_per_iter": t}
+    ws = OB.Workspace(T[:n_b], FI, Y0, beta0, threads=threads)
+    t, it = _time_iters(ws, 2, temp0, budget_s)
+    ws.close()
+    out["blas"] = {"value": (1.0 / t) * (n_b / N_full), "cores": threads, "sample_points": n_b,
+                   "iters": it, "s_per_iter": t}
+    return out
+
+
+def cpu_baseline(T, FI, Y0, beta0, temp0, N_full):
+    v = cpu_variants(T, FI, Y0, beta0, temp0, N_full)
+    best = max(v, key=lambda k: v[k]["value"])
+    b = v[best]
+    return {"value": b["value"], "unit": "EM iters/s", "cores": b["cores"], "kind": "port",
+            "extrapolated": True, "variant": best, "variants": v,
+            "sample": f"first {b['sample_points']} of the {N_full} points (K, D, M and the "
+                      f"initial state unchanged), {b['iters']} timed iterations of the "
+                      f"reference-semantics CPU restatement ({best}), scaled linearly in N; "
+                      f"median {b['s_per_iter']:.3f} s per iteration"}
 
 
 def main_gb300(args):
@@ -302,59 +416,79 @@ def main_gb300(args):
     stream_cls = torch.cuda.ExternalStream
     T, X, FI, Y0, beta0, temp0 = make_problem(args.n)
     N, D = T.shape
-    K = FI.shape[0]
+    K, M1 = FI.shape
     form = args.form
-    ctx, ms, phases, clocks, beta = run_form(torch, pkg, form, T, FI, Y0, beta0, temp0,
-                                             args.steps, args.warmup, rank, world, stream_cls,
-                                             clocks=(rank == 0))
+    want_err = rank == 0 and form != "fp64" and args.fp64_steps > 0
+    ctx, ms, phases, clocks, beta, rec = run_form(
+        torch, pkg, form, T, FI, Y0, beta0, temp0, args.steps, max(args.warmup, 1), rank, world,
+        stream_cls, clocks=(rank == 0), probe=want_err)
     ms_step = ms / args.steps
     value = whole_job_rate(args.steps, ms, world)
     launches = sum(p["launches"] for p in phases.values())
     e2e_ms, h2d, d2h = e2e_steps(torch, pkg, ctx, max(1, args.e2e_steps), beta, temp0, stream_cls)
     e2e_ms = max_over_ranks(e2e_ms, world)
     e2e_value = whole_job_rate(max(1, args.e2e_steps), e2e_ms, world)
+    nT = 1 if bf16_exact(T) else 2
     ctx.close()
 
     peaks, peak_src = measured_peaks()
     dom = max(("estep", "mstep_pass"), key=lambda p: phases[p]["ms"])
     per_launch_ms = phases[dom]["ms"] / max(1, phases[dom]["calls"])
-    flops = algorithmic_flops(form, dom, N, K, D)
+    canon = canonical_flops(dom, N, K, D)
+    issued = issued_flops(form, dom, nT, N, K, D)
+    achieved = canon / (per_launch_ms / 1000.0) / 1e12
+    burst = peaks.get("bf16_tflops", 1900.0)
+    sustained = peaks.get("bf16_tflops_sustained", burst)
     if form == "bf16x3":
-        peak = peaks.get("bf16_tflops_sustained", peaks.get("bf16_tflops"))
-        peak_note = f"bf16 dense, sustained ({peak_src})"
+        peak = burst / 3.0
+        peak_note = (f"bf16 dense burst ({peak_src}) / 3: three BF16 products stand for one "
+                     "canonical FP32-accurate product")
+        tensor_util = issued / (per_launch_ms / 1000.0) / 1e12 / burst
     else:
         peak = 1.25 if form == "fp64" else 75.0
         peak_note = f"{form} nominal (no measured {form} peak)"
-    achieved = flops / (per_launch_ms / 1000.0) / 1e12
+        tensor_util = None
     traffic = traffic_summary().get(f"{form}:{dom}")
     traffic_note = None
     if traffic is not None:
         traffic = traffic.get("bytes_per_point", 0.0) * N
-        traffic_note = "ncu dram__bytes_read.sum + dram__bytes_write.sum per point (profiles/traffic.json), x N"
+        traffic_note = ("ncu dram__bytes_read.sum + dram__bytes_write.sum per point "
+                        "(profiles/traffic.json), x N")
+    step_flops = canonical_step_flops(N, K, D, M1)
     roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": achieved / peak, "traffic": traffic, "kernel": dom,
-                "per_launch_ms": per_launch_ms, "peak_source": peak_note,
-                "frac_of_burst_peak": achieved / peaks.get("bf16_tflops", peak) if form == "bf16x3" else None,
+                "per_launch_ms": per_launch_ms, "canonical_flop_per_launch": canon,
+                "peak_source": peak_note,
+                "frac_of_sustained": (achieved / (sustained / 3.0)) if form == "bf16x3" else None,
+                "tensor_util": tensor_util,
+                "tensor_util_what": "products the kernel issues (unpadded) / launch time / "
+                                    "bf16 dense burst peak",
+                "step": {"canonical_flop": step_flops,
+                         "achieved": step_flops / (ms_step / 1000.0) / 1e12,
+                         "frac": step_flops / (ms_step / 1000.0) / 1e12 / peak},
                 "traffic_source": traffic_note}
 
     fp64 = None
+    errors = None
     if args.fp64_steps > 0 and form != "fp64":
-        c64, ms64, ph64, _, _ = run_form(torch, pkg, "fp64", T, FI, Y0, beta0, temp0,
-                                         args.fp64_steps, 1, rank, world, stream_cls)
+        c64, ms64, ph64, _, _, rec64 = run_form(torch, pkg, "fp64", T, FI, Y0, beta0, temp0,
+                                                args.fp64_steps, 1, rank, world, stream_cls,
+                                                probe=want_err)
         c64.close()
         fp64 = {"value": world * args.fp64_steps / (ms64 / 1000.0), "unit": "EM iters/s",
                 "ms_per_step": ms64 / args.fp64_steps, "steps": args.fp64_steps}
+        if want_err:
+            errors = form_errors(rec, rec64, N, D, float((T * T).sum()))
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(T, FI, Y0, beta0, temp0, min(args.cpu_sample, N), N)
+        cpu = cpu_baseline(T, FI, Y0, beta0, temp0, N)
 
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "EM iters/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": {"bf16x3": "bf16x3 (fp32 accumulate, fp64 reductions)", "fp64": "f64",
-                      "fp32": "f32"}[form],
+            "dtype": DTYPES[form],
             "data": "synthetic (seeded binary fingerprints, stand-in for the 166-bit "
                     "chemical-fingerprint data set)",
             "config": {"workload": f"DA-GTM EM iteration, N={N}, D={D}, K={K} (20^3), "
@@ -369,6 +503,7 @@ def main_gb300(args):
             "roofline": roofline,
             "phases_ms_per_step": {p: v["ms"] / args.steps for p, v in phases.items()},
             "fp64_form": fp64,
+            "errors_vs_fp64_form": errors,
             "cpu_baseline": cpu,
         }
         print(json.dumps(line), flush=True)
@@ -434,35 +569,43 @@ def main_ctemp(args):
 
 
 def main_reference(args):
+    """The reference's CPU path (restated: the reference itself needs MPI, GSL
+    and HDF5) on the host cores, from the same data and initial state as the
+    GPU arm; each step is one EM iteration on the first points of the data,
+    scaled linearly to N (an extrapolation, flagged as such)."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    from oracle import oracle as O
-    O.build()
+    from oracle import oracle_blas as OB
+    T, X, FI, Y0, beta0, temp0 = make_problem(args.n)
+    N_full = T.shape[0]
+    n_sample = min(args.ref_sample, N_full)
     threads = os.cpu_count() or 1
-    O.set_threads(threads)
-    n_sample = args.cpu_sample
-    T, X, FI, Y0, beta0, temp0 = make_problem(n_sample)
-    N_full = args.n
-    ws = O.Workspace(T, FI, Y0, beta0)
+    ws = OB.Workspace(T[:n_sample], FI, Y0, beta0, threads=threads)
     for _ in range(args.warmup):
         ws.iteration(1, temp0)
     t0 = time.perf_counter()
     for _ in range(args.steps):
         ws.iteration(1, temp0)
     dt = (time.perf_counter() - t0) / args.steps
+    ws.close()
     value = (1.0 / dt) * (n_sample / N_full)
-    sample = (f"{n_sample} of the {N_full} points per step (K, D, M unchanged), reference-"
-              f"semantics CPU restatement with dense K x N matrices, scaled linearly in N")
+    variants = cpu_variants(T, FI, Y0, beta0, temp0, N_full, budget_s=5.0)
+    sample = (f"first {n_sample} of the {N_full} points per step (K, D, M and the initial "
+              f"state unchanged), numpy/OpenBLAS restatement of the reference's iteration on "
+              f"{threads} threads, {dt:.3f} s per step, scaled linearly in N")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "EM iters/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": dt * 1000.0 * (N_full / n_sample), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded binary fingerprints)",
-            "config": {"workload": f"DA-GTM EM iteration, N={N_full}, D=166, K=8000, M=64 + bias",
+            "extrapolated": True, "sample_points": n_sample,
+            "config": {"workload": f"DA-GTM EM iteration, N={N_full}, D=166, K=8000 (20^3), "
+                                   "M=64 (4^3) + bias, reference CPU path (restated)",
                        "N": N_full, "D": 166, "K": 8000, "M": 64, "L": 3},
             "cpu_baseline": {"value": value, "unit": "EM iters/s", "cores": threads,
-                             "kind": "port", "sample": sample},
+                             "kind": "port", "extrapolated": True, "sample": sample,
+                             "variants": variants},
             "e2e": {"value": value, "unit": "EM iters/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)

@@ -139,6 +139,17 @@ int grid_rows(int rows)
     return b > 4864 ? 4864 : (b < 1 ? 1 : b);
 }
 
+}  // namespace
+
+int launch_norms_f32(const float *X, int rows, int D, double *out, cudaStream_t s)
+{
+    norms_f32_kernel<<<grid_rows(rows), 256, 0, s>>>(X, rows, D, out);
+    DGTM_CUDA_TRY(cudaGetLastError());
+    return DGTM_OK;
+}
+
+namespace {
+
 int check_args(const float *Y, const float *T, int N, int K, int D, double beta, double temp,
                void *ws, size_t ws_bytes, size_t need)
 {

@@ -7,10 +7,13 @@
 // call CUDA at all; a process whose device memory is entirely handed out by
 // another allocator, so a fresh cudaMalloc would fail or break its budget; a
 // latency-critical loop that cannot afford the implicit synchronisation of an
-// allocation).  dgtm_fe_forward_noalloc serves them: it runs the same
-// kernels, with its scratch in one fixed array of DGTM_FE_NOALLOC_BYTES
-// compiled into this library.  Every GPU that loads the library holds that
-// array until the process exits.  No call allocates anything.
+// allocation).  dgtm_fe_forward_noalloc serves them: it runs the FP32
+// CUDA-core kernels of the FP32 form (the FP32 E-step and its reductions),
+// with its scratch in one fixed array of DGTM_FE_NOALLOC_BYTES compiled into
+// this library.  Every GPU that loads the library holds that array until the
+// process exits.  No call allocates anything itself; the first call on a
+// device may be the moment the driver loads this library's device code (and
+// with it the array), under CUDA's lazy module loading.
 #include "common.cuh"
 #include "kernels.cuh"
 
@@ -28,10 +31,48 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[DGTM_FE_NOALLOC
 
 constexpr int kMaxDevices = 64;
 std::mutex g_scratch_mu;
-void *g_scratch_addr[kMaxDevices];  // device address of the array, per device
 
-// Looks the array's device address up once per device, with that device
-// current; later calls reuse it.
+// The array's device address per device, with the ID of the CUDA context it
+// was looked up in.  A context that is torn down and created again (after a
+// cudaDeviceReset, say) reloads this library's device code, and the array may
+// then sit elsewhere: a new context ID triggers a new lookup.
+struct ScratchAddr {
+    unsigned long long ctx_id;
+    void *addr;
+};
+ScratchAddr g_scratch[kMaxDevices];
+
+typedef int (*PfnCtxGetCurrent)(void **ctx);
+typedef int (*PfnCtxGetId)(void *ctx, unsigned long long *id);
+
+// ID of the calling thread's current CUDA context (driver entry points looked
+// up through the runtime, so the library does not link the driver library).
+// Returns false when the thread has no current context yet.
+bool current_context_id(unsigned long long *id)
+{
+    static PfnCtxGetCurrent get_current = nullptr;
+    static PfnCtxGetId get_id = nullptr;
+    if (!get_current || !get_id) {
+        void *p1 = nullptr, *p2 = nullptr;
+        cudaDriverEntryPointQueryResult q1, q2;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p1, 12000, cudaEnableDefault,
+                                             &q1) != cudaSuccess ||
+            q1 != cudaDriverEntryPointSuccess ||
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &p2, 12000, cudaEnableDefault, &q2) !=
+                cudaSuccess ||
+            q2 != cudaDriverEntryPointSuccess)
+            return false;
+        get_current = (PfnCtxGetCurrent) p1;
+        get_id = (PfnCtxGetId) p2;
+    }
+    void *ctx = nullptr;
+    return get_current(&ctx) == 0 && ctx && get_id(ctx, id) == 0;
+}
+
+// Set-up, once per device and context: with that device current, look up the
+// array's device address (cudaGetSymbolAddress).  The first lookup in a
+// process may make the driver load this library's device code, which is
+// when the array is reserved on that device; later calls reuse the address.
 int scratch_on_current_device(void **out)
 {
     int dev = 0;
@@ -41,8 +82,12 @@ int scratch_on_current_device(void **out)
                   kMaxDevices);
         return DGTM_ENOTSUP;
     }
+    // a thread that has not used the runtime yet has no current context:
+    // the lookup below binds the device's primary context, then it is named
+    unsigned long long id = 0;
+    bool have_id = current_context_id(&id);
     std::lock_guard<std::mutex> lock(g_scratch_mu);
-    if (!g_scratch_addr[dev]) {
+    if (!have_id || !g_scratch[dev].addr || g_scratch[dev].ctx_id != id) {
         void *p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess || !p) {
@@ -50,9 +95,13 @@ int scratch_on_current_device(void **out)
                       cudaGetErrorString(e));
             return DGTM_ECUDA;
         }
-        g_scratch_addr[dev] = p;
+        if (!have_id && !current_context_id(&id)) {
+            set_error(DGTM_ECUDA, "no current CUDA context for the no-alloc scratch");
+            return DGTM_ECUDA;
+        }
+        g_scratch[dev] = ScratchAddr{id, p};
     }
-    *out = g_scratch_addr[dev];
+    *out = g_scratch[dev].addr;
     return DGTM_OK;
 }
 
@@ -84,34 +133,10 @@ NoAllocLayout layout(int N, int K)
     return L;
 }
 
-__global__ void noalloc_norms_kernel(const float *__restrict__ X, int rows, int D,
-                                     double *__restrict__ out)
-{
-    const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
-    for (int r = blockIdx.x * wpb + (threadIdx.x >> 5); r < rows; r += gridDim.x * wpb) {
-        double s = 0.0;
-        for (int d = lane; d < D; d += 32) {
-            const double v = (double) X[(size_t) r * D + d];
-            s += v * v;
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1)
-            s += __shfl_xor_sync(0xffffffffu, s, o);
-        if (lane == 0)
-            out[r] = s;
-    }
-}
-
 __global__ void noalloc_value_kernel(const double *__restrict__ S, double base, double temp,
                                      double *__restrict__ F)
 {
     F[0] = base + temp * S[1];
-}
-
-int rows_grid(int rows)
-{
-    int b = (rows + 7) / 8;
-    return b > 4864 ? 4864 : (b < 1 ? 1 : b);
 }
 
 }  // namespace
@@ -153,9 +178,9 @@ extern "C" int dgtm_fe_forward_noalloc(const float *Y, const float *T, int N, in
     double *part = reinterpret_cast<double *>(ws + L.part);
     double *S = reinterpret_cast<double *>(ws + L.scal);
     cudaStream_t s = (cudaStream_t) stream;
-    noalloc_norms_kernel<<<rows_grid(N), 256, 0, s>>>(T, N, D, tt);
-    noalloc_norms_kernel<<<rows_grid(K), 256, 0, s>>>(Y, K, D, yy);
-    DGTM_CUDA_TRY(cudaGetLastError());
+    if ((r = launch_norms_f32(T, N, D, tt, s)) != DGTM_OK ||
+        (r = launch_norms_f32(Y, K, D, yy, s)) != DGTM_OK)
+        return r;
     Pass1Args<float> a{T, Y, tt, yy, N, D, K, beta / 2.0, beta / (2.0 * temp), 1, colstat, part};
     if ((r = launch_pass1_simt<float>(a, s)) != DGTM_OK)
         return r;

@@ -98,6 +98,8 @@ int launch_ctemp_batch(const CtempPlan &pl, const double *T64, const float *T32,
                        void *scratch, double *gsum_dev, double *out_dev, cudaStream_t s);
 // yy = |y|^2 for a given Y.
 int launch_norms(const double *X, int rows, int D, double *out, cudaStream_t s);
+// out[r] = |x_r|^2 in FP64 for an FP32 row-major matrix (rows x D).
+int launch_norms_f32(const float *X, int rows, int D, double *out, cudaStream_t s);
 // out[0] = sum_i v[i] (fixed order) + add; out[1] = num / out[0].
 int launch_sum_ratio(const double *v, int n, double add, double num, double *out,
                      cudaStream_t s);

@@ -211,17 +211,22 @@ int dgtm_fe_backward(const float *Y, const float *T, int N, int K, int D, double
  * even a workspace: code running where cudaMalloc is forbidden or unwanted (a
  * host callback; a process whose device memory is all handed out by another
  * allocator; a latency-critical loop that cannot pay for the synchronisation
- * an allocation implies).  It runs the same kernels as dgtm_fe_forward and
- * writes F (one device double) the same way, but keeps its scratch in a
- * fixed array of DGTM_FE_NOALLOC_BYTES inside this library, which every GPU
- * that loads the library holds until the process exits.  It calls no
- * allocator.  Limits and rules:
+ * an allocation implies).  It computes the same F with the FP32 CUDA-core
+ * kernels of the FP32 form and writes it (one device double) the same way,
+ * but keeps its scratch in a fixed array of DGTM_FE_NOALLOC_BYTES inside this
+ * library, which every GPU that loads the library holds until the process
+ * exits.  It calls no allocator.  Limits and rules:
  *   - the scratch needs about 24 N + 8 K bytes (plus alignment); problems
  *     that need more than DGTM_FE_NOALLOC_BYTES are rejected with
  *     DGTM_EINVAL and a message giving the bytes needed;
- *   - the first call on each device looks up the array's device address
- *     (cudaGetSymbolAddress) with that device current: make that first call
- *     before any stream capture;
+ *   - set-up happens in the first call on each device (and again in the first
+ *     call after that device's context was destroyed and recreated, e.g. by
+ *     cudaDeviceReset): with the device current it looks up the array's
+ *     device address (cudaGetSymbolAddress).  Under CUDA's lazy module loading
+ *     that lookup is what makes the driver load this library's device code,
+ *     so the array is reserved on the device at that moment and not before.
+ *     Make that first call before any stream capture; from the second call on
+ *     nothing is loaded or reserved;
  *   - all calls share the one array, so calls that may overlap on the GPU
  *     (other streams, other host threads) race with each other: serialise
  *     them; nothing in the array needs to start at zero.

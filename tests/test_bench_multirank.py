@@ -69,15 +69,17 @@ def test_reference_arm_other_ranks_exit_quietly():
 
 
 def test_reference_arm_prints_the_contract_line():
-    """Rank 0 of the reference arm times the oracle on a small sample of the
-    workload and prints one JSON line with the metric, unit and config of the
-    GPU arm, its cpu_baseline and a zero-copy e2e."""
+    """Rank 0 of the reference arm times the CPU restatement on a small sample
+    of the workload (the first points of the same data, the same initial
+    state) and prints one JSON line with the metric, unit and config of the
+    GPU arm, its cpu_baseline (flagged as extrapolated, with the three CPU
+    variants) and a zero-copy e2e."""
     import json
     sys.path.insert(0, ROOT)
     import bench
     env = {k: v for k, v in os.environ.items() if k not in ("RANK", "WORLD_SIZE", "LOCAL_RANK")}
     r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference",
-                        "--steps", "1", "--warmup", "0", "--cpu-sample", "64"], env=env,
+                        "--steps", "1", "--warmup", "0", "--ref-sample", "64"], env=env,
                        capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr
     lines = [ln for ln in r.stdout.splitlines() if ln.strip()]
@@ -88,5 +90,8 @@ def test_reference_arm_prints_the_contract_line():
     assert d["config"]["N"] == 1_000_000 and d["config"]["K"] == 8000 and d["config"]["D"] == 166
     cb = d["cpu_baseline"]
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"]
+    assert d["extrapolated"] is True and cb["extrapolated"] is True and d["sample_points"] == 64
+    assert set(cb["variants"]) == {"faithful", "port_omp", "blas"}
+    assert cb["variants"]["faithful"]["cores"] == 1
     assert d["e2e"] == {"value": d["value"], "unit": "EM iters/s", "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}

@@ -3,10 +3,12 @@
 It exists for callers that cannot allocate device memory at all -- code that
 runs where cudaMalloc is forbidden or too costly, or whose device memory is
 owned by another allocator.  Through the C ABI it must give the same F as
-dgtm_fe_forward (which takes a caller workspace), on two calls in a row with
-different problems, allocate no device memory after its first call on the
-device, and refuse a problem too large for its fixed scratch array with a
-clear error.  This file is collected last on purpose.
+dgtm_fe_forward (which takes a caller workspace) and as the oracle, on two
+calls in a row with different problems, allocate no device memory once its
+first call on the device has run (that call may be the one that makes the
+driver load the library's device code, array included), and refuse a
+problem too large for its fixed scratch array with a clear error.  This file
+is collected last on purpose.
 """
 import ctypes
 
@@ -51,11 +53,23 @@ def problem(seed, N, K, D):
             torch.tensor(T, device="cuda").contiguous())
 
 
-def test_noalloc_forward_matches_the_workspace_forward(pkg):
+def oracle_F(orc, Y, T, beta, temp):
+    """F = N nfree of the reference's DA quality (FP64, on the FP32 inputs)."""
+    Yh = Y.double().cpu().numpy()
+    Th = T.double().cpu().numpy()
+    N, D = Th.shape
+    K = Yh.shape[0]
+    _, _, vgc2 = orc.resp(orc.dist(Yh, Th), beta, 1, temp)
+    return N * orc.qual(N, K, D, beta, vgc2, 1, temp)
+
+
+def test_noalloc_forward_matches_the_workspace_forward(pkg, orc):
     lib = pkg.load_library()
     stream = torch.cuda.current_stream().cuda_stream
     # two calls in a row; the second, smaller problem reuses the array the
-    # first one filled
+    # first one filled.  The first call on the device may load the library's
+    # device code (and with it the array), so the second is the one whose
+    # memory is watched: free device memory and torch's own counters.
     cases = [(11, 4096, 256, 16, 5.0, 1.7), (12, 1000, 100, 12, 9.0, 1.0)]
     for i, (seed, N, K, D, beta, temp) in enumerate(cases):
         Y, T = problem(seed, N, K, D)
@@ -64,11 +78,17 @@ def test_noalloc_forward_matches_the_workspace_forward(pkg):
         torch.cuda.synchronize()
         if i == 1:
             free_before = torch.cuda.mem_get_info()[0]
+            alloc_before = torch.cuda.memory_allocated()
+            reserved_before = torch.cuda.memory_reserved()
         F = forward_noalloc(lib, Y, T, beta, temp, stream, F_out)
         if i == 1:
+            assert torch.cuda.memory_allocated() == alloc_before
+            assert torch.cuda.memory_reserved() == reserved_before
             assert torch.cuda.mem_get_info()[0] == free_before
         assert np.isfinite(F)
-        assert F == pytest.approx(F_ref, rel=1e-12, abs=1e-9)
+        # the free-energy tests' tolerance on F
+        assert F == pytest.approx(F_ref, rel=1e-5)
+        assert F == pytest.approx(oracle_F(orc, Y, T, beta, temp), rel=1e-5)
 
 
 def test_noalloc_forward_rejects_problems_beyond_its_scratch(pkg):
