@@ -30,6 +30,16 @@ thousands of iterations (an uncapped run did not finish in 15 minutes).
 ``--ctemp`` is another separate measurement: the wall time of the AUTO
 schedule's critical-temperature call (dgtm_next_ctemp) on the workload, after
 one E-step at the start temperature.
+
+``--fe`` times the differentiation configuration: the annealed free energy
+and its gradient (dgtm_fe_forward + dgtm_fe_backward for dY, dT and dbeta)
+at N = 65,536 points in D = 64 (16-component mixture, sd 0.2), K = 4096,
+FP32 data, L2 flushed between steps.
+
+``--large`` times the large split-precision configuration: EM iterations at
+N = 4,000,000 binary vectors (50 prototypes), K = 32,768 (32^3), M = 512
+(8^3) + bias, then the gradient projection of 1,000,000 held-out points onto
+the fixed map (gradient steps on F through dgtm_fe_backward's dT).
 """
 from __future__ import annotations
 
@@ -77,6 +87,12 @@ def parse():
     ap.add_argument("--ctemp", action="store_true",
                     help="time the AUTO schedule's critical-temperature call instead")
     ap.add_argument("--ctemp-calls", type=int, default=1)
+    ap.add_argument("--fe", action="store_true",
+                    help="time the free energy's forward + backward (differentiation config)")
+    ap.add_argument("--large", action="store_true",
+                    help="time the large split-precision configuration and the projection")
+    ap.add_argument("--proj-steps", type=int, default=20,
+                    help="gradient steps of the projection in --large")
     return ap.parse_args()
 
 
@@ -568,6 +584,175 @@ def main_ctemp(args):
                    "N": args.n, "D": w["D"], "K": w["K"]}}), flush=True)
 
 
+class L2Flush:
+    """Writes a buffer larger than L2 (129 MB) between timed steps."""
+
+    def __init__(self, torch, mb=512):
+        self.buf = torch.empty(mb << 18, dtype=torch.float32, device="cuda")
+
+    def __call__(self):
+        self.buf.fill_(1.0)
+
+
+def fe_buffers(torch, pkg, N, K, D):
+    import ctypes
+    lib = pkg.load_library()
+    size = ctypes.c_size_t()
+    pkg._check(lib.dgtm_fe_workspace_size(N, K, D, ctypes.byref(size)))
+    ws = torch.empty(size.value + 256, dtype=torch.uint8, device="cuda")
+    return lib, ws, ws.data_ptr() + ((-ws.data_ptr()) % 256), size.value
+
+
+def main_fe(args):
+    """Forward + backward of the annealed free energy at the differentiation
+    configuration, through the C ABI on torch's stream."""
+    import torch
+    pkg = importlib.import_module("da-gtm_gb300")
+    ds = importlib.import_module("da-gtm_gb300.datasets")
+    N, D, K = 65536, 64, 4096
+    beta, temp = 4.0, 2.0
+    Th = ds.gaussian_mixture(N, D, 16, 0.2, seed=0).astype(np.float32)
+    rng = np.random.default_rng(0)
+    Yh = (Th[rng.integers(0, N, K)] + 0.05 * rng.standard_normal((K, D))).astype(np.float32)
+    T = torch.tensor(Th, device="cuda")
+    Y = torch.tensor(Yh, device="cuda")
+    lib, ws, wp, wsz = fe_buffers(torch, pkg, N, K, D)
+    F = torch.empty((), dtype=torch.float64, device="cuda")
+    g = torch.ones((), dtype=torch.float64, device="cuda")
+    dY = torch.empty_like(Y)
+    dT = torch.empty_like(T)
+    db = torch.empty((), dtype=torch.float64, device="cuda")
+    st = torch.cuda.current_stream().cuda_stream
+    flush = L2Flush(torch)
+
+    def fwd():
+        pkg._check(lib.dgtm_fe_forward(Y.data_ptr(), T.data_ptr(), N, K, D, beta, temp, wp, wsz,
+                                       st, F.data_ptr()))
+
+    def bwd():
+        pkg._check(lib.dgtm_fe_backward(Y.data_ptr(), T.data_ptr(), N, K, D, beta, temp, wp, wsz,
+                                        st, g.data_ptr(), dY.data_ptr(), dT.data_ptr(),
+                                        db.data_ptr()))
+
+    for _ in range(max(3, args.warmup)):
+        fwd()
+        bwd()
+    torch.cuda.synchronize()
+    t_f, t_b = [], []
+    for _ in range(args.steps):
+        flush()
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        e0.record()
+        fwd()
+        e1.record()
+        bwd()
+        e2.record()
+        e2.synchronize()
+        t_f.append(e0.elapsed_time(e1))
+        t_b.append(e0.elapsed_time(e2) - e0.elapsed_time(e1))
+    ms_f, ms_b = statistics.mean(t_f), statistics.mean(t_b)
+    ms = ms_f + ms_b
+    canon = 3 * 2.0 * K * N * D
+    peaks, src = measured_peaks()
+    peak = peaks.get("bf16_tflops", 1900.0) / 3.0
+    print(json.dumps({
+        "mode": "fe",
+        "metric": "free-energy forward + backward (dY, dT, dbeta) per second",
+        "value": 1000.0 / ms, "unit": "fwd+bwd/s", "higher_is_better": True,
+        "ms_per_step": ms, "ms_forward": ms_f, "ms_backward": ms_b, "steps": args.steps,
+        "F": F.item(), "finite": bool(torch.isfinite(dT).all() and torch.isfinite(dY).all()),
+        "roofline": {"bound": "tensor", "canonical_flop": canon, "achieved": canon / ms / 1e9,
+                     "peak": peak, "unit": "TFLOP/s", "frac": canon / ms / 1e9 / peak,
+                     "peak_source": f"bf16 dense burst ({src}) / 3"},
+        "dtype": "fp32 data, split-BF16 tensor-core products, fp64 reductions",
+        "data": "synthetic (16-component Gaussian mixture, sd 0.2)",
+        "config": {"workload": f"annealed free energy and gradient, N={N}, D={D}, K={K}, "
+                               f"beta={beta}, temp={temp}", "N": N, "D": D, "K": K,
+                   "l2": "flushed between steps (512 MB write)"}}), flush=True)
+
+
+def main_large(args):
+    """EM iterations of the large split-precision configuration, then the
+    gradient projection of held-out points onto the fixed map."""
+    import ctypes
+    import torch
+    pkg = importlib.import_module("da-gtm_gb300")
+    ds = importlib.import_module("da-gtm_gb300.datasets")
+    st = importlib.import_module("da-gtm_gb300.gtm_setup")
+    N, D, K, M, L = 4_000_000, 166, 32768, 512, 3
+    T = ds.fingerprints(N, D, 50, seed=0)
+    # width 0.5: at the reference's 2 the 512 basis functions on a 32^3 grid
+    # are numerically dependent (cond(FI^T FI) = 3e19) and W is undetermined
+    X, FI, W0, beta0 = st.random_init(T[:200_000], L, K, M, 0.5, seed=1)
+    Y0 = FI @ W0
+    temp0 = st.start_temp(T[:200_000], 0.99)
+    ctx = pkg.Context(T, FI, "bf16x3")
+    ctx.set_Y(Y0)
+    beta = beta0
+    for _ in range(max(1, args.warmup)):
+        ctx.estep(beta, 1, temp0)
+        beta, _, _ = ctx.mstep(want_W=False)
+    ctx.set_timing(True)
+    ctx.reset_timing()
+    steps = max(1, args.steps)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        ctx.estep(beta, 1, temp0)
+        beta, _, _ = ctx.mstep(want_W=False)
+    torch.cuda.synchronize()
+    em_s = (time.perf_counter() - t0) / steps
+    phases = {p: v["ms"] / steps for p, v in ctx.timing().items()}
+    Ymap = torch.tensor(ctx.get_Y(), dtype=torch.float32, device="cuda")
+    ctx.close()
+    del T
+    # held-out points: the same generator, another seed
+    Nh = 1_000_000
+    Th = torch.tensor(ds.fingerprints(Nh, D, 50, seed=7, dtype=np.float32), device="cuda")
+    lib, ws, wp, wsz = fe_buffers(torch, pkg, Nh, K, D)
+    F = torch.empty((), dtype=torch.float64, device="cuda")
+    g = torch.ones((), dtype=torch.float64, device="cuda")
+    dT = torch.empty_like(Th)
+    sptr = torch.cuda.current_stream().cuda_stream
+    step = 1.0 / beta
+    P = Th.clone()
+
+    def grad_step():
+        pkg._check(lib.dgtm_fe_forward(Ymap.data_ptr(), P.data_ptr(), Nh, K, D, beta, 1.0, wp,
+                                       wsz, sptr, F.data_ptr()))
+        pkg._check(lib.dgtm_fe_backward(Ymap.data_ptr(), P.data_ptr(), Nh, K, D, beta, 1.0, wp,
+                                        wsz, sptr, g.data_ptr(), None, dT.data_ptr(), None))
+        P.add_(dT, alpha=step)
+
+    grad_step()
+    P.copy_(Th)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.proj_steps):
+        grad_step()
+    e1.record()
+    e1.synchronize()
+    proj_ms = e0.elapsed_time(e1)
+    moved = float((P - Th).norm(dim=1).mean())
+    print(json.dumps({
+        "mode": "large",
+        "metric": "EM iters/sec at N=4M, K=32768, M=512 (bf16x3) and projected points/sec",
+        "value": 1.0 / em_s, "unit": "EM iters/s", "higher_is_better": True,
+        "ms_per_step": em_s * 1000.0, "steps": steps, "phases_ms_per_step": phases,
+        "projection": {"points": Nh, "gradient_steps": args.proj_steps,
+                       "ms": proj_ms, "ms_per_gradient_step": proj_ms / args.proj_steps,
+                       "points_per_s": Nh / (proj_ms / 1000.0),
+                       "step_size": "1/beta (one step is the fixed-point update at temp 1)",
+                       "mean_displacement": moved, "finite": bool(torch.isfinite(P).all())},
+        "dtype": "bf16x3 (split BF16 products, fp32 accumulate, fp64 reductions)",
+        "data": "synthetic (seeded binary fingerprints, 50 prototypes)",
+        "config": {"workload": f"DA-GTM EM iteration, N={N}, D={D}, K={K} (32^3), M={M} (8^3) "
+                               "+ bias, width 0.5, bf16x3 form; projection of 1M held-out "
+                               "points", "N": N, "D": D, "K": K, "M": M, "L": L,
+                   "temp": temp0}}), flush=True)
+
+
 def main_reference(args):
     """The reference's CPU path (restated: the reference itself needs MPI, GSL
     and HDF5) on the host cores, from the same data and initial state as the
@@ -619,6 +804,12 @@ if __name__ == "__main__":
     elif a.ctemp:
         if dist_env()[0] == 0:
             main_ctemp(a)
+    elif a.fe:
+        if dist_env()[0] == 0:
+            main_fe(a)
+    elif a.large:
+        if dist_env()[0] == 0:
+            main_large(a)
     elif a.impl == "reference":
         main_reference(a)
     else:

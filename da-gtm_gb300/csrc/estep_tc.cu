@@ -74,7 +74,8 @@ struct P1Params {
     double c1, c2;        // beta/2, beta/(2 temp)
     int isDA, two_temps;  // two_temps: isDA and temp != 1
     const float *Y32;     // K x D
-    const double *T64;    // N x D (exact data, read when T is split in two pieces)
+    const double *T64;    // N x D (exact data, read when T is split in two pieces) ...
+    const float *T32;     // ... or, when not null, the data as given in FP32
     const uint32_t *Tb;   // nT x Npad x Dp BF16 (as BF16 pairs)
     double2 *colstat;     // N
     float4 *colq;         // Npad
@@ -445,6 +446,13 @@ __global__ void __launch_bounds__(P1_THREADS, 1)
                             }
                         }
                     }
+                }
+            } else if (active && p.T32) {
+                const float *tn = p.T32 + (size_t) n * p.D;
+#pragma unroll 8
+                for (int d = 0; d < p.D; d++) {
+                    const float df = yk[d] - tn[d];
+                    dsum = fmaf(df, df, dsum);
                 }
             } else if (active) {
                 const double *tn = p.T64 + (size_t) n * p.D;
@@ -937,6 +945,312 @@ P2Kernel pass2_for(int np, int kl, int nt)
 }
 
 // ---------------------------------------------------------------------------
+// pass 3: C_n = sum_k R_kn y_k for every point (the free energy's gradient
+// with respect to the data, and the projection of new points onto a map).
+// The transpose of pass 2's problem: points own the rows and the centres are
+// streamed.  One CTA per 128-point tile; the tile's data pieces live in
+// tensor memory as the A operand of the distance product, like pass 1.  Per
+// 64-centre chunk of Y (hi and lo pieces through a TMA ring):
+//   MMA 1  S = T Y^T (M = 128 points, N = 64 centres, A from tensor memory);
+//   eight warps (four lane quarters x two 32-centre halves) turn S into
+//          R = exp2(scale (S - m) - log2 s) with the forward's per-point
+//          statistics, split into BF16 hi / lo and written over S;
+//   MMA 2  OUT += R Y (M = 128 points, N = D rounded up to 64, K = 16
+//          centres, A = R from tensor memory, B = the same Y chunk read
+//          MN-major): R_hi Y_hi + R_hi Y_lo + R_lo Y_hi.
+// Two S buffers let MMA 1 of the next chunk run while the warps work.  OUT
+// is moved to C (FP32, global) every P3_SEG chunks (a segment) so that no
+// accumulator runs over more than 2048 centres: the tensor pipe's FP32
+// accumulation drifts low over long runs of MMAs, as measured for pass 2.
+// ---------------------------------------------------------------------------
+constexpr int P3_THREADS = 320;  // warp 0 TMA, warp 1 MMA, warps 2-9 responsibilities
+constexpr int P3_TILE = 128;     // points per CTA (MMA M)
+constexpr int P3_BK = 64;        // centres per chunk
+constexpr int P3_SEG = 32;       // chunks per segment of the output accumulator
+
+struct P3Params {
+    int N, D, Npad, Kpad, nchunk, nstage, nout;  // nout = D rounded up to 64
+    const float4 *colq;  // Npad: (m, scale, log2 s) of each point at the temperature
+    float *C;            // N x D
+    int *status;
+};
+
+template <int NP, int KL, int NT>
+__global__ void __launch_bounds__(P3_THREADS, 1)
+    tc_rty_kernel(const __grid_constant__ CUtensorMap tmY, const __grid_constant__ CUtensorMap tmT,
+                  const P3Params p)
+{
+    constexpr int ACOL = NP * 32;          // TMEM columns of one data piece
+    constexpr int KS = 4 * (NP - 1) + KL;  // 16-deep steps of the distance product
+    constexpr int YPANEL = P3_BK * 128;    // 8 KB: 64 centres x 64 depths
+    constexpr int SLOT = NP * YPANEL;      // one piece (hi or lo) of a chunk
+    constexpr int DPANEL = P3_TILE * 128;  // 16 KB: 128 points x 64 depths
+    constexpr int NDATA = 2 * NT;          // ring slots that first hold the data pieces
+    constexpr int S_COL = NT * ACOL;       // two 64-column S / R buffers
+    constexpr int O_COL = S_COL + 2 * P3_BK;
+    static_assert(O_COL + NP * 64 <= 512, "pass 3 tensor memory plan");
+    static_assert(NDATA * SLOT == NT * NP * DPANEL, "data pieces fill whole ring slots");
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char *base = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
+    const int nslot = p.nstage;
+    unsigned char *Yslot = base;
+    uint64_t *bars = (uint64_t *) (Yslot + nslot * SLOT);
+    uint64_t *y_full = bars;
+    uint64_t *y_empty = bars + nslot;
+    uint64_t *t_full = bars + 2 * nslot;
+    uint64_t *t_done = t_full + 1;
+    uint64_t *s_full = t_done + 1;   // [2]
+    uint64_t *s_free = s_full + 2;   // [2]
+    uint64_t *p_full = s_free + 2;   // [2]
+    uint64_t *o_full = p_full + 2;
+    uint64_t *o_empty = o_full + 1;
+    uint64_t *drain = o_empty + 1;
+    uint32_t *tmem_sh = (uint32_t *) (drain + 1);
+    __shared__ int failed;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int n0 = blockIdx.x * P3_TILE;
+    const int nseg = (p.nchunk + P3_SEG - 1) / P3_SEG;
+
+    if (threadIdx.x == 0) {
+        failed = 0;
+        for (int s = 0; s < nslot; s++) {
+            mbar_init(&y_full[s], 1);
+            mbar_init(&y_empty[s], 1);
+        }
+        mbar_init(t_full, 1);
+        mbar_init(t_done, 1);
+        for (int b = 0; b < 2; b++) {
+            mbar_init(&s_full[b], 1);
+            mbar_init(&s_free[b], 1);
+            mbar_init(&p_full[b], 256);
+        }
+        mbar_init(o_full, 1);
+        mbar_init(o_empty, 256);
+        mbar_init(drain, 1);
+        fence_barrier_init();
+    }
+    if (warp == 0) {
+        tmem_alloc(tmem_sh, 512);
+        tc_fence_before();
+    }
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = __shfl_sync(0xffffffffu, *tmem_sh, 0);
+
+    if (warp == 0 && lane == 0) {
+        // ---------------- producer ----------------
+        prefetch_tmap(&tmY);
+        prefetch_tmap(&tmT);
+        unsigned char *dstage = Yslot + (nslot - NDATA) * SLOT;
+        mbar_expect_tx(t_full, (uint32_t) (NT * NP * DPANEL));
+#pragma unroll
+        for (int tp = 0; tp < NT; tp++)
+#pragma unroll
+            for (int pn = 0; pn < NP; pn++)
+                tma_load_2d(dstage + (tp * NP + pn) * DPANEL, &tmT, t_full, PANEL_ELEMS * pn,
+                            tp * p.Npad + n0);
+        for (int it = 0; it < 2 * p.nchunk; it++) {
+            const int q = it % nslot;
+            if (it >= nslot && !mbar_wait(&y_empty[q], ((it / nslot) & 1) ^ 1u, p.status, 41)) {
+                failed = 1;
+                break;
+            }
+            if (it < nslot && q >= nslot - NDATA && !mbar_wait(t_done, 0, p.status, 42)) {
+                failed = 1;
+                break;
+            }
+            const int c = it >> 1, piece = it & 1;
+            mbar_expect_tx(&y_full[q], (uint32_t) SLOT);
+#pragma unroll
+            for (int pn = 0; pn < NP; pn++)
+                tma_load_2d(Yslot + q * SLOT + pn * YPANEL, &tmY, &y_full[q], PANEL_ELEMS * pn,
+                            piece * p.Kpad + c * P3_BK);
+        }
+    } else if (warp == 1) {
+        // ---------------- MMA issuer (whole warp; one elected lane issues) ----------------
+        const uint32_t id1 = idesc_bf16(P3_TILE, P3_BK, 0, 0);
+        const uint32_t id2 = idesc_bf16(P3_TILE, p.nout, 0, 1);
+        const uint64_t yk = sdesc_sw128(smem_u32(Yslot), 16, 1024);      // K-major (MMA 1)
+        const uint64_t ymn = sdesc_sw128(smem_u32(Yslot), YPANEL, 1024);  // MN-major (MMA 2)
+        bool ok = mbar_wait_w(t_full, 0, p.status, 43);
+        if (ok) {
+            tc_fence_after();
+            const uint64_t tdesc = yk + (uint64_t) ((nslot - NDATA) * (SLOT >> 4));
+#pragma unroll
+            for (int tp = 0; tp < NT; tp++)
+#pragma unroll
+                for (int pn = 0; pn < NP; pn++)
+#pragma unroll
+                    for (int kk = 0; kk < (pn == NP - 1 ? KL : 4); kk++)
+                        tmem_cp_w(tmem + (uint32_t) (tp * ACOL + pn * 32 + kk * 8),
+                                  tdesc + (uint64_t) ((tp * NP + pn) * (DPANEL >> 4) + 2 * kk));
+            mma_commit_w(t_done);
+            ok = mbar_wait_w(t_done, 0, p.status, 43);
+            tc_fence_after();
+        }
+        for (int c = 0; ok && c <= p.nchunk; c++) {
+            if (c < p.nchunk) {
+                const int b = c & 1;
+                if (c >= 2 && !mbar_wait_w(&s_free[b], ((c - 2) >> 1) & 1, p.status, 44)) {
+                    ok = false;
+                    break;
+                }
+                const uint32_t d = tmem + (uint32_t) (S_COL + b * P3_BK);
+#pragma unroll
+                for (int piece = 0; piece < 2; piece++) {
+                    const int it = 2 * c + piece, q = it % nslot;
+                    if (!mbar_wait_w(&y_full[q], (it / nslot) & 1, p.status, 45)) {
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint64_t bd = yk + (uint64_t) (q * (SLOT >> 4));
+#pragma unroll
+                    for (int tp = 0; tp < (piece == 0 ? NT : 1); tp++)
+#pragma unroll
+                        for (int ks = 0; ks < KS; ks++)
+                            mma_ts_w(d, tmem + (uint32_t) (tp * ACOL + ks * 8),
+                                     bd + (uint64_t) ((ks >> 2) * (YPANEL >> 4) + 2 * (ks & 3)), id1,
+                                     (piece | tp | ks) ? 1u : 0u);
+                }
+                if (!ok)
+                    break;
+                mma_commit_w(&s_full[b]);
+            }
+            if (c > 0) {
+                const int j = c - 1, b = j & 1;
+                if (!mbar_wait_w(&p_full[b], (j >> 1) & 1, p.status, 46)) {
+                    ok = false;
+                    break;
+                }
+                const int seg = j / P3_SEG;
+                const bool seg_first = (j % P3_SEG) == 0;
+                if (seg_first && seg > 0 && !mbar_wait_w(o_empty, (seg - 1) & 1, p.status, 47)) {
+                    ok = false;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t a0 = tmem + (uint32_t) (S_COL + b * P3_BK);
+                const int qh = (2 * j) % nslot, ql = (2 * j + 1) % nslot;
+#pragma unroll
+                for (int pr = 0; pr < 3; pr++) {
+                    // (R hi, Y hi), (R hi, Y lo), (R lo, Y hi)
+                    const int rp = pr == 2 ? 1 : 0;
+                    const uint64_t bd = ymn + (uint64_t) ((pr == 1 ? ql : qh) * (SLOT >> 4));
+#pragma unroll
+                    for (int kk = 0; kk < P3_BK / 16; kk++)
+                        // centres 16 kk .. 16 kk + 15 belong to half kk / 2, whose 32
+                        // columns hold R hi (16) then R lo (16)
+                        mma_ts_w(tmem + (uint32_t) O_COL,
+                                 a0 + (uint32_t) ((kk >> 1) * 32 + rp * 16 + (kk & 1) * 8),
+                                 bd + (uint64_t) (kk * (2048 >> 4)), id2,
+                                 (!seg_first || pr || kk) ? 1u : 0u);
+                }
+                mma_commit_w(&y_empty[qh]);
+                mma_commit_w(&y_empty[ql]);
+                mma_commit_w(&s_free[b]);
+                if ((j % P3_SEG) == P3_SEG - 1 || j == p.nchunk - 1)
+                    mma_commit_w(o_full);
+            }
+        }
+        if (!ok)
+            failed = 1;
+    } else if (warp >= 2) {
+        // ---------------- responsibilities and the segment drains ----------------
+        const int q = warp & 3;          // TMEM lane quarter: points 32 q .. 32 q + 31
+        const int h = (warp - 2) >> 2;   // centres 32 h .. 32 h + 31 of a chunk
+        const int row = q * 32 + lane;
+        const int n = n0 + row;
+        const uint32_t lane_base = tmem + ((uint32_t) (q * 32) << 16);
+        const float4 cq = p.colq[n];  // n < Npad: padding points carry R = 0
+        bool ok = true;
+        // OUT (this thread's row) to C: 32-column batches, batch i to half i % 2
+        auto drain_out = [&](bool add) {
+#pragma unroll 1
+            for (int c0 = 32 * h; c0 < p.nout; c0 += 64) {
+                uint32_t v[32];
+                tmem_ld32(lane_base + (uint32_t) (O_COL + c0), v);
+                tmem_ld_wait();
+                if (n < p.N) {
+                    float *dst = p.C + (size_t) n * p.D + c0;
+#pragma unroll
+                    for (int e = 0; e < 32; e++) {
+                        if (c0 + e < p.D)
+                            dst[e] = add ? dst[e] + __uint_as_float(v[e]) : __uint_as_float(v[e]);
+                    }
+                }
+            }
+        };
+        for (int c = 0; c < p.nchunk; c++) {
+            const int b = c & 1;
+            if (!mbar_wait(&s_full[b], (c >> 1) & 1, p.status, 48)) {
+                ok = false;
+                break;
+            }
+            tc_fence_after();
+            const uint32_t col0 = (uint32_t) (S_COL + b * P3_BK + h * 32);
+            uint32_t va[32];
+            tmem_ld32(lane_base + col0, va);
+            tmem_ld_wait();
+            uint32_t hi[16], lo[16];
+#pragma unroll
+            for (int e = 0; e < 16; e++) {
+                const float r0 = ex2(fmaf(__uint_as_float(va[2 * e]) - cq.x, cq.y, -cq.z));
+                const float r1 = ex2(fmaf(__uint_as_float(va[2 * e + 1]) - cq.x, cq.y, -cq.z));
+                const uint32_t hh = pack_bf16(r0, r1);
+                hi[e] = hh;
+                lo[e] = pack_bf16(r0 - bf16lo_to_f32(hh), r1 - bf16hi_to_f32(hh));
+            }
+            tmem_st16(lane_base + col0, hi);
+            tmem_st16(lane_base + col0 + 16, lo);
+            tmem_st_wait();
+            tc_fence_before();
+            mbar_arrive(&p_full[b]);
+            if ((c % P3_SEG) == P3_SEG - 1 || c == p.nchunk - 1) {
+                const int seg = c / P3_SEG;
+                if (!mbar_wait(o_full, seg & 1, p.status, 49)) {
+                    ok = false;
+                    break;
+                }
+                tc_fence_after();
+                drain_out(seg > 0);
+                if (seg + 1 < nseg) {
+                    tc_fence_before();
+                    mbar_arrive(o_empty);
+                }
+            }
+        }
+        if (!ok)
+            failed = 1;
+    }
+    __syncthreads();
+    if (failed && warp == 1) {
+        mma_commit_w(drain);
+        mbar_wait_w(drain, 0, p.status, 50, 100000000ull);
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0)
+        tmem_dealloc(tmem, 512);
+}
+
+using P3Kernel = void (*)(const CUtensorMap, const CUtensorMap, const P3Params);
+
+// the pass-3 instantiation for a shape (NP <= 3 panels, KL steps in the last, NT pieces)
+P3Kernel pass3_for(int np, int kl, int nt)
+{
+#define DGTM_P3(NP_, KL_, NT_) \
+    if (np == NP_ && kl == KL_ && nt == NT_) return tc_rty_kernel<NP_, KL_, NT_>;
+#define DGTM_P3_KL(NP_, NT_) DGTM_P3(NP_, 1, NT_) DGTM_P3(NP_, 2, NT_) DGTM_P3(NP_, 3, NT_) DGTM_P3(NP_, 4, NT_)
+    DGTM_P3_KL(1, 1) DGTM_P3_KL(1, 2) DGTM_P3_KL(2, 1) DGTM_P3_KL(2, 2) DGTM_P3_KL(3, 1) DGTM_P3_KL(3, 2)
+#undef DGTM_P3_KL
+#undef DGTM_P3
+    return nullptr;
+}
+
+// ---------------------------------------------------------------------------
 // operand preparation and the slot reduction
 // ---------------------------------------------------------------------------
 __global__ void t_exact_kernel(const double *__restrict__ T64, size_t n, int *inexact)
@@ -950,9 +1264,12 @@ __global__ void t_exact_kernel(const double *__restrict__ T64, size_t n, int *in
     }
 }
 
-// T pieces (nT x Npad x Dp): value pieces, three columns of ones, zero padding.
-__global__ void t_split_kernel(const double *__restrict__ T64, int N, int D, int Dp, int Npad,
-                               int nT, __nv_bfloat16 *__restrict__ Tb)
+// T pieces (nT x Npad x Dp): value pieces, three columns of ones, zero
+// padding.  F: the data as the caller holds it (FP64 for a context, FP32 for
+// the free energy); the second piece is the remainder t - hi, rounded to BF16.
+template <typename F>
+__global__ void t_split_kernel(const F *__restrict__ T, int N, int D, int Dp, int Npad, int nT,
+                               __nv_bfloat16 *__restrict__ Tb)
 {
     const size_t total = (size_t) Npad * Dp;
     for (size_t i = blockIdx.x * (size_t) blockDim.x + threadIdx.x; i < total;
@@ -961,10 +1278,10 @@ __global__ void t_split_kernel(const double *__restrict__ T64, int N, int D, int
         float hi = 0.f, lo = 0.f;
         if (n < N) {
             if (d < D) {
-                const double t = T64[(size_t) n * D + d];
+                const F t = T[(size_t) n * D + d];
                 const __nv_bfloat16 h = __float2bfloat16_rn((float) t);
                 hi = __bfloat162float(h);
-                lo = (float) (t - (double) hi);
+                lo = (float) (t - (F) hi);
             } else if (d < D + 3) {
                 hi = 1.f;
             }
@@ -975,9 +1292,10 @@ __global__ void t_split_kernel(const double *__restrict__ T64, int N, int D, int
     }
 }
 
-// Y pieces (2 x Kpad x Dp) with the folded -|y_hat|^2/2 column, and Y in FP32.
-// One warp per centre row.
-__global__ void y_split_kernel(const double *__restrict__ Y64, int K, int D, int Dp, int Kpad,
+// Y pieces (2 x Kpad x Dp) with the folded -|y_hat|^2/2 column, and Y in FP32
+// (when Y32 is not null).  One warp per centre row.
+template <typename F>
+__global__ void y_split_kernel(const F *__restrict__ Y64, int K, int D, int Dp, int Kpad,
                                __nv_bfloat16 *__restrict__ Yb, float *__restrict__ Y32)
 {
     const int lane = threadIdx.x & 31;
@@ -995,14 +1313,15 @@ __global__ void y_split_kernel(const double *__restrict__ Y64, int K, int D, int
         }
         double q = 0.0;
         for (int d = lane; d < D; d += 32) {
-            const double y = Y64[(size_t) k * D + d];
+            const double y = (double) Y64[(size_t) k * D + d];
             const __nv_bfloat16 h = __float2bfloat16_rn((float) y);
             const double hd = (double) __bfloat162float(h);
             const __nv_bfloat16 l = __float2bfloat16_rn((float) (y - hd));
             const double yh = hd + (double) __bfloat162float(l);
             hi[d] = h;
             lo[d] = l;
-            Y32[(size_t) k * D + d] = (float) y;
+            if (Y32)
+                Y32[(size_t) k * D + d] = (float) y;
             q += yh * yh;
         }
 #pragma unroll
@@ -1118,18 +1437,20 @@ static int p2_unit_tiles(int ntiles, int ktiles, int grid_max)
 struct TcState {
     int N, D, K, sms;
     int Dp, npanel, Npad, Kpad, nT, ksteps;
-    int nchunk, nstage1, nstage2, ntile1, bn2;
+    int nchunk, nstage1, nstage2, nstage3, ntile1, bn2;
     int ntiles2, unit_tiles, units_per_k, nunits, grid2;
-    size_t smem1, smem2;
+    size_t smem1, smem2, smem3;
     P1Kernel pass1;
     P2Kernel pass2;
+    P3Kernel pass3;
     __nv_bfloat16 *Tb, *Yb;
     float *Y32;
     float4 *colq;
     float *RTpart;
     int *status, *hstatus;
     const double *tt, *T64;
-    CUtensorMap tmT1, tmT2, tmY1;
+    const float *T32;  // the data in FP32 (free energy), or null
+    CUtensorMap tmT1, tmT2, tmY1, tmY3;
 };
 
 static int grid_for(size_t n, int per = 256, int cap = 8192)
@@ -1140,10 +1461,111 @@ static int grid_for(size_t n, int per = 256, int cap = 8192)
     return b == 0 ? 1 : (int) b;
 }
 
-int tc_create(TcState **out, int N, int D, int K, int sms, const double *T64, const double *tt,
-              cudaStream_t s)
+// The split form's shapes, kernel instantiations and shared-memory plans for
+// N points, K centres, D dimensions and nT data pieces (no allocation).
+static int tc_plan(TcState *st, int N, int D, int K, int sms, int nT)
 {
-    *out = nullptr;
+    if (D + 3 > 3 * PANEL_ELEMS) {
+        // pass 2 keeps the R T accumulator (D + 3 padded to 64-column panels),
+        // two S/P buffers and the centres in the 512 tensor-memory columns
+        set_error(DGTM_ENOTSUP, "the split-BF16 form supports D <= 189 (D = %d)", D);
+        return DGTM_ENOTSUP;
+    }
+    st->N = N;
+    st->D = D;
+    st->K = K;
+    st->sms = sms;
+    st->nT = nT;
+    st->Dp = round_up(D + 3, PANEL_ELEMS);
+    st->npanel = st->Dp / PANEL_ELEMS;
+    st->ksteps = (D + 3 + 15) / 16;  // columns D + 3 .. Dp - 1 are zero in both operands
+    st->Npad = round_up(N, NPAD_ALIGN);
+    st->Kpad = round_up(K, P1_BK);
+    st->nchunk = st->Kpad / P1_BK;
+    // exact 0/1 data: two 128-point tiles per pass-1 CTA; split data (two T
+    // pieces) one, to fit tensor memory.  Pass-2 tiles are 64 points.
+    st->ntile1 = (nT == 1) ? 2 : 1;
+    st->bn2 = P2_TILE;
+    st->ntiles2 = st->Npad / st->bn2;
+    const int ktiles2 = (K + P2_BK - 1) / P2_BK;
+    st->unit_tiles = p2_unit_tiles(st->ntiles2, ktiles2, sms);
+    st->units_per_k = (st->ntiles2 + st->unit_tiles - 1) / st->unit_tiles;
+    st->nunits = ktiles2 * st->units_per_k;
+    st->grid2 = st->nunits < sms ? st->nunits : sms;
+    const size_t bar_bytes = 64 * 8 + 16 + 2 * 256 * 8;
+    const int klast = st->ksteps - 4 * (st->npanel - 1);
+    // pass 1: Y slots of one chunk piece (npanel panels of 16 KB); the data
+    // tiles live in tensor memory
+    const size_t slot1 = (size_t) st->npanel * P1_BK * 128;
+    int ns1 = (int) ((SMEM_LIMIT - 1024 - bar_bytes) / slot1);
+    if (ns1 > 12)
+        ns1 = 12;
+    st->pass1 = pass1_for(st->npanel, klast, nT);
+    // pass 2: the point-tile ring (T pieces + column statistics); the centres
+    // live in tensor memory
+    const size_t ts2 = (size_t) nT * st->npanel * P2_TILE * 128 + P2_TILE * 16;
+    const size_t rtbuf2 =
+        p2_segbuf(st->npanel, nT) ? (size_t) P2_BK * (st->npanel * PANEL_ELEMS + 4) * 4 : 0;
+    int ns2 = (int) ((SMEM_LIMIT - 1024 - bar_bytes - rtbuf2) / ts2);
+    if (ns2 > 8)
+        ns2 = 8;
+    st->pass2 = (st->npanel <= 3) ? pass2_for(st->npanel, klast, nT) : nullptr;
+    // pass 3: Y slots of one 64-centre chunk piece; the first 2 nT slots
+    // stage the data tile on its way to tensor memory
+    const size_t slot3 = (size_t) st->npanel * P3_BK * 128;
+    int ns3 = (int) ((SMEM_LIMIT - 1024 - bar_bytes) / slot3);
+    if (ns3 > 12)
+        ns3 = 12;
+    st->pass3 = (st->npanel <= 3) ? pass3_for(st->npanel, klast, nT) : nullptr;
+    if (!st->pass2 || !st->pass3) {
+        set_error(DGTM_ENOTSUP, "the split-BF16 form supports D <= 189 (D = %d)", D);
+        return DGTM_ENOTSUP;
+    }
+    if (ns1 < 2 || ns2 < 2 || ns3 < 4 || ns3 < 2 * nT || !st->pass1) {
+        set_error(DGTM_ENOTSUP, "the split-BF16 form does not fit shared memory (D = %d)", D);
+        return DGTM_ENOTSUP;
+    }
+    st->nstage1 = ns1;
+    st->nstage2 = ns2;
+    st->nstage3 = ns3;
+    st->smem1 = 1024 + (size_t) ns1 * slot1 + bar_bytes;
+    st->smem2 = 1024 + (size_t) ns2 * ts2 + rtbuf2 + bar_bytes;
+    st->smem3 = 1024 + (size_t) ns3 * slot3 + bar_bytes;
+    cudaError_t e = cudaFuncSetAttribute(st->pass1, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int) st->smem1);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(st->pass2, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int) st->smem2);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(st->pass3, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int) st->smem3);
+    if (e != cudaSuccess) {
+        set_error(DGTM_ECUDA, "tc_plan: %s", cudaGetErrorString(e));
+        return DGTM_ECUDA;
+    }
+    return DGTM_OK;
+}
+
+// The TMA maps of the operand buffers the state points to.
+static int tc_maps(TcState *st)
+{
+    int rc;
+    // T pieces stacked by rows (pass-1 data tiles, pass-2 tiles), Y pieces
+    // stacked by rows (pass-1 chunks, pass-3 chunks)
+    if ((rc = make_tmap_bf16(&st->tmT1, st->Tb, (uint64_t) st->nT * st->Npad, st->Dp, st->Dp,
+                             P1_TILE, PANEL_ELEMS)) != DGTM_OK ||
+        (rc = make_tmap_bf16(&st->tmT2, st->Tb, (uint64_t) st->nT * st->Npad, st->Dp, st->Dp,
+                             P2_TILE, PANEL_ELEMS)) != DGTM_OK ||
+        (rc = make_tmap_bf16(&st->tmY1, st->Yb, 2 * (uint64_t) st->Kpad, st->Dp, st->Dp, P1_BK,
+                             PANEL_ELEMS)) != DGTM_OK ||
+        (rc = make_tmap_bf16(&st->tmY3, st->Yb, 2 * (uint64_t) st->Kpad, st->Dp, st->Dp, P3_BK,
+                             PANEL_ELEMS)) != DGTM_OK)
+        return rc;
+    return DGTM_OK;
+}
+
+static int sm10x_or_fail()
+{
     int dev = 0, major = 0, minor = 0;
     DGTM_CUDA_TRY(cudaGetDevice(&dev));
     DGTM_CUDA_TRY(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev));
@@ -1153,26 +1575,24 @@ int tc_create(TcState **out, int N, int D, int K, int sms, const double *T64, co
                   major, minor);
         return DGTM_ENOTSUP;
     }
+    return DGTM_OK;
+}
+
+int tc_create(TcState **out, int N, int D, int K, int sms, const double *T64, const double *tt,
+              cudaStream_t s)
+{
+    *out = nullptr;
+    int rc = sm10x_or_fail();
+    if (rc != DGTM_OK)
+        return rc;
     if (D + 3 > 3 * PANEL_ELEMS) {
-        // pass 2 keeps the R T accumulator (D + 3 padded to 64-column panels),
-        // two S/P buffers and the centres in the 512 tensor-memory columns
         set_error(DGTM_ENOTSUP, "the split-BF16 form supports D <= 189 (D = %d)", D);
         return DGTM_ENOTSUP;
     }
     TcState *st = new TcState();
-    st->N = N;
-    st->D = D;
-    st->K = K;
-    st->sms = sms;
     st->tt = tt;
     st->T64 = T64;
-    st->Dp = round_up(D + 3, PANEL_ELEMS);
-    st->npanel = st->Dp / PANEL_ELEMS;
-    st->ksteps = (D + 3 + 15) / 16;  // columns D + 3 .. Dp - 1 are zero in both operands
-    st->Npad = round_up(N, NPAD_ALIGN);
-    st->Kpad = round_up(K, P1_BK);
-    st->nchunk = st->Kpad / P1_BK;
-    int rc = DGTM_OK;
+    st->T32 = nullptr;
     auto fail = [&](int code) {
         tc_destroy(st);
         return code;
@@ -1194,21 +1614,9 @@ int tc_create(TcState **out, int N, int D, int K, int sms, const double *T64, co
         set_error(DGTM_ECUDA, "tc_create: %s", cudaGetErrorString(e));
         return fail(DGTM_ECUDA);
     }
-    st->nT = (*st->hstatus) ? 2 : 1;
-    // exact 0/1 data: two 128-point tiles per pass-1 CTA; split data (two T
-    // pieces) one, to fit tensor memory.  Pass-2 tiles are 64 points.
-    st->ntile1 = (st->nT == 1) ? 2 : 1;
-    st->bn2 = P2_TILE;
-
+    if ((rc = tc_plan(st, N, D, K, sms, (*st->hstatus) ? 2 : 1)) != DGTM_OK)
+        return fail(rc);
     const size_t tpl = (size_t) st->Npad * st->Dp, ypl = (size_t) st->Kpad * st->Dp;
-    // pass 2 work units
-    st->ntiles2 = st->Npad / st->bn2;
-    const int ktiles2 = (K + P2_BK - 1) / P2_BK;
-    st->unit_tiles = p2_unit_tiles(st->ntiles2, ktiles2, sms);
-    st->units_per_k = (st->ntiles2 + st->unit_tiles - 1) / st->unit_tiles;
-    st->nunits = ktiles2 * st->units_per_k;
-    st->grid2 = st->nunits < sms ? st->nunits : sms;
-
     e = cudaMalloc((void **) &st->Tb, sizeof(__nv_bfloat16) * tpl * st->nT);
     if (e == cudaSuccess)
         e = cudaMalloc((void **) &st->Yb, sizeof(__nv_bfloat16) * ypl * 2);
@@ -1222,61 +1630,15 @@ int tc_create(TcState **out, int N, int D, int K, int sms, const double *T64, co
         set_error(DGTM_ENOMEM, "tc_create: %s", cudaGetErrorString(e));
         return fail(DGTM_ENOMEM);
     }
-    t_split_kernel<<<grid_for(tpl), 256, 0, s>>>(T64, N, D, st->Dp, st->Npad, st->nT, st->Tb);
+    t_split_kernel<double><<<grid_for(tpl), 256, 0, s>>>(T64, N, D, st->Dp, st->Npad, st->nT,
+                                                         st->Tb);
     e = cudaGetLastError();
     if (e != cudaSuccess) {
         set_error(DGTM_ECUDA, "t_split: %s", cudaGetErrorString(e));
         return fail(DGTM_ECUDA);
     }
-    // tensor maps: T pieces stacked by rows (pass-1 data tiles, pass-2 tiles),
-    // Y pieces stacked by rows (pass-1 chunks)
-    if ((rc = make_tmap_bf16(&st->tmT1, st->Tb, (uint64_t) st->nT * st->Npad, st->Dp, st->Dp,
-                             P1_TILE, PANEL_ELEMS)) != DGTM_OK ||
-        (rc = make_tmap_bf16(&st->tmT2, st->Tb, (uint64_t) st->nT * st->Npad, st->Dp, st->Dp,
-                             P2_TILE, PANEL_ELEMS)) != DGTM_OK ||
-        (rc = make_tmap_bf16(&st->tmY1, st->Yb, 2 * (uint64_t) st->Kpad, st->Dp, st->Dp, P1_BK,
-                             PANEL_ELEMS)) != DGTM_OK)
+    if ((rc = tc_maps(st)) != DGTM_OK)
         return fail(rc);
-    // shared memory plans
-    const size_t bar_bytes = 64 * 8 + 16 + 2 * 256 * 8;
-    // pass 1: Y slots of one chunk piece (npanel panels of 16 KB); the data
-    // tiles live in tensor memory
-    const size_t slot1 = (size_t) st->npanel * P1_BK * 128;
-    int ns1 = (int) ((SMEM_LIMIT - 1024 - bar_bytes) / slot1);
-    if (ns1 > 12)
-        ns1 = 12;
-    st->pass1 = pass1_for(st->npanel, st->ksteps - 4 * (st->npanel - 1), st->nT);
-    // pass 2: the point-tile ring (T pieces + column statistics); the centres
-    // live in tensor memory
-    const size_t ts2 = (size_t) st->nT * st->npanel * P2_TILE * 128 + P2_TILE * 16;
-    const size_t rtbuf2 =
-        p2_segbuf(st->npanel, st->nT) ? (size_t) P2_BK * (st->npanel * PANEL_ELEMS + 4) * 4 : 0;
-    int ns2 = (int) ((SMEM_LIMIT - 1024 - bar_bytes - rtbuf2) / ts2);
-    if (ns2 > 8)
-        ns2 = 8;
-    const int klast = st->ksteps - 4 * (st->npanel - 1);
-    st->pass2 = (st->npanel <= 3) ? pass2_for(st->npanel, klast, st->nT) : nullptr;
-    if (!st->pass2) {
-        set_error(DGTM_ENOTSUP, "the split-BF16 form supports D <= 189 (D = %d)", D);
-        return fail(DGTM_ENOTSUP);
-    }
-    if (ns1 < 2 || ns2 < 2 || !st->pass1) {
-        set_error(DGTM_ENOTSUP, "the split-BF16 form does not fit shared memory (D = %d)", D);
-        return fail(DGTM_ENOTSUP);
-    }
-    st->nstage1 = ns1;
-    st->nstage2 = ns2;
-    st->smem1 = 1024 + (size_t) ns1 * slot1 + bar_bytes;
-    st->smem2 = 1024 + (size_t) ns2 * ts2 + rtbuf2 + bar_bytes;
-    e = cudaFuncSetAttribute(st->pass1, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int) st->smem1);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(st->pass2, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int) st->smem2);
-    if (e != cudaSuccess) {
-        set_error(DGTM_ECUDA, "tc_create: %s", cudaGetErrorString(e));
-        return fail(DGTM_ECUDA);
-    }
     *out = st;
     return DGTM_OK;
 }
@@ -1306,7 +1668,7 @@ void tc_y_copies(TcState *st, YCopies *cp)
 
 int tc_prepare_y(TcState *st, const double *Y64, cudaStream_t s)
 {
-    y_split_kernel<<<grid_for((size_t) st->Kpad * 32, 256, 4096), 256, 0, s>>>(
+    y_split_kernel<double><<<grid_for((size_t) st->Kpad * 32, 256, 4096), 256, 0, s>>>(
         Y64, st->K, st->D, st->Dp, st->Kpad, st->Yb, st->Y32);
     DGTM_CUDA_TRY(cudaGetLastError());
     return DGTM_OK;
@@ -1338,6 +1700,7 @@ int tc_estep(TcState *st, const double *, double c1, double c2, int isDA, double
     p.two_temps = isDA && (c1 != c2);
     p.Y32 = st->Y32;
     p.T64 = st->T64;
+    p.T32 = st->T32;
     p.Tb = (const uint32_t *) st->Tb;
     p.colstat = colstat;
     p.colq = st->colq;
@@ -1395,6 +1758,129 @@ int tc_check_status(TcState *st)
         return DGTM_ETIMEOUT;
     }
     return DGTM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// the free energy's tensor-core passes over caller-owned FP32 arrays
+// ---------------------------------------------------------------------------
+static size_t align256(size_t x) { return (x + 255) & ~(size_t) 255; }
+
+// A plan over the workspace: T always in two BF16 pieces (the data of a
+// gradient step are real-valued, and the piece count must be known without
+// inspecting them); Y pieces with the folded -|y|^2/2 columns; the column
+// statistics; the pass-2 slots; the status word of the bounded waits.
+static int fe_state(int N, int K, int D, int sms, TcState *st, TcFeLayout *L)
+{
+    int rc = sm10x_or_fail();
+    if (rc != DGTM_OK)
+        return rc;
+    if ((rc = tc_plan(st, N, D, K, sms, 2)) != DGTM_OK)
+        return rc;
+    size_t o = 0;
+    auto take = [&](size_t bytes) {
+        const size_t at = o;
+        o += align256(bytes);
+        return at;
+    };
+    L->Tb = take(sizeof(__nv_bfloat16) * 2 * (size_t) st->Npad * st->Dp);
+    L->Yb = take(sizeof(__nv_bfloat16) * 2 * (size_t) st->Kpad * st->Dp);
+    L->colq = take(sizeof(float4) * (size_t) st->Npad);
+    L->RTpart = take(sizeof(float) * (size_t) st->nunits * P2_BK * st->Dp);
+    L->status = take(sizeof(int));
+    L->total = o;
+    L->pass1_blocks = tc_pass1_blocks(st);
+    return DGTM_OK;
+}
+
+static int fe_bind(const TcFeLayout &L, void *ws, TcState *st)
+{
+    char *b = static_cast<char *>(ws);
+    st->Tb = reinterpret_cast<__nv_bfloat16 *>(b + L.Tb);
+    st->Yb = reinterpret_cast<__nv_bfloat16 *>(b + L.Yb);
+    st->colq = reinterpret_cast<float4 *>(b + L.colq);
+    st->RTpart = reinterpret_cast<float *>(b + L.RTpart);
+    st->status = reinterpret_cast<int *>(b + L.status);
+    st->hstatus = nullptr;
+    st->T64 = nullptr;
+    st->tt = nullptr;
+    return tc_maps(st);
+}
+
+int tc_fe_layout(int N, int K, int D, int sms, TcFeLayout *L)
+{
+    TcState st{};
+    return fe_state(N, K, D, sms, &st, L);
+}
+
+int tc_fe_estep(const TcFeLayout &L, void *ws, const float *Y, const float *T, int N, int K, int D,
+                int sms, double c1, double c2, double2 *colstat, double *part, cudaStream_t s)
+{
+    TcState st{};
+    TcFeLayout L2;
+    int rc = fe_state(N, K, D, sms, &st, &L2);
+    if (rc != DGTM_OK)
+        return rc;
+    if (L2.total != L.total) {
+        set_error(DGTM_EINVAL, "free-energy workspace plan changed between calls");
+        return DGTM_EINVAL;
+    }
+    if ((rc = fe_bind(L, ws, &st)) != DGTM_OK)
+        return rc;
+    st.Y32 = const_cast<float *>(Y);
+    st.T32 = T;
+    DGTM_CUDA_TRY(cudaMemsetAsync(st.status, 0, sizeof(int), s));
+    const size_t tpl = (size_t) st.Npad * st.Dp;
+    t_split_kernel<float><<<grid_for(tpl), 256, 0, s>>>(T, N, D, st.Dp, st.Npad, 2, st.Tb);
+    DGTM_CUDA_TRY(cudaGetLastError());
+    y_split_kernel<float><<<grid_for((size_t) st.Kpad * 32, 256, 4096), 256, 0, s>>>(
+        Y, K, D, st.Dp, st.Kpad, st.Yb, nullptr);
+    DGTM_CUDA_TRY(cudaGetLastError());
+    int nl = 0;
+    // tc_estep clears the status word again; a failure of this call shows there
+    return tc_estep(&st, nullptr, c1, c2, 1, colstat, part, s, &nl);
+}
+
+int tc_fe_stats(const TcFeLayout &L, void *ws, int N, int K, int D, int sms, double *G,
+                double *RT, cudaStream_t s)
+{
+    TcState st{};
+    TcFeLayout L2;
+    int rc = fe_state(N, K, D, sms, &st, &L2);
+    if (rc != DGTM_OK || (rc = fe_bind(L, ws, &st)) != DGTM_OK)
+        return rc;
+    int nl = 0;
+    if ((rc = tc_mstep_pass(&st, nullptr, 0.0, s, &nl)) != DGTM_OK)
+        return rc;
+    return tc_mstep_reduce(&st, G, RT, s, &nl);
+}
+
+int tc_fe_rty(const TcFeLayout &L, void *ws, int N, int K, int D, int sms, float *C,
+              cudaStream_t s)
+{
+    TcState st{};
+    TcFeLayout L2;
+    int rc = fe_state(N, K, D, sms, &st, &L2);
+    if (rc != DGTM_OK || (rc = fe_bind(L, ws, &st)) != DGTM_OK)
+        return rc;
+    P3Params p;
+    p.N = N;
+    p.D = D;
+    p.Npad = st.Npad;
+    p.Kpad = st.Kpad;
+    p.nchunk = st.Kpad / P3_BK;
+    p.nstage = st.nstage3;
+    p.nout = round_up(D, PANEL_ELEMS);  // whole 128-byte swizzle atoms of the MN-major Y
+    p.colq = st.colq;
+    p.C = C;
+    p.status = st.status;
+    st.pass3<<<st.Npad / P3_TILE, P3_THREADS, st.smem3, s>>>(st.tmY3, st.tmT1, p);
+    DGTM_CUDA_TRY(cudaGetLastError());
+    return DGTM_OK;
+}
+
+int *tc_fe_status(const TcFeLayout &L, void *ws)
+{
+    return reinterpret_cast<int *>(static_cast<char *>(ws) + L.status);
 }
 
 }  // namespace dgtm

@@ -31,4 +31,28 @@ int tc_mstep_reduce(TcState *st, double *G, double *RT, cudaStream_t s, int *nla
 int tc_fetch_status(TcState *st, cudaStream_t s);
 int tc_check_status(TcState *st);
 
+// The free energy's tensor-core passes over caller-owned FP32 device arrays
+// (the data always in two BF16 pieces).  The layout gives byte offsets into a
+// 256-byte aligned region of the caller's workspace that the passes own; the
+// column statistics and the pass-1 partial sums are the caller's.
+struct TcFeLayout {
+    size_t Tb = 0, Yb = 0, colq = 0, RTpart = 0, status = 0, total = 0;
+    int pass1_blocks = 0;
+};
+// DGTM_ENOTSUP when the device or D is outside the split form.
+int tc_fe_layout(int N, int K, int D, int sms, TcFeLayout *L);
+// The operand pieces of Y and T, then pass 1 at c1 = beta/2, c2 = beta/(2 temp)
+// (DA): column statistics, the per-point statistics for passes 2 and 3, and
+// per-CTA partial sums of the two per-point terms.  Clears the status word.
+int tc_fe_estep(const TcFeLayout &L, void *ws, const float *Y, const float *T, int N, int K, int D,
+                int sms, double c1, double c2, double2 *colstat, double *part, cudaStream_t s);
+// Pass 2 and the slot sum: G = rowsum R and RT = R T (FP64) of the tempered R.
+int tc_fe_stats(const TcFeLayout &L, void *ws, int N, int K, int D, int sms, double *G,
+                double *RT, cudaStream_t s);
+// Pass 3: C = R^T Y (N x D, FP32), C_n = sum_k R_kn y_k.
+int tc_fe_rty(const TcFeLayout &L, void *ws, int N, int K, int D, int sms, float *C,
+              cudaStream_t s);
+// The device status word (non-zero: a bounded wait gave up).
+int *tc_fe_status(const TcFeLayout &L, void *ws);
+
 }  // namespace dgtm

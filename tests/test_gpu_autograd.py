@@ -3,8 +3,10 @@ torch.autograd.Function) against FP64 references.
 
 F is checked against N times the oracle's DA quality; dF/dY, dF/dT and
 dF/dbeta against the FP64 analytic gradient and against FP64 central finite
-differences of the oracle's F (step 1e-6).  The forward/backward compute in
-FP32 with FP64 reductions: relative tolerances 1e-5 on F, 1e-3 on gradients.
+differences of the oracle's F (step 1e-6).  On a Blackwell GPU with D <= 189
+the contractions run on the tensor cores in the split-BF16 form (three BF16
+products per FP32 product, FP32 accumulation, FP64 reductions); elsewhere on
+FP32 CUDA cores.  Relative tolerances 1e-5 on F, 1e-3 on gradients.
 """
 import importlib
 
@@ -61,6 +63,41 @@ def test_free_energy_and_analytic_gradient(pkg, orc, problem, beta, temp):
     dT_ref = -beta * (T - R.T @ Y)
     N, D = T.shape
     db_ref = N * D / (2 * beta) - 0.5 * (R * Dm).sum()
+    assert np.max(np.abs(dY - dY_ref)) <= 1e-3 * np.max(np.abs(dY_ref))
+    assert np.max(np.abs(dT - dT_ref)) <= 1e-3 * np.max(np.abs(dT_ref))
+    assert db == pytest.approx(db_ref, rel=1e-3)
+
+
+@pytest.mark.parametrize("N,K,D,binary", [(1000, 300, 37, False), (3000, 520, 166, True),
+                                          (777, 64, 189, False), (129, 130, 1, False),
+                                          (5000, 2100, 64, False)])
+def test_shapes_against_oracle(pkg, orc, N, K, D, binary):
+    """Ragged point and centre counts (tiles and chunks only partly filled),
+    D from 1 to the split form's 189, binary and real-valued data; the
+    centre count 2100 spans two 2048-centre accumulator segments of the data
+    gradient."""
+    rng = np.random.default_rng(N + K + D)
+    if binary:
+        T = (rng.random((N, D)) < 0.3).astype(np.float64)
+        Y = T[rng.integers(0, N, K)] * 0.7 + 0.15 + 0.05 * rng.standard_normal((K, D))
+        beta = 3.0
+    else:
+        T = rng.random((N, D))
+        Y = T[rng.integers(0, N, K)] + 0.05 * rng.standard_normal((K, D))
+        beta = 40.0 / max(1.0, D ** 0.5)
+    Y = Y.astype(np.float32).astype(np.float64)
+    T = T.astype(np.float32).astype(np.float64)
+    temp = 1.6
+    F, dY, dT, db = run_fe(pkg, Y, T, beta, temp)
+    Fo, R, Dm = oracle_F(orc, Y, T, beta, temp)
+    G = R.sum(1)
+    dY_ref = -beta * (G[:, None] * Y - R @ T)
+    dT_ref = -beta * (T - R.T @ Y)
+    db_ref = N * D / (2 * beta) - 0.5 * (R * Dm).sum()
+    print(f"N={N} K={K} D={D}: F {abs(F / Fo - 1):.1e} dY "
+          f"{np.max(np.abs(dY - dY_ref)) / np.max(np.abs(dY_ref)):.1e} dT "
+          f"{np.max(np.abs(dT - dT_ref)) / np.max(np.abs(dT_ref)):.1e} db {abs(db / db_ref - 1):.1e}")
+    assert F == pytest.approx(Fo, rel=1e-5)
     assert np.max(np.abs(dY - dY_ref)) <= 1e-3 * np.max(np.abs(dY_ref))
     assert np.max(np.abs(dT - dT_ref)) <= 1e-3 * np.max(np.abs(dT_ref))
     assert db == pytest.approx(db_ref, rel=1e-3)
