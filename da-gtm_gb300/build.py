@@ -94,7 +94,7 @@ def build_driver() -> str:
         return DRIVER
     cxx = shutil.which("g++") or "g++"
     cmd = [cxx, "-O2", "-std=c++17", "-Wall", "-I" + INCLUDE] + srcs + [
-        "-L" + HERE, "-ldagtm_gb300", "-Wl,-rpath,$ORIGIN", "-o", DRIVER + ".tmp"]
+        "-L" + HERE, "-ldagtm_gb300", "-lz", "-Wl,-rpath,$ORIGIN", "-o", DRIVER + ".tmp"]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"driver build failed:\n{res.stdout}\n{res.stderr}")

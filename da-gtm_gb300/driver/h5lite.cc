@@ -6,6 +6,8 @@
 #include <cstring>
 #include <fstream>
 
+#include <zlib.h>
+
 namespace h5lite {
 
 namespace {
@@ -52,7 +54,11 @@ bool header_messages(const Buf &f, uint64_t addr, std::vector<Msg> &msgs, std::s
                 err = "truncated header message";
                 return false;
             }
-            if (t == 0x10) {  // continuation
+            if (t == 0x10) {  // continuation: address, length
+                if (sz < 16) {
+                    err = "truncated continuation message";
+                    return false;
+                }
                 blocks.push_back({f.u(p + 8, 8), f.u(p + 16, 8)});
             }
             msgs.push_back({t, p + 8, sz});
@@ -101,6 +107,162 @@ bool group_entries(const Buf &f, uint64_t btree, std::vector<std::pair<uint64_t,
     return true;
 }
 
+// Filters of a chunked dataset's pipeline (message 0x0B), in order.
+bool filter_pipeline(const Buf &f, const Msg &m, std::vector<int> &ids, std::string &err)
+{
+    if (!f.in(m.off, 8) || m.size < 8) {
+        err = "truncated filter pipeline message";
+        return false;
+    }
+    const int ver = f.b[m.off], nf = f.b[m.off + 1];
+    uint64_t p = m.off + (ver == 1 ? 8 : 2);
+    const uint64_t end = m.off + m.size;
+    for (int i = 0; i < nf; i++) {
+        if (p + 2 > end) {
+            err = "truncated filter description";
+            return false;
+        }
+        const int id = (int) f.u(p, 2);
+        uint64_t name_len = 0;
+        if (ver == 1 || id >= 256) {
+            if (p + 4 > end) {
+                err = "truncated filter description";
+                return false;
+            }
+            name_len = f.u(p + 2, 2);
+            p += 4;
+        } else {
+            p += 2;
+        }
+        if (p + 4 > end) {
+            err = "truncated filter description";
+            return false;
+        }
+        const uint64_t nval = f.u(p + 2, 2);
+        p += 4;
+        if (ver == 1)
+            name_len = (name_len + 7) & ~(uint64_t) 7;
+        p += name_len + 4 * nval;
+        if (ver == 1 && (nval & 1))
+            p += 4;
+        if (p > end) {
+            err = "truncated filter description";
+            return false;
+        }
+        ids.push_back(id);
+    }
+    return true;
+}
+
+// Undo the byte shuffle of `n` elements of `size` bytes.
+void unshuffle(std::vector<uint8_t> &v, int size)
+{
+    const size_t n = v.size() / (size_t) size;
+    std::vector<uint8_t> out(v.size());
+    for (size_t i = 0; i < n; i++)
+        for (int b = 0; b < size; b++)
+            out[i * size + b] = v[(size_t) b * n + i];
+    v.swap(out);
+}
+
+struct ChunkInfo {
+    int nd;                   // dataset rank
+    std::vector<uint64_t> cd; // chunk dims
+    std::vector<int> filters;
+    int elem;
+};
+
+// Walk a version-1 B-tree of chunks (node type 1) and copy every chunk's
+// elements into `dst` (row-major, dims `dims`).
+bool read_chunks(const Buf &f, uint64_t addr, const ChunkInfo &ci, const std::vector<uint64_t> &dims,
+                 uint8_t *dst, std::string &err, int depth = 0)
+{
+    if (depth > 32 || !f.in(addr, 24) || memcmp(&f.b[addr], "TREE", 4) != 0 || f.b[addr + 4] != 1) {
+        err = "bad chunk B-tree";
+        return false;
+    }
+    const int level = f.b[addr + 5];
+    const int used = (int) f.u(addr + 6, 2);
+    const int nd = ci.nd;
+    const uint64_t ks = 8 + 8 * (uint64_t) (nd + 1);  // size, filter mask, nd + 1 offsets
+    uint64_t p = addr + 24;
+    uint64_t chunk_elems = 1;
+    for (int d = 0; d < nd; d++)
+        chunk_elems *= ci.cd[d];
+    const uint64_t chunk_bytes = chunk_elems * (uint64_t) ci.elem;
+    for (int i = 0; i < used; i++) {
+        if (!f.in(p, ks + 8)) {
+            err = "truncated chunk B-tree";
+            return false;
+        }
+        const uint64_t csz = f.u(p, 4);
+        const uint32_t mask = (uint32_t) f.u(p + 4, 4);
+        std::vector<uint64_t> off(nd);
+        for (int d = 0; d < nd; d++)
+            off[d] = f.u(p + 8 + 8 * (uint64_t) d, 8);
+        const uint64_t child = f.u(p + ks, 8);
+        p += ks + 8;
+        if (level > 0) {
+            if (!read_chunks(f, child, ci, dims, dst, err, depth + 1))
+                return false;
+            continue;
+        }
+        if (!f.in(child, csz)) {
+            err = "chunk extends past the end of the file";
+            return false;
+        }
+        std::vector<uint8_t> raw(f.b.begin() + child, f.b.begin() + child + csz);
+        // filters are undone in reverse order; a set mask bit skips that filter
+        for (int j = (int) ci.filters.size() - 1; j >= 0; j--) {
+            if (mask & (1u << j))
+                continue;
+            if (ci.filters[j] == 1) {
+                std::vector<uint8_t> out(chunk_bytes);
+                uLongf n = (uLongf) chunk_bytes;
+                if (uncompress(out.data(), &n, raw.data(), (uLong) raw.size()) != Z_OK ||
+                    n != chunk_bytes) {
+                    err = "deflate chunk does not inflate to its size";
+                    return false;
+                }
+                raw.swap(out);
+            } else if (ci.filters[j] == 2) {
+                unshuffle(raw, ci.elem);
+            } else {
+                err = "unsupported filter " + std::to_string(ci.filters[j]);
+                return false;
+            }
+        }
+        if (raw.size() != chunk_bytes) {
+            err = "chunk has the wrong size";
+            return false;
+        }
+        // copy the part of the chunk inside the dataset, row by row of the last dimension
+        std::vector<uint64_t> idx(nd, 0);
+        const uint64_t last = ci.cd[nd - 1];
+        for (uint64_t r = 0; r < chunk_elems / last; r++) {
+            uint64_t rem = r;
+            bool inside = true;
+            uint64_t at = 0;
+            for (int d = nd - 2; d >= 0; d--) {
+                idx[d] = rem % ci.cd[d];
+                rem /= ci.cd[d];
+            }
+            for (int d = 0; d < nd - 1; d++) {
+                const uint64_t g = off[d] + idx[d];
+                if (g >= dims[d])
+                    inside = false;
+                at = at * dims[d] + g;
+            }
+            if (!inside || off[nd - 1] >= dims[nd - 1])
+                continue;
+            const uint64_t n = std::min<uint64_t>(last, dims[nd - 1] - off[nd - 1]);
+            at = at * dims[nd - 1] + off[nd - 1];
+            memcpy(dst + at * ci.elem, raw.data() + r * last * ci.elem, n * ci.elem);
+        }
+    }
+    return true;
+}
+
 }  // namespace
 
 bool read_file(const std::string &path, std::map<std::string, Dataset> &out, std::string &err)
@@ -129,7 +291,7 @@ bool read_file(const std::string &path, std::map<std::string, Dataset> &out, std
         return false;
     uint64_t btree = UNDEF, heap = UNDEF;
     for (const Msg &m : msgs)
-        if (m.type == 0x11) {
+        if (m.type == 0x11 && m.size >= 16) {
             btree = f.u(m.off, 8);
             heap = f.u(m.off + 8, 8);
         }
@@ -144,22 +306,41 @@ bool read_file(const std::string &path, std::map<std::string, Dataset> &out, std
     for (auto &e : ents) {
         if (e.first >= heap_size || !f.in(heap_data + e.first, 1))
             continue;
-        std::string name((const char *) &f.b[heap_data + e.first]);
+        const char *nm = (const char *) &f.b[heap_data + e.first];
+        const uint64_t room = std::min<uint64_t>(heap_size - e.first, f.b.size() - (heap_data + e.first));
+        const size_t nlen = strnlen(nm, (size_t) room);
+        if (nlen == room)
+            continue;  // unterminated name
+        std::string name(nm, nlen);
         std::vector<Msg> dm;
         if (!header_messages(f, e.second, dm, err))
             return false;
         Dataset ds;
-        int cls = -1, size = 0;
-        bool is_signed = true, have_space = false, have_layout = false;
+        int cls = -1, size = 0, layout = -1;
+        bool is_signed = true, have_space = false;
         uint64_t data_addr = UNDEF, data_size = 0;
+        ChunkInfo ci{};
+        const Msg *pipeline = nullptr;
         for (const Msg &m : dm) {
             if (m.type == 0x1) {
+                if (m.size < 8) {
+                    err = "truncated dataspace of " + name;
+                    return false;
+                }
                 const int ver = f.b[m.off], nd = f.b[m.off + 1];
                 const uint64_t d0 = m.off + (ver == 1 ? 8 : 4);
+                if (d0 + 8 * (uint64_t) nd > m.off + m.size || !f.in(d0, 8 * (uint64_t) nd)) {
+                    err = "truncated dataspace of " + name;
+                    return false;
+                }
                 for (int i = 0; i < nd; i++)
                     ds.dims.push_back(f.u(d0 + 8 * (uint64_t) i, 8));
                 have_space = true;
             } else if (m.type == 0x3) {
+                if (m.size < 8) {
+                    err = "truncated datatype of " + name;
+                    return false;
+                }
                 cls = f.b[m.off] & 0x0f;
                 size = (int) f.u(m.off + 4, 4);
                 if (cls == 0)
@@ -168,26 +349,72 @@ bool read_file(const std::string &path, std::map<std::string, Dataset> &out, std
                     err = "big-endian datasets are not supported (" + name + ")";
                     return false;
                 }
+            } else if (m.type == 0xB) {
+                pipeline = &m;
             } else if (m.type == 0x8) {
-                if (f.b[m.off] != 3 || f.b[m.off + 1] != 1)
-                    continue;  // not contiguous: skipped below
-                data_addr = f.u(m.off + 2, 8);
-                data_size = f.u(m.off + 10, 8);
-                have_layout = true;
+                if (m.size < 2 || f.b[m.off] != 3)
+                    continue;  // only layout message version 3
+                layout = f.b[m.off + 1];
+                if (layout == 1 && m.size >= 18) {  // contiguous: address, size
+                    data_addr = f.u(m.off + 2, 8);
+                    data_size = f.u(m.off + 10, 8);
+                } else if (layout == 0 && m.size >= 4) {  // compact: size, raw data
+                    data_size = f.u(m.off + 2, 2);
+                    if (4 + data_size > m.size) {
+                        err = "truncated compact data of " + name;
+                        return false;
+                    }
+                    data_addr = m.off + 4;
+                } else if (layout == 2 && m.size >= 3) {  // chunked: rank + 1, B-tree, dims
+                    const int cnd = f.b[m.off + 2];
+                    if (cnd < 2 || 11 + 4 * (uint64_t) cnd > m.size) {
+                        err = "truncated chunked layout of " + name;
+                        return false;
+                    }
+                    data_addr = f.u(m.off + 3, 8);
+                    ci.nd = cnd - 1;
+                    for (int i = 0; i < cnd; i++)
+                        ci.cd.push_back(f.u(m.off + 11 + 4 * (uint64_t) i, 4));
+                    ci.elem = (int) ci.cd.back();
+                    ci.cd.pop_back();
+                } else {
+                    layout = -1;
+                }
             }
         }
-        if (!have_space || !have_layout || cls < 0)
-            continue;  // groups, chunked or compact datasets are not read
+        if (!have_space || layout < 0 || cls < 0)
+            continue;  // groups, external or virtual layouts are not read
+        if (!(cls == 1 && (size == 8 || size == 4)) && !(cls == 0 && (size == 4 || size == 8)))
+            continue;
         uint64_t count = 1;
         for (uint64_t d : ds.dims)
             count *= d;
-        if (data_addr == UNDEF) {
+        std::vector<uint8_t> chunked;
+        if (layout == 2) {
+            if ((size_t) ci.nd != ds.dims.size() || ci.elem != size) {
+                err = "chunk shape of " + name + " does not match its dataspace";
+                return false;
+            }
+            for (uint64_t c : ci.cd)
+                if (c == 0) {
+                    err = "zero chunk dimension in " + name;
+                    return false;
+                }
+            if (pipeline && !filter_pipeline(f, *pipeline, ci.filters, err))
+                return false;
+            chunked.assign(count * (uint64_t) size, 0);  // unwritten chunks read as 0
+            if (data_addr != UNDEF && count &&
+                !read_chunks(f, data_addr, ci, ds.dims, chunked.data(), err)) {
+                err += " (" + name + ")";
+                return false;
+            }
+        } else if (data_addr == UNDEF) {
             count = 0;  // never written: empty
         } else if (!f.in(data_addr, count * (uint64_t) size) || data_size < count * (uint64_t) size) {
             err = "dataset " + name + " extends past the end of the file";
             return false;
         }
-        const uint8_t *src = count ? &f.b[data_addr] : nullptr;
+        const uint8_t *src = !count ? nullptr : (layout == 2 ? chunked.data() : &f.b[data_addr]);
         if (cls == 1 && (size == 8 || size == 4)) {
             ds.f64.resize(count);
             for (uint64_t i = 0; i < count; i++) {

@@ -5,10 +5,17 @@
 // every dataset is created with default properties, i.e. a contiguous
 // layout, 2-D matrices row-major and scalars as one-element 1-D datasets,
 // all in the root group.  No HDF5 library is available here, so this file
-// reads and writes exactly that subset of the format:
+// reads and writes that part of the format:
 //   superblock version 0, a root group held in a symbol table (version-1
-//   B-tree and local heap), version-1 object headers, contiguous datasets of
+//   B-tree and local heap), version-1 object headers, datasets of
 //   little-endian IEEE float64 / float32 and signed int32 / int64.
+// The reader also takes compact and chunked datasets (layout message
+// version 3; chunks indexed by a version-1 B-tree), with the deflate (zlib)
+// and shuffle filters, as HDF5 tools such as h5repack write them and as the
+// reference's sample output data/Oil.out.h5 is stored; the writer writes
+// contiguous datasets only.  Every offset read from a file is checked
+// against the file's size: a truncated or malformed file gives an error,
+// never a read outside the buffer.
 // Files written here open with any HDF5 reader; files written by the
 // reference (HDF5 1.8 defaults) open here.
 #pragma once
@@ -27,8 +34,9 @@ struct Dataset {
     bool is_int = false;
 };
 
-// Read every contiguous dataset of the root group.  Returns false and fills
-// `err` when the file uses a feature outside the subset above.
+// Read every dataset of the root group (contiguous, compact or chunked).
+// Returns false and fills `err` when the file uses a feature outside the
+// subset above or is malformed.
 bool read_file(const std::string &path, std::map<std::string, Dataset> &out, std::string &err);
 
 class Writer {

@@ -4,10 +4,11 @@ Reads ``data/Oil.h5`` (the input the reference ships) and ``data/Oil.out.h5``
 (an output file the reference wrote for it: a converged DA-GTM state with
 K = 125 (5^3, L = 3), M = 8 (2^3) RBF centres plus bias, N = 1000, D = 12)
 from a jychoi-hpc/da-gtm checkout and stores the arrays the parity tests
-need in ``oil_golden.npz``; ``oil_input.h5`` is a byte copy of the input
-file, for the command-line driver's HDF5 reader.  The reference tree is not available where the
-GPU tests run, so only the .npz travels; this script is kept beside it so
-the fixture can be regenerated:
+need in ``oil_golden.npz``; ``oil_input.h5`` and ``oil_output.h5`` are byte
+copies of the two files, for the command-line driver's HDF5 reader (the
+output file's datasets are chunked and deflate-compressed).  The reference
+tree is not available where the GPU tests run, so only these fixtures
+travel; this script is kept beside them so they can be regenerated:
 
     python tests/golden/make_golden.py /path/to/da-gtm/data
 
@@ -175,9 +176,12 @@ def main(data_dir):
     # the input file itself (written by the HDF5 library the reference links),
     # the fixture of the command-line driver's reader
     shutil.copyfile(os.path.join(data_dir, "Oil.h5"), os.path.join(here, "oil_input.h5"))
+    shutil.copyfile(os.path.join(data_dir, "Oil.out.h5"), os.path.join(here, "oil_output.h5"))
     for k, v in g.items():
         print(k, v.shape, v.dtype)
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/data")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py <the reference checkout's data directory>")
+    main(sys.argv[1])

@@ -37,7 +37,8 @@ def cpu_driver(tmp_path_factory, orc):
     exe = str(d / "dagtm")
     srcs = sorted(glob.glob(os.path.join(ROOT, "da-gtm_gb300", "driver", "*.cc")))
     subprocess.check_call(["g++", "-O2", "-std=c++17", "-I" + inc] + srcs +
-                          ["-L" + str(d), "-ldagtm_gb300", "-Wl,-rpath," + str(d), "-o", exe])
+                          ["-L" + str(d), "-ldagtm_gb300", "-lz", "-Wl,-rpath," + str(d), "-o",
+                           exe])
     return exe
 
 
