@@ -34,7 +34,8 @@ ERRORS = {1: "EINVAL", 2: "ECUDA", 3: "ENOTSPD", 4: "ENONFINITE", 5: "ETIMEOUT",
 # every symbol the header declares (checked by the CPU tests)
 ABI_SYMBOLS = ("dgtm_version", "dgtm_last_error_string", "dgtm_ctx_create", "dgtm_ctx_destroy",
                "dgtm_set_solver", "dgtm_set_Y", "dgtm_get_Y", "dgtm_get_W", "dgtm_estep",
-               "dgtm_mstep", "dgtm_get_stats", "dgtm_map", "dgtm_get_R_block", "dgtm_next_ctemp",
+               "dgtm_mstep", "dgtm_get_stats", "dgtm_map", "dgtm_get_R_block", "dgtm_map_rd",
+               "dgtm_get_RD_block", "dgtm_next_ctemp",
                "dgtm_next_ctemp_k", "dgtm_set_timing",
                "dgtm_reset_timing", "dgtm_get_timing", "dgtm_get_stream", "dgtm_selftest",
                "dgtm_fe_workspace_size", "dgtm_fe_forward", "dgtm_fe_backward",
@@ -77,6 +78,8 @@ def load_library(path: str = LIB_PATH):
         "dgtm_get_stats": (i, [vp, _dp, _dp, i]),
         "dgtm_map": (i, [vp, _dp, i, _dp, i]),
         "dgtm_get_R_block": (i, [vp, i, i, i, i, _dp, i]),
+        "dgtm_map_rd": (i, [vp, _dp, i, _dp, i]),
+        "dgtm_get_RD_block": (i, [vp, i, i, i, i, _dp, i]),
         "dgtm_next_ctemp": (i, [vp, d, d, d, _dp, _dp]),
         "dgtm_next_ctemp_k": (i, [vp, d, d, d, _dp, _dp, _dp]),
         "dgtm_set_timing": (i, [vp, i]),
@@ -272,6 +275,21 @@ class Context:
     def R_block(self, k0: int, nk: int, n0: int, nn: int) -> np.ndarray:
         R = np.empty((nk, nn))
         _check(load_library().dgtm_get_R_block(self._h, k0, nk, n0, nn, _p(R), nn))
+        return R
+
+    def map_rd(self, X) -> np.ndarray:
+        """(R o D)^T X after an M-step: the reference's MAP when it stops on
+        its iteration cap (R of the last E-step times the squared distances
+        to the new centres)."""
+        X = _f64(X)
+        L = X.shape[1]
+        M = np.empty((self.N, L))
+        _check(load_library().dgtm_map_rd(self._h, _p(X), L, _p(M), L))
+        return M
+
+    def RD_block(self, k0: int, nk: int, n0: int, nn: int) -> np.ndarray:
+        R = np.empty((nk, nn))
+        _check(load_library().dgtm_get_RD_block(self._h, k0, nk, n0, nn, _p(R), nn))
         return R
 
     def next_ctemp(self, temp: float, beta: float, eps: float, gg=None,

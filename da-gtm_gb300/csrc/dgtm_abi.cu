@@ -13,6 +13,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <utility>
 #include <vector>
 
 // Row-block copy.  When both pitches equal the row width the block is
@@ -57,6 +58,8 @@ struct dgtm_ctx {
     double *FI;        // K x M1
     float2 *FIp;       // K x M1 FP32 (hi, lo) pairs for update_y (FP32 / split forms)
     double *Y64;       // K x D (master copy of the centres)
+    double *Yprev;     // K x D: the centres before the last M-step (swapped, not copied)
+    double *yyprev;    // K
     float *Y32;        // K x D (FP32 form)
     double *yy;        // K
     double *W;         // M1 x D
@@ -82,6 +85,7 @@ struct dgtm_ctx {
     long long launches[DGTM_NPHASES], calls[DGTM_NPHASES];
     // state
     int stats_valid;   // colstat belongs to the current Y
+    int prev_valid;    // colstat belongs to Yprev (an M-step since the last E-step)
     int rt_valid;      // G / RT computed
     int w_valid;
     int dropped;       // pivots dropped by the last Cholesky solve
@@ -191,7 +195,8 @@ void free_ctx(dgtm_ctx *c)
 {
     if (!c)
         return;
-    void *ptrs[] = {c->T64, c->T32, c->tt, c->FI, c->FIp, c->Y64, c->Y32, c->yy, c->W, c->colstat,
+    void *ptrs[] = {c->T64, c->T32, c->tt, c->FI, c->FIp, c->Y64, c->Yprev, c->yyprev, c->Y32, c->yy,
+                    c->W, c->colstat,
                     c->part, c->Gpart, c->RTpart, c->G, c->RT, c->A, c->B, c->work, c->bterm, c->abpart,
                     c->scal, c->flag};
     for (void *p : ptrs)
@@ -285,6 +290,8 @@ int dgtm_ctx_create(int N, int D, int K, int M1, const double *T, int ldT, const
     CK(dev_alloc(&c->FI, (size_t) K * M1));
     CK(dev_alloc(&c->Y64, KD));
     CK(dev_alloc(&c->yy, K));
+    CK(dev_alloc(&c->Yprev, KD));
+    CK(dev_alloc(&c->yyprev, K));
     CK(dev_alloc(&c->W, (size_t) M1 * D));
     CK(dev_alloc(&c->colstat, N));
     CK(dev_alloc(&c->G, K));
@@ -379,6 +386,7 @@ int dgtm_set_Y(dgtm_ctx *ctx, const double *Y, int ldY)
     int nl = 0;
     DGTM_TRY(refresh_y_copies(ctx, &nl));
     ctx->stats_valid = 0;
+    ctx->prev_valid = 0;
     ctx->rt_valid = 0;
     return sync_and_check(ctx);
 }
@@ -459,6 +467,7 @@ int dgtm_estep(dgtm_ctx *ctx, double beta, int isDA, double temp, double *llh, d
         *nfree = q_free;
     ctx->beta = beta;
     ctx->temp = temp;
+    ctx->prev_valid = 0;
     ctx->isDA = isDA;
     ctx->stats_valid = 1;
     ctx->rt_valid = 0;
@@ -514,6 +523,10 @@ int dgtm_mstep(dgtm_ctx *ctx, double *W, int ldW, double *Y, int ldY, double *be
         cp.Y32 = ctx->Y32;
     else if (ctx->precision == DGTM_BF16X3)
         tc_y_copies(ctx->tc, &cp);
+    // the new centres go to the spare buffers, which then become the current
+    // ones: the centres of the last E-step stay on the device (dgtm_map_rd)
+    std::swap(ctx->Y64, ctx->Yprev);
+    std::swap(ctx->yy, ctx->yyprev);
     DGTM_TRY(launch_update_y(ctx->FI, ctx->FIp, ctx->W, ctx->G, ctx->RT, K, M1, D, ctx->Y64,
                              ctx->yy, ctx->bterm, cp, ctx->flag + 2, ctx->stream));
     DGTM_TRY(launch_sum_ratio(ctx->bterm, K, ctx->sum_tt, (double) ((long long) N * D),
@@ -537,6 +550,7 @@ int dgtm_mstep(dgtm_ctx *ctx, double *W, int ldW, double *Y, int ldY, double *be
     if (ctx->tc)
         DGTM_TRY(tc_check_status(ctx->tc));
     ctx->stats_valid = 0;
+    ctx->prev_valid = 1;
     ctx->rt_valid = 1;
     ctx->w_valid = 1;
     ctx->dropped = ctx->hflag[1];
@@ -626,11 +640,21 @@ int dgtm_get_stream(dgtm_ctx *ctx, void **stream)
     return DGTM_OK;
 }
 
-int dgtm_map(dgtm_ctx *ctx, const double *X, int L, double *M, int ldM)
+}  // extern "C"
+
+namespace {
+
+// M = R^T X, or with rd (R o D)^T X: R of the last E-step, which an M-step has
+// followed, times the squared distances to the new centres.
+int map_impl(dgtm_ctx *ctx, const double *X, int L, double *M, int ldM, bool rd)
 {
     DGTM_TRY(check_ctx(ctx));
-    if (!ctx->stats_valid) {
+    if (!rd && !ctx->stats_valid) {
         set_error(DGTM_ESTATE, "dgtm_map needs an E-step on the current centres first");
+        return DGTM_ESTATE;
+    }
+    if (rd && !ctx->prev_valid) {
+        set_error(DGTM_ESTATE, "dgtm_map_rd needs an M-step after the last E-step");
         return DGTM_ESTATE;
     }
     if (!X || !M || L < 1 || L > 8 || ldM < L) {
@@ -649,8 +673,12 @@ int dgtm_map(dgtm_ctx *ctx, const double *X, int L, double *M, int ldM)
     cudaError_t e = cudaMemcpyAsync(dX, X, sizeof(double) * ctx->K * L, cudaMemcpyHostToDevice,
                                     ctx->stream);
     if (e == cudaSuccess) {
-        r = launch_map(ctx->T64, ctx->Y64, ctx->tt, ctx->yy, ctx->colstat, ctx->N, ctx->D, ctx->K,
-                       c, dX, L, dM, ctx->stream);
+        if (rd)
+            r = launch_map(ctx->T64, ctx->Yprev, ctx->tt, ctx->yyprev, ctx->colstat, ctx->N, ctx->D,
+                           ctx->K, c, dX, L, dM, ctx->stream, ctx->Y64, ctx->yy);
+        else
+            r = launch_map(ctx->T64, ctx->Y64, ctx->tt, ctx->yy, ctx->colstat, ctx->N, ctx->D,
+                           ctx->K, c, dX, L, dM, ctx->stream);
         if (r == DGTM_OK)
             e = copy_rows(M, sizeof(double) * (size_t) ldM, dM, sizeof(double) * L,
                                   sizeof(double) * L, ctx->N, cudaMemcpyDeviceToHost,
@@ -665,6 +693,62 @@ int dgtm_map(dgtm_ctx *ctx, const double *X, int L, double *M, int ldM)
         return DGTM_ECUDA;
     }
     return r;
+}
+
+int r_block_impl(dgtm_ctx *ctx, int k0, int nk, int n0, int nn, double *R, int ldR, bool rd)
+{
+    DGTM_TRY(check_ctx(ctx));
+    if (!rd && !ctx->stats_valid) {
+        set_error(DGTM_ESTATE, "dgtm_get_R_block needs an E-step on the current centres first");
+        return DGTM_ESTATE;
+    }
+    if (rd && !ctx->prev_valid) {
+        set_error(DGTM_ESTATE, "dgtm_get_RD_block needs an M-step after the last E-step");
+        return DGTM_ESTATE;
+    }
+    if (!R || k0 < 0 || n0 < 0 || nk < 1 || nn < 1 || k0 + nk > ctx->K || n0 + nn > ctx->N ||
+        ldR < nn) {
+        set_error(DGTM_EINVAL, "bad R block k0=%d nk=%d n0=%d nn=%d ldR=%d", k0, nk, n0, nn, ldR);
+        return DGTM_EINVAL;
+    }
+    const double c = ctx->isDA ? ctx->beta / (2.0 * ctx->temp) : ctx->beta / 2.0;
+    double *dR = nullptr;
+    DGTM_TRY(dev_alloc(&dR, (size_t) nk * nn));
+    int r = rd ? launch_r_block(ctx->T64, ctx->Yprev, ctx->tt, ctx->yyprev, ctx->colstat, ctx->D,
+                                ctx->K, c, k0, nk, n0, nn, dR, ctx->stream, ctx->Y64, ctx->yy)
+               : launch_r_block(ctx->T64, ctx->Y64, ctx->tt, ctx->yy, ctx->colstat, ctx->D, ctx->K,
+                                c, k0, nk, n0, nn, dR, ctx->stream);
+    cudaError_t e = cudaSuccess;
+    if (r == DGTM_OK)
+        e = copy_rows(R, sizeof(double) * (size_t) ldR, dR, sizeof(double) * nn,
+                              sizeof(double) * nn, nk, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(ctx->stream);
+    cudaFree(dR);
+    if (e != cudaSuccess) {
+        set_error(DGTM_ECUDA, "dgtm_get_R_block: %s", cudaGetErrorString(e));
+        return DGTM_ECUDA;
+    }
+    return r;
+}
+
+}  // namespace
+
+extern "C" {
+
+int dgtm_map(dgtm_ctx *ctx, const double *X, int L, double *M, int ldM)
+{
+    return map_impl(ctx, X, L, M, ldM, false);
+}
+
+int dgtm_map_rd(dgtm_ctx *ctx, const double *X, int L, double *M, int ldM)
+{
+    return map_impl(ctx, X, L, M, ldM, true);
+}
+
+int dgtm_get_RD_block(dgtm_ctx *ctx, int k0, int nk, int n0, int nn, double *R, int ldR)
+{
+    return r_block_impl(ctx, k0, nk, n0, nn, R, ldR, true);
 }
 
 int dgtm_next_ctemp(dgtm_ctx *ctx, double temp, double beta, double eps, const double *gg,
@@ -755,33 +839,7 @@ int dgtm_next_ctemp_k(dgtm_ctx *ctx, double temp, double beta, double eps, const
 
 int dgtm_get_R_block(dgtm_ctx *ctx, int k0, int nk, int n0, int nn, double *R, int ldR)
 {
-    DGTM_TRY(check_ctx(ctx));
-    if (!ctx->stats_valid) {
-        set_error(DGTM_ESTATE, "dgtm_get_R_block needs an E-step on the current centres first");
-        return DGTM_ESTATE;
-    }
-    if (!R || k0 < 0 || n0 < 0 || nk < 1 || nn < 1 || k0 + nk > ctx->K || n0 + nn > ctx->N ||
-        ldR < nn) {
-        set_error(DGTM_EINVAL, "bad R block k0=%d nk=%d n0=%d nn=%d ldR=%d", k0, nk, n0, nn, ldR);
-        return DGTM_EINVAL;
-    }
-    const double c = ctx->isDA ? ctx->beta / (2.0 * ctx->temp) : ctx->beta / 2.0;
-    double *dR = nullptr;
-    DGTM_TRY(dev_alloc(&dR, (size_t) nk * nn));
-    int r = launch_r_block(ctx->T64, ctx->Y64, ctx->tt, ctx->yy, ctx->colstat, ctx->D, ctx->K, c,
-                           k0, nk, n0, nn, dR, ctx->stream);
-    cudaError_t e = cudaSuccess;
-    if (r == DGTM_OK)
-        e = copy_rows(R, sizeof(double) * (size_t) ldR, dR, sizeof(double) * nn,
-                              sizeof(double) * nn, nk, cudaMemcpyDeviceToHost, ctx->stream);
-    if (e == cudaSuccess)
-        e = cudaStreamSynchronize(ctx->stream);
-    cudaFree(dR);
-    if (e != cudaSuccess) {
-        set_error(DGTM_ECUDA, "dgtm_get_R_block: %s", cudaGetErrorString(e));
-        return DGTM_ECUDA;
-    }
-    return r;
+    return r_block_impl(ctx, k0, nk, n0, nn, R, ldR, false);
 }
 
 }  // extern "C"

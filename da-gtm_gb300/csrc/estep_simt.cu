@@ -398,6 +398,9 @@ __global__ void __launch_bounds__(NT) pass2_simt_kernel(Pass2Args<F> a)
 // MAP projection M = R^T X and explicit blocks of R (FP64, from the column
 // statistics of the last E-step)
 // ---------------------------------------------------------------------------
+// RD: the weights are R_kn d'_kn with d' the squared distance to a second set
+// of centres Y2 (|y2|^2 in yy2): the reference's R o D after its beta update.
+template <bool RD>
 __global__ void __launch_bounds__(NT) map_kernel(const double *__restrict__ T,
                                                  const double *__restrict__ Y,
                                                  const double *__restrict__ tt,
@@ -405,12 +408,15 @@ __global__ void __launch_bounds__(NT) map_kernel(const double *__restrict__ T,
                                                  const double2 *__restrict__ colstat, int N,
                                                  int D, int K, double c,
                                                  const double *__restrict__ X, int L,
+                                                 const double *__restrict__ Y2,
+                                                 const double *__restrict__ yy2,
                                                  double *__restrict__ Mout)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int ldt = D | 1;
     double *Tt = reinterpret_cast<double *>(smem_raw);
     double(*Ys)[BKT + 1] = reinterpret_cast<double(*)[BKT + 1]>(Tt + BN * ldt);
+    double(*Ys2)[BKT + 1] = Ys + DC;  // RD only
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
     const int n0 = blockIdx.x * BN;
     for (int idx = threadIdx.x; idx < BN * D; idx += NT) {
@@ -432,30 +438,37 @@ __global__ void __launch_bounds__(NT) map_kernel(const double *__restrict__ T,
     }
     const double invK = 1.0 / (double) K;
     for (int k0 = 0; k0 < K; k0 += BKT) {
-        double acc[4][4];
+        double acc[4][4], acc2[4][4];
 #pragma unroll
         for (int i = 0; i < 4; i++)
 #pragma unroll
             for (int j = 0; j < 4; j++)
-                acc[i][j] = 0.0;
+                acc[i][j] = acc2[i][j] = 0.0;
         for (int d0 = 0; d0 < D; d0 += DC) {
             __syncthreads();
             load_y_slice<double>(Ys, Y, K, D, k0, d0);
+            if (RD)
+                load_y_slice<double>(Ys2, Y2, K, D, k0, d0);
             __syncthreads();
             const int dl = min(DC, D - d0);
             for (int dd = 0; dd < dl; dd++) {
-                double tv[4], yv[4];
+                double tv[4], yv[4], yv2[4];
 #pragma unroll
                 for (int i = 0; i < 4; i++)
                     tv[i] = Tt[(ty + 16 * i) * ldt + d0 + dd];
 #pragma unroll
-                for (int j = 0; j < 4; j++)
+                for (int j = 0; j < 4; j++) {
                     yv[j] = Ys[dd][tx + 16 * j];
+                    yv2[j] = RD ? Ys2[dd][tx + 16 * j] : 0.0;
+                }
 #pragma unroll
                 for (int i = 0; i < 4; i++)
 #pragma unroll
-                    for (int j = 0; j < 4; j++)
+                    for (int j = 0; j < 4; j++) {
                         acc[i][j] += tv[i] * yv[j];
+                        if (RD)
+                            acc2[i][j] += tv[i] * yv2[j];
+                    }
             }
         }
 #pragma unroll
@@ -473,6 +486,8 @@ __global__ void __launch_bounds__(NT) map_kernel(const double *__restrict__ T,
                     const double dd = ((-2.0 * acc[i][j]) + yyk) + ttn[i];
                     r = exp(-c * (dd - dmn[i]) - lsn[i]);
                 }
+                if (RD)  // the reference's operation order: -2 y.t, + |y|^2, + |t|^2
+                    r *= ((-2.0 * acc2[i][j]) + yy2[gk]) + ttn[i];
 #pragma unroll
                 for (int l = 0; l < 8; l++)
                     if (l < L)
@@ -497,7 +512,8 @@ __global__ void __launch_bounds__(NT) map_kernel(const double *__restrict__ T,
 __global__ void r_block_kernel(const double *__restrict__ T, const double *__restrict__ Y,
                                const double *__restrict__ tt, const double *__restrict__ yy,
                                const double2 *__restrict__ colstat, int D, int K, double c,
-                               int k0, int nk, int n0, int nn, double *__restrict__ R)
+                               int k0, int nk, int n0, int nn, const double *__restrict__ Y2,
+                               const double *__restrict__ yy2, double *__restrict__ R)
 {
     const size_t total = (size_t) nk * nn;
     for (size_t i = blockIdx.x * (size_t) blockDim.x + threadIdx.x; i < total;
@@ -514,31 +530,46 @@ __global__ void r_block_kernel(const double *__restrict__ T, const double *__res
             const double dd = ((-2.0 * dot) + yy[k]) + tt[n];
             r = exp(-c * (dd - cs.x) - cs.y);
         }
+        if (Y2) {
+            double dot = 0.0;
+            for (int d = 0; d < D; d++)
+                dot += Y2[(size_t) k * D + d] * T[(size_t) n * D + d];
+            r *= ((-2.0 * dot) + yy2[k]) + tt[n];
+        }
         R[i] = r;
     }
 }
 
 int launch_map(const double *T, const double *Y, const double *tt, const double *yy,
                const double2 *colstat, int N, int D, int K, double c, const double *X, int L,
-               double *M, cudaStream_t s)
+               double *M, cudaStream_t s, const double *Y2, const double *yy2)
 {
-    const size_t smem = sizeof(double) * ((size_t) BN * (D | 1) + (size_t) DC * (BKT + 1));
-    DGTM_CUDA_TRY(cudaFuncSetAttribute(map_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int) smem));
-    map_kernel<<<ceil_div(N, BN), NT, smem, s>>>(T, Y, tt, yy, colstat, N, D, K, c, X, L, M);
+    const size_t smem =
+        sizeof(double) * ((size_t) BN * (D | 1) + (size_t) (Y2 ? 2 : 1) * DC * (BKT + 1));
+    if (Y2) {
+        DGTM_CUDA_TRY(cudaFuncSetAttribute(map_kernel<true>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem));
+        map_kernel<true><<<ceil_div(N, BN), NT, smem, s>>>(T, Y, tt, yy, colstat, N, D, K, c, X,
+                                                            L, Y2, yy2, M);
+    } else {
+        DGTM_CUDA_TRY(cudaFuncSetAttribute(map_kernel<false>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem));
+        map_kernel<false><<<ceil_div(N, BN), NT, smem, s>>>(T, Y, tt, yy, colstat, N, D, K, c, X,
+                                                             L, nullptr, nullptr, M);
+    }
     DGTM_CUDA_TRY(cudaGetLastError());
     return DGTM_OK;
 }
 
 int launch_r_block(const double *T, const double *Y, const double *tt, const double *yy,
                    const double2 *colstat, int D, int K, double c, int k0, int nk, int n0, int nn,
-                   double *R, cudaStream_t s)
+                   double *R, cudaStream_t s, const double *Y2, const double *yy2)
 {
     size_t blocks = ((size_t) nk * nn + 255) / 256;
     if (blocks > 8192)
         blocks = 8192;
     r_block_kernel<<<(unsigned) blocks, 256, 0, s>>>(T, Y, tt, yy, colstat, D, K, c, k0, nk, n0,
-                                                    nn, R);
+                                                    nn, Y2, yy2, R);
     DGTM_CUDA_TRY(cudaGetLastError());
     return DGTM_OK;
 }

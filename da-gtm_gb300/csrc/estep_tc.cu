@@ -1253,15 +1253,23 @@ P3Kernel pass3_for(int np, int kl, int nt)
 // ---------------------------------------------------------------------------
 // operand preparation and the slot reduction
 // ---------------------------------------------------------------------------
-__global__ void t_exact_kernel(const double *__restrict__ T64, size_t n, int *inexact)
+// flags |= 1 when a value is not exactly a BF16 number, |= 2 when a value is
+// neither 0 nor 1
+__global__ void t_class_kernel(const double *__restrict__ T64, size_t n, int *flags)
 {
+    int f = 0;
     for (size_t i = blockIdx.x * (size_t) blockDim.x + threadIdx.x; i < n;
          i += (size_t) gridDim.x * blockDim.x) {
         const double t = T64[i];
         const double h = (double) __bfloat162float(__float2bfloat16_rn((float) t));
         if (h != t)
-            atomicExch(inexact, 1);
+            f |= 1;
+        if (t != 0.0 && t != 1.0)
+            f |= 2;
     }
+    f = __reduce_or_sync(0xffffffffu, f);
+    if (f && (threadIdx.x & 31) == 0)
+        atomicOr(flags, f);
 }
 
 // T pieces (nT x Npad x Dp): value pieces, three columns of ones, zero
@@ -1437,6 +1445,7 @@ static int p2_unit_tiles(int ntiles, int ktiles, int grid_max)
 struct TcState {
     int N, D, K, sms;
     int Dp, npanel, Npad, Kpad, nT, ksteps;
+    int binary;  // every data value is 0 or 1
     int nchunk, nstage1, nstage2, nstage3, ntile1, bn2;
     int ntiles2, unit_tiles, units_per_k, nunits, grid2;
     size_t smem1, smem2, smem3;
@@ -1603,7 +1612,7 @@ int tc_create(TcState **out, int N, int D, int K, int sms, const double *T64, co
     if (e == cudaSuccess)
         e = cudaMemsetAsync(st->status, 0, sizeof(int), s);
     if (e == cudaSuccess) {
-        t_exact_kernel<<<grid_for((size_t) N * D), 256, 0, s>>>(T64, (size_t) N * D, st->status);
+        t_class_kernel<<<grid_for((size_t) N * D), 256, 0, s>>>(T64, (size_t) N * D, st->status);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess)
@@ -1614,7 +1623,8 @@ int tc_create(TcState **out, int N, int D, int K, int sms, const double *T64, co
         set_error(DGTM_ECUDA, "tc_create: %s", cudaGetErrorString(e));
         return fail(DGTM_ECUDA);
     }
-    if ((rc = tc_plan(st, N, D, K, sms, (*st->hstatus) ? 2 : 1)) != DGTM_OK)
+    st->binary = (*st->hstatus & 2) == 0;
+    if ((rc = tc_plan(st, N, D, K, sms, (*st->hstatus & 1) ? 2 : 1)) != DGTM_OK)
         return fail(rc);
     const size_t tpl = (size_t) st->Npad * st->Dp, ypl = (size_t) st->Kpad * st->Dp;
     e = cudaMalloc((void **) &st->Tb, sizeof(__nv_bfloat16) * tpl * st->nT);
@@ -1677,7 +1687,7 @@ int tc_prepare_y(TcState *st, const double *Y64, cudaStream_t s)
 int tc_pass1_blocks(const TcState *st) { return st->Npad / (st->ntile1 * P1_TILE); }
 
 int tc_estep(TcState *st, const double *, double c1, double c2, int isDA, double2 *colstat,
-             double *part, cudaStream_t s, int *nlaunch)
+             double *part, cudaStream_t s, int *nlaunch, bool need_llh)
 {
     P1Params p;
     p.N = st->N;
@@ -1694,10 +1704,13 @@ int tc_estep(TcState *st, const double *, double c1, double c2, int isDA, double
     p.ksteps = st->ksteps;
     p.c1 = c1;
     p.c2 = c2;
-    p.c1l = (float) (2.0 * c1 * 1.4426950408889634);
     p.c2l = (float) (2.0 * c2 * 1.4426950408889634);
+    // without the log-likelihood only the sums at `temp` are formed (the
+    // temperature-1 terms are then not meaningful; c1 still drives the
+    // zero-column test)
+    p.c1l = need_llh ? (float) (2.0 * c1 * 1.4426950408889634) : p.c2l;
     p.isDA = isDA;
-    p.two_temps = isDA && (c1 != c2);
+    p.two_temps = need_llh && isDA && (c1 != c2);
     p.Y32 = st->Y32;
     p.T64 = st->T64;
     p.T32 = st->T32;
@@ -1836,8 +1849,9 @@ int tc_fe_estep(const TcFeLayout &L, void *ws, const float *Y, const float *T, i
         Y, K, D, st.Dp, st.Kpad, st.Yb, nullptr);
     DGTM_CUDA_TRY(cudaGetLastError());
     int nl = 0;
-    // tc_estep clears the status word again; a failure of this call shows there
-    return tc_estep(&st, nullptr, c1, c2, 1, colstat, part, s, &nl);
+    // tc_estep clears the status word again; a failure of this call shows
+    // there.  The free energy needs the statistics at `temp` only.
+    return tc_estep(&st, nullptr, c1, c2, 1, colstat, part, s, &nl, false);
 }
 
 int tc_fe_stats(const TcFeLayout &L, void *ws, int N, int K, int D, int sms, double *G,
@@ -1876,6 +1890,24 @@ int tc_fe_rty(const TcFeLayout &L, void *ws, int N, int K, int D, int sms, float
     st.pass3<<<st.Npad / P3_TILE, P3_THREADS, st.smem3, s>>>(st.tmY3, st.tmT1, p);
     DGTM_CUDA_TRY(cudaGetLastError());
     return DGTM_OK;
+}
+
+void tc_view(const TcState *st, TcView *v)
+{
+    v->N = st->N;
+    v->D = st->D;
+    v->K = st->K;
+    v->Dp = st->Dp;
+    v->npanel = st->npanel;
+    v->Npad = st->Npad;
+    v->Kpad = st->Kpad;
+    v->nT = st->nT;
+    v->binary = st->binary;
+    v->ksteps = st->ksteps;
+    v->Tb = st->Tb;
+    v->Yb = st->Yb;
+    v->colq = st->colq;
+    v->status = st->status;
 }
 
 int *tc_fe_status(const TcFeLayout &L, void *ws)

@@ -167,11 +167,11 @@ __global__ void fe_dt_inplace_kernel(const float *__restrict__ T, int N, int D, 
                                      const double *__restrict__ gF, const int *__restrict__ status,
                                      float *__restrict__ dT)
 {
-    const double g = fe_failed(status) ? NAN : (gF ? gF[0] : 1.0);
+    const float gb = (float) (-(fe_failed(status) ? NAN : (gF ? gF[0] : 1.0)) * beta);
     const size_t total = (size_t) N * D;
     for (size_t i = blockIdx.x * (size_t) blockDim.x + threadIdx.x; i < total;
          i += (size_t) gridDim.x * blockDim.x)
-        dT[i] = (float) (-g * beta * ((double) T[i] - (double) dT[i]));
+        dT[i] = gb * (T[i] - dT[i]);
 }
 
 // dbeta = g (N D / (2 beta) - sum R o D / 2), sum R o D = S[0]

@@ -40,13 +40,17 @@ template <typename F>
 int launch_pass2_simt(const Pass2Args<F> &a, int nsplit, cudaStream_t s, bool own = false);
 int pass1_simt_blocks(int N);
 int pass2_simt_ktiles(int K);
-// M = R^T X (N x L, L <= 8) and explicit R blocks, FP64, from the column statistics.
+// M = R^T X (N x L, L <= 8) and explicit R blocks, FP64, from the column
+// statistics.  With Y2 (and its |y|^2 in yy2) every R_kn is multiplied by the
+// squared distance of t_n to the centre k of Y2 (the reference's R o D).
 int launch_map(const double *T, const double *Y, const double *tt, const double *yy,
                const double2 *colstat, int N, int D, int K, double c, const double *X, int L,
-               double *M, cudaStream_t s);
+               double *M, cudaStream_t s, const double *Y2 = nullptr,
+               const double *yy2 = nullptr);
 int launch_r_block(const double *T, const double *Y, const double *tt, const double *yy,
                    const double2 *colstat, int D, int K, double c, int k0, int nk, int n0, int nn,
-                   double *R, cudaStream_t s);
+                   double *R, cudaStream_t s, const double *Y2 = nullptr,
+                   const double *yy2 = nullptr);
 
 // ---- M-step (FP64, all forms) ---------------------------------------------------
 // Sum nsplit slices in a fixed order: G[k] = sum_s Gpart[s][k], RT = sum_s RTpart[s].

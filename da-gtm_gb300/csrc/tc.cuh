@@ -18,9 +18,10 @@ int tc_prepare_y(TcState *st, const double *Y64, cudaStream_t s);
 struct YCopies;
 void tc_y_copies(TcState *st, YCopies *cp);
 // E-step: column statistics (exact-minimum shift, log s_n) and per-block
-// partial sums of the llh / nfree terms.
+// partial sums of the llh / nfree terms (need_llh = false: the nfree terms
+// only, half the exponentials when temp != 1).
 int tc_estep(TcState *st, const double *Y64, double c1, double c2, int isDA, double2 *colstat,
-             double *part, cudaStream_t s, int *nlaunch);
+             double *part, cudaStream_t s, int *nlaunch, bool need_llh = true);
 int tc_pass1_blocks(const TcState *st);
 // Responsibility pass (tensor cores): per-slice partial G and RT.
 int tc_mstep_pass(TcState *st, const double2 *colstat, double c, cudaStream_t s, int *nlaunch);
@@ -54,5 +55,16 @@ int tc_fe_rty(const TcFeLayout &L, void *ws, int N, int K, int D, int sms, float
               cudaStream_t s);
 // The device status word (non-zero: a bounded wait gave up).
 int *tc_fe_status(const TcFeLayout &L, void *ws);
+
+// The split form's device operands as other passes need them.
+struct TcView {
+    int N, D, K, Dp, npanel, Npad, Kpad, nT, ksteps;
+    int binary;           // every data value is 0 or 1
+    const void *Tb;       // nT x Npad x Dp BF16: data pieces, columns D..D+2 = 1
+    const void *Yb;       // 2 x Kpad x Dp BF16: centre pieces, -|y|^2/2 at D..D+2 of hi
+    const float4 *colq;   // Npad: (m, scale, log2 s) of the last E-step
+    int *status;          // bounded-wait status word
+};
+void tc_view(const TcState *st, TcView *v);
 
 }  // namespace dgtm

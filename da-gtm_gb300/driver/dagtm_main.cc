@@ -225,6 +225,7 @@ struct Opts {
                 dM = "M", did = "id", dlb = "lb", dtemp = "temp", diter = "iter", dseed = "seed",
                 dqual = "qual";
     int form = DGTM_FP64, solver = DGTM_SOLVE_SVD;
+    bool rd_output = false;  // -J
 };
 
 void help()
@@ -244,6 +245,7 @@ void help()
         "-i filename  : input HDF5 filename",
         "-I           : interpolation",
         "-j number    : maximum number of iterations",
+        "-J           : after a -j stop, write M and R from R o D, as the reference does",
         "-k number    : largest K of the hierarchical DA (default: 32768)",
         "-K number    : number of latent data K (eg, 100, 1k, 1M)",
         "-l           : log to file",
@@ -276,7 +278,7 @@ Opts parse(int argc, char **argv)
     Opts o;
     int c;
     opterr = 0;
-    while ((c = getopt(argc, argv, "a:b:B:c:e:E:f:F:g:G:hHi:Ij:k:K:lL:mM:no:pP:Q:r:Rs:S:t:v:w:W:x:z:")) != -1) {
+    while ((c = getopt(argc, argv, "a:b:B:c:e:E:f:F:g:G:hHi:Ij:Jk:K:lL:mM:no:pP:Q:r:Rs:S:t:v:w:W:x:z:")) != -1) {
         switch (c) {
         case 'a': o.alpha = atof(optarg); break;
         case 'b': o.dbeta = optarg; break;
@@ -314,6 +316,7 @@ Opts parse(int argc, char **argv)
         case 'i': o.in = optarg; break;
         case 'I': o.interpolation = true; break;
         case 'j': o.maxloop = atoi(optarg); break;
+        case 'J': o.rd_output = !o.rd_output; break;
         case 'k': o.Kmax = atoi(optarg); break;
         case 'K': {
             float num = 0, unit = 1;
@@ -552,7 +555,8 @@ int main(int argc, char **argv)
     check(dgtm_set_solver(ctx, o.solver), "dgtm_set_solver");
     check(dgtm_set_Y(ctx, Y.data(), D), "dgtm_set_Y");
 
-    auto write_output = [&](const std::vector<double> &Mout, double qual, bool include_R) {
+    auto write_output = [&](const std::vector<double> &Mout, double qual, bool include_R,
+                            bool rd = false) {
         h5lite::Writer w;
         std::map<std::string, h5lite::Dataset> old;
         w.add_f64(o.dT, {(uint64_t) N, (uint64_t) D}, T.data());
@@ -564,7 +568,10 @@ int main(int argc, char **argv)
             w.add_f64(o.dW, {(uint64_t) M + 1, (uint64_t) D}, W.data());
         if (include_R) {
             std::vector<double> R((size_t) K * N);
-            check(dgtm_get_R_block(ctx, 0, K, 0, N, R.data(), N), "dgtm_get_R_block");
+            if (rd)
+                check(dgtm_get_RD_block(ctx, 0, K, 0, N, R.data(), N), "dgtm_get_RD_block");
+            else
+                check(dgtm_get_R_block(ctx, 0, K, 0, N, R.data(), N), "dgtm_get_R_block");
             w.add_f64(o.dR, {(uint64_t) K, (uint64_t) N}, R.data());
         }
         w.add_scalar_f64(o.dbeta, beta);
@@ -849,14 +856,20 @@ int main(int argc, char **argv)
     fflush(g_log);
 
     // ---- output (dagtm/dagtm.cxx:2342-2552): the MAP needs responsibilities
-    // of the final centres; after a maxloop break the reference reuses R o D
-    // here, this driver runs one more E-step instead.
+    // of the final centres.  After a maxloop break the reference reuses the R
+    // that dagtm_mpi_beta multiplied by the new distances (comm/mpicomm.c:288):
+    // with -J this driver writes that R o D too; by default it runs one more
+    // E-step on the final centres instead.
     if (!o.out.empty()) {
-        if (!stats_current)
+        const bool rd = o.rd_output && !stats_current;
+        if (!stats_current && !rd)
             check(dgtm_estep(ctx, beta, o.isDA, temp, &llh, &nfree), "dgtm_estep");
         std::vector<double> Mout((size_t) N * L);
-        check(dgtm_map(ctx, X.data(), L, Mout.data(), L), "dgtm_map");
-        h5lite::Writer w = write_output(Mout, qual, o.save_R);
+        if (rd)
+            check(dgtm_map_rd(ctx, X.data(), L, Mout.data(), L), "dgtm_map_rd");
+        else
+            check(dgtm_map(ctx, X.data(), L, Mout.data(), L), "dgtm_map");
+        h5lite::Writer w = write_output(Mout, qual, o.save_R, rd);
         for (const Snap &sn : snaps)
             w.add_f64(sn.name, sn.dims, sn.v.data());
         if (o.log_progress) {

@@ -135,6 +135,20 @@ int dgtm_get_R_block(dgtm_ctx *ctx, int k0, int nk, int n0, int nn, double *R,
                      int ldR);
 
 /*
+ * The reference's output after a run that stopped on its iteration cap (-j):
+ * there the break comes after dagtm_mpi_beta has multiplied R in place by
+ * the squared distances to the new centres (comm/mpicomm.c:288), and the
+ * MAP and the -R dump are computed from that R o D (dagtm/dagtm.cxx:2348-2355,
+ * 2406-2414).  dgtm_map_rd and dgtm_get_RD_block give M = (R o D)^T X and
+ * blocks of R o D: R of the last E-step (on the centres before the last
+ * M-step, which the context keeps) times the squared distance of each point
+ * to the current centres.  They need an M-step after the last E-step
+ * (DGTM_ESTATE otherwise).  FP64 in every precision form.
+ */
+int dgtm_map_rd(dgtm_ctx *ctx, const double *X, int L, double *M, int ldM);
+int dgtm_get_RD_block(dgtm_ctx *ctx, int k0, int nk, int n0, int nn, double *R, int ldR);
+
+/*
  * Next critical temperature of the AUTO cooling schedule, from the
  * responsibilities R of the last E-step.  For each centre k, with
  * x_n = t_n - y_k:  S1 = sum_n R_kn x_n x_n^T, S2 = sum_n R_kn^2 x_n x_n^T,

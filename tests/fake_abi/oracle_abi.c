@@ -23,7 +23,7 @@
 struct dgtm_ctx {
     int N, D, K, M1, solver, precision;
     double *T, *FI, *Y, *W, *Dm, *R, *Rc, *vgc, *vgc2, *G, *RT, *A, *B;
-    int stats_valid, w_valid, rt_valid;
+    int stats_valid, w_valid, rt_valid, rd_valid;
 };
 
 static char g_err[256] = "";
@@ -89,6 +89,7 @@ int dgtm_set_Y(dgtm_ctx *c, const double *Y, int ldY)
     orc_dist(c->K, c->N, c->D, c->Y, c->T, c->Dm);
     c->stats_valid = 0;
     c->rt_valid = 0;
+    c->rd_valid = 0;
     return DGTM_OK;
 }
 
@@ -122,6 +123,7 @@ int dgtm_estep(dgtm_ctx *c, double beta, int isDA, double temp, double *llh, dou
         *nfree = f;
     c->stats_valid = 1;
     c->rt_valid = 0;
+    c->rd_valid = 0;
     return DGTM_OK;
 }
 
@@ -154,6 +156,7 @@ int dgtm_mstep(dgtm_ctx *c, double *W, int ldW, double *Y, int ldY, double *beta
     c->stats_valid = 0;
     c->w_valid = 1;
     c->rt_valid = 1;
+    c->rd_valid = 1;  /* orc_beta left R o D in c->R, as dagtm_mpi_beta does */
     return DGTM_OK;
 }
 
@@ -180,6 +183,29 @@ int dgtm_map(dgtm_ctx *c, const double *X, int L, double *M, int ldM)
                 s += c->Rc[(size_t) k * c->N + n] * X[(size_t) k * L + l];
             M[(size_t) n * ldM + l] = s;
         }
+    return DGTM_OK;
+}
+
+int dgtm_map_rd(dgtm_ctx *c, const double *X, int L, double *M, int ldM)
+{
+    if (!c->rd_valid)
+        return fail(DGTM_ESTATE, "dgtm_map_rd needs an M-step after the last E-step");
+    for (int n = 0; n < c->N; n++)
+        for (int l = 0; l < L; l++) {
+            double s = 0.0;
+            for (int k = 0; k < c->K; k++)
+                s += c->R[(size_t) k * c->N + n] * X[(size_t) k * L + l];
+            M[(size_t) n * ldM + l] = s;
+        }
+    return DGTM_OK;
+}
+
+int dgtm_get_RD_block(dgtm_ctx *c, int k0, int nk, int n0, int nn, double *R, int ldR)
+{
+    if (!c->rd_valid)
+        return fail(DGTM_ESTATE, "dgtm_get_RD_block needs an M-step after the last E-step");
+    for (int k = 0; k < nk; k++)
+        memcpy(R + (size_t) k * ldR, c->R + (size_t) (k0 + k) * c->N + n0, sizeof(double) * nn);
     return DGTM_OK;
 }
 

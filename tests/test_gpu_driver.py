@@ -1,6 +1,17 @@
-"""The `dagtm` command end to end on the reference's oil input: the options,
-the `:::` trace, checkpoints, restart, interpolation and the output layout of
-dagtm/dagtm.cxx, with the EM step on the GPU."""
+"""The `dagtm` command end to end on the reference's oil input, with the EM
+step on the GPU: the options, the `:::` trace, checkpoints, restart,
+interpolation, the output layout of dagtm/dagtm.cxx, and its traces against
+the package's temperature loop served by the oracle (tests/oracle_ctx.py),
+not by this library.
+
+Every run starts from a restart file the driver wrote after one iteration of
+its own set-up, below the first critical temperature, so that the centres
+leave the trivial solution within the run and the traces move.  Basis width
+factor 1 (-G 1): the reference's 2 makes A = FI^T G FI on the oil basis
+ill-conditioned (cond ~6e9), and any two FP64 solvers then differ in the
+centres by ~1e-6; at width 1 the FP64 form follows the oracle to 1e-9.  The
+split form is held to its stated 1e-4.
+"""
 import os
 import re
 import signal
@@ -12,6 +23,7 @@ import numpy as np
 import pytest
 
 from conftest import ROOT
+from oracle_ctx import OracleCtx
 
 sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
 from make_golden import H5File  # noqa: E402
@@ -34,49 +46,90 @@ def trace(stdout):
     return np.array([[float(x) for x in m.groups()] for m in rows if m])
 
 
-def test_run_trace_and_output(tmp_path, pkg, golden):
-    # -e 0: every iteration stays at the start temperature, so the comparison
-    # below does not hinge on where |diff| first drops under eps
-    out = run(["-i", OIL_IN, "-o", "out.h5", "-K", "125", "-L", "3", "-M", "8", "-s", "7",
-               "-j", "40", "-n", "-p", "-a", "0.95", "-e", "0", "-F", "fp64"], tmp_path)
+def oil_T(golden):
+    return golden["T_in"].astype(np.float64)
+
+
+def start_state(tmp_path, pkg, golden, extra, frac=0.6):
+    """One driver iteration from its own set-up, started at frac x the first
+    critical temperature: the restart file both loops start from."""
+    st = __import__("importlib").import_module(pkg.__name__ + ".gtm_setup")
+    t0 = frac * st.first_critical_temp(oil_T(golden))
+    run(["-i", OIL_IN, "-o", "s0.h5", "-j", "1", "-n", "-S", f"{float(t0):.17g}"] + extra,
+        tmp_path)
+    f = H5File(str(tmp_path / "s0.h5"))
+    return (f.read("X"), f.read("FI"), f.read("Y"), float(f.read("beta")[0]),
+            float(f.read("temp")[0]), int(f.read("iter")[0]))
+
+
+def test_run_trace_and_output(tmp_path, pkg, orc, golden):
+    common = ["-K", "125", "-L", "3", "-M", "8", "-s", "7", "-G", "1", "-F", "fp64",
+              "-Q", "cholesky"]
+    X, FI, Y, beta, temp, it = start_state(tmp_path, pkg, golden, common + ["-a", "0.9"])
+    out = run(["-i", OIL_IN, "-r", "s0.h5", "-o", "out.h5", "-j", "150", "-n", "-p", "-a", "0.9",
+               "-e", "1e-6", "-F", "fp64", "-Q", "cholesky", "-G", "1"], tmp_path)
     tr = trace(out)
-    assert len(tr) == 40 and tr[0][0] == 1 and tr[-1][0] == 40
     assert "SUMMARY" in out and "Num. of Iterations" in out
     f = H5File(str(tmp_path / "out.h5"))
     for name in ("T", "M", "X", "FI", "Y", "W", "beta", "temp", "iter", "seed", "qual", "id", "lb",
                  "Temp", "LLH", "NFree"):
         assert name in f.datasets, name
-    assert np.array_equal(f.read("T"), golden["T_in"].astype(np.float64))
+    assert np.array_equal(f.read("T"), oil_T(golden))
     assert np.array_equal(f.read("lb"), golden["lb_in"])
-    X, FI, Y, W = f.read("X"), f.read("FI"), f.read("Y"), f.read("W")
-    assert X.shape == (125, 3) and FI.shape == (125, 9) and W.shape == (9, 12)
-    assert np.array_equal(X, golden["X"]) and np.max(np.abs(FI - golden["FI"])) < 1e-15
-    assert np.max(np.abs(FI @ W - Y)) < 1e-6 * np.max(np.abs(Y))
+    assert f.read("X").shape == (125, 3) and f.read("W").shape == (9, 12)
     M = f.read("M")
     assert M.shape == (1000, 3) and np.all(np.abs(M) <= 1.0 + 1e-12)
-    assert int(f.read("iter")[0]) == 40 and int(f.read("seed")[0]) == 7
-    assert np.allclose(f.read("NFree"), tr[:, 4], rtol=1e-6)
-    # the driver's trace agrees with the package's own loop from the same set-up
-    st = __import__("importlib").import_module(pkg.__name__ + ".gtm_setup")
-    T = golden["T_in"].astype(np.float64)
-    _, FI0, W0, beta0 = st.random_init(T, 3, 125, 8, 2.0, seed=7)
-    with pkg.Context(T, FI0, "fp64", solver="svd") as c:
-        c.set_Y(FI0 @ W0)
-        ref = pkg.anneal(c, beta0, st.start_temp(T, 0.95), alpha=0.95, eps=0.0, maxloop=40)
-    assert np.allclose(tr[:, 4], ref.nfree_trace, rtol=1e-5, atol=1e-6)
+    ctx = OracleCtx(orc, oil_T(golden), FI, Y)
+    ref = pkg.anneal(ctx, beta, temp, alpha=0.9, eps=1e-6, iter0=it, maxloop=150)
+    assert len(tr) == len(ref.nfree_trace) >= 150
+    assert len(set(ref.temp_trace)) >= 2  # the run crosses temperatures
+    assert np.ptp(f.read("NFree")) > 1.0  # the centres leave the trivial solution
+    np.testing.assert_allclose(f.read("Temp"), ref.temp_trace, rtol=1e-12)
+    np.testing.assert_allclose(f.read("NFree"), ref.nfree_trace, rtol=1e-9)
+    np.testing.assert_allclose(f.read("LLH"), ref.llh_trace, rtol=1e-9)
+    np.testing.assert_allclose(f.read("Y"), ctx.Y, rtol=1e-9, atol=1e-12)
+    np.testing.assert_allclose(tr[:, 4], ref.nfree_trace, rtol=1e-6)  # printed to 7 digits
 
 
-def test_checkpoint_restart_and_interpolation(tmp_path):
-    # -e 0 keeps the whole run at one temperature, where a restart resumes exactly
-    common = ["-i", OIL_IN, "-K", "125", "-L", "3", "-M", "8", "-s", "3", "-a", "0.9", "-e", "0"]
+def test_maxloop_stop_writes_the_references_R_o_D_with_J(tmp_path, pkg, orc, golden):
+    """-J: after a -j stop the MAP and the -R dump come from R o D, the R that
+    dagtm_mpi_beta multiplied by the new distances (comm/mpicomm.c:288,
+    dagtm/dagtm.cxx:2348-2414); the oracle's loop leaves the same R o D."""
+    common = ["-K", "125", "-L", "3", "-M", "8", "-s", "5", "-G", "1", "-F", "fp64",
+              "-Q", "cholesky"]
+    X, FI, Y, beta, temp, it = start_state(tmp_path, pkg, golden, common + ["-a", "0.9"])
+    run(["-i", OIL_IN, "-r", "s0.h5", "-o", "rd.h5", "-j", "12", "-n", "-J", "-R", "-a", "0.9",
+         "-e", "0", "-F", "fp64", "-Q", "cholesky", "-G", "1"], tmp_path)
+    ref = orc.run(oil_T(golden), FI, Y, beta, temp, isDA=1, alpha=0.9, eps=0.0, iter0=it,
+                  maxloop=12, solver=1, want_R=True)
+    f = H5File(str(tmp_path / "rd.h5"))
+    RD = ref["R"]
+    assert not np.allclose(RD.sum(axis=0), 1.0)  # R o D, not R
+    np.testing.assert_allclose(f.read("R"), RD, rtol=1e-8, atol=1e-12 * np.max(RD))
+    Mref = RD.T @ X
+    np.testing.assert_allclose(f.read("M"), Mref, rtol=1e-8, atol=1e-10 * np.max(np.abs(Mref)))
+    # without -J: one more E-step on the final centres, R columns sum to one
+    run(["-i", OIL_IN, "-r", "s0.h5", "-o", "clean.h5", "-j", "12", "-n", "-R", "-a", "0.9",
+         "-e", "0", "-F", "fp64", "-Q", "cholesky", "-G", "1"], tmp_path)
+    g = H5File(str(tmp_path / "clean.h5"))
+    assert np.allclose(g.read("R").sum(axis=0), 1.0, atol=1e-12)
+    np.testing.assert_allclose(g.read("Y"), f.read("Y"), rtol=1e-13)
+
+
+def test_checkpoint_restart_and_interpolation(tmp_path, golden):
+    # started below the first critical temperature (-S 1.5): the trace moves
+    common = ["-i", OIL_IN, "-K", "125", "-L", "3", "-M", "8", "-s", "3", "-a", "0.9", "-e", "0",
+              "-S", "1.5", "-Q", "cholesky"]
     full = trace(run(common + ["-j", "16", "-n"], tmp_path))
+    assert np.min(np.abs(np.diff(full[9:16, 4]))) > 1e-6 * np.max(np.abs(full[:, 4]))
     run(common + ["-j", "10", "-P", "5", "-w", "ck."], tmp_path)
     assert (tmp_path / "ck.5.h5").exists() and (tmp_path / "ck.10.h5").exists()
     ck = H5File(str(tmp_path / "ck.10.h5"))
     for name in ("X", "FI", "Y", "beta", "temp", "iter", "seed", "qual"):
         assert name in ck.datasets
     assert int(ck.read("iter")[0]) == 10
-    rest = trace(run(common + ["-r", "ck.10.h5", "-j", "6", "-n"], tmp_path))
+    rest = trace(run(["-i", OIL_IN, "-r", "ck.10.h5", "-j", "6", "-n", "-a", "0.9", "-e", "0",
+                      "-Q", "cholesky"], tmp_path))
     assert rest[0][0] == 11 and len(rest) == 6
     # a checkpoint is taken after an iteration's E-step, before its M-step (as
     # the reference takes it), so the restart repeats the E-step of iteration
@@ -94,7 +147,12 @@ def test_signal_forces_a_checkpoint_and_exit(tmp_path):
                          stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True)
     time.sleep(3.0)
     p.send_signal(signal.SIGCHLD)
-    out, err = p.communicate(timeout=120)
+    try:
+        out, err = p.communicate(timeout=120)
+    except subprocess.TimeoutExpired:
+        p.kill()  # this test's own child
+        p.communicate()
+        raise
     assert p.returncode == 0, err
     files = list(tmp_path.glob("sig.*.h5"))
     assert len(files) == 1
@@ -102,86 +160,88 @@ def test_signal_forces_a_checkpoint_and_exit(tmp_path):
     assert str(files[0]).endswith(f"sig.{n}.h5")
 
 
-def test_auto_schedule_matches_package_loop(tmp_path, pkg, golden):
+def test_auto_schedule_against_the_oracle_loop(tmp_path, pkg, orc, golden):
     # -c auto: after each temperature the next one is the critical temperature
     # of dgtm_next_ctemp (or temp * alpha when none is below the current one)
-    out = run(["-i", OIL_IN, "-o", "auto.h5", "-K", "125", "-L", "3", "-M", "8", "-s", "3",
-               "-j", "60", "-c", "auto", "-a", "0.9", "-e", "1e-3", "-F", "fp64"], tmp_path)
+    common = ["-K", "125", "-L", "3", "-M", "8", "-s", "3", "-G", "1", "-F", "fp64",
+              "-Q", "cholesky"]
+    X, FI, Y, beta, temp, it = start_state(tmp_path, pkg, golden, common + ["-c", "auto"])
+    out = run(["-i", OIL_IN, "-r", "s0.h5", "-o", "auto.h5", "-j", "80", "-n", "-p", "-c", "auto",
+               "-a", "0.9", "-e", "1e-5", "-F", "fp64", "-Q", "cholesky", "-G", "1"], tmp_path)
     assert "Cooling Schedule = AUTO" in " ".join(out.split())
-    tr = trace(out)
+    f = H5File(str(tmp_path / "auto.h5"))
     temps = []
-    for t in tr[:, 3]:
+    for t in f.read("Temp"):
         if not temps or t != temps[-1]:
             temps.append(t)
     assert len(temps) >= 2 and all(a > b for a, b in zip(temps, temps[1:]))
-    st = __import__("importlib").import_module(pkg.__name__ + ".gtm_setup")
-    T = golden["T_in"].astype(np.float64)
-    _, FI0, W0, beta0 = st.random_init(T, 3, 125, 8, 2.0, seed=3)
-    with pkg.Context(T, FI0, "fp64", solver="svd") as c:
-        c.set_Y(FI0 @ W0)
-        ref = pkg.anneal(c, beta0, st.start_temp(T, 0.9), schedule="auto", alpha=0.9, eps=1e-3,
-                         maxloop=60)
-    n = min(len(tr), len(ref.nfree_trace))
-    assert n >= 10
-    assert np.allclose(tr[:n, 3], ref.temp_trace[:n], rtol=1e-6)
-    assert np.allclose(tr[:n, 4], ref.nfree_trace[:n], rtol=1e-5, atol=1e-6)
+    ctx = OracleCtx(orc, oil_T(golden), FI, Y)
+    ref = pkg.anneal(ctx, beta, temp, schedule="auto", alpha=0.9, eps=1e-5, iter0=it,
+                     maxloop=80)
+    np.testing.assert_allclose(f.read("Temp"), ref.temp_trace, rtol=1e-9)
+    np.testing.assert_allclose(f.read("NFree"), ref.nfree_trace, rtol=1e-9)
 
 
-def test_hda_expands_and_writes_snapshots(tmp_path, pkg, golden):
+def test_hda_expands_and_writes_snapshots(tmp_path, pkg, orc, golden):
     # -H on the EXP schedule from K = 8 (L = 3), started below the first
     # critical temperature: the grid doubles per dimension twice within 200
-    # iterations (8 -> 64 -> 512), as the package loop does from the same set-up
-    st = __import__("importlib").import_module(pkg.__name__ + ".gtm_setup")
-    T = golden["T_in"].astype(np.float64)
-    t0 = 0.6 * st.first_critical_temp(T)
-    out = run(["-i", OIL_IN, "-o", "hda.h5", "-K", "8", "-L", "3", "-M", "8", "-s", "3", "-H",
-               "-S", f"{float(t0):.17g}", "-j", "200", "-n", "-p", "-a", "0.9", "-e", "1e-6", "-F", "fp64",
-               "-Q", "cholesky"], tmp_path)
+    # iterations (8 -> 64 -> 512), as the oracle-served loop does from the
+    # same restart file
+    common = ["-K", "8", "-L", "3", "-M", "8", "-s", "3", "-H", "-F", "fp64", "-Q", "cholesky"]
+    X, FI, Y, beta, temp, it = start_state(tmp_path, pkg, golden, common + ["-a", "0.9"])
+    out = run(["-i", OIL_IN, "-r", "s0.h5", "-o", "hda.h5", "-j", "200", "-n", "-p", "-H",
+               "-a", "0.9", "-e", "1e-6", "-F", "fp64", "-Q", "cholesky"], tmp_path)
     tr = trace(out)
     Ks = tr[:, 2].astype(int)
-    assert Ks[0] == 8 and Ks[-1] == 512
-    grow = [int(tr[i, 0]) for i in range(1, len(tr)) if Ks[i] != Ks[i - 1]]
-    _, FI0, W0, beta0 = st.random_init(T, 3, 8, 8, 2.0, seed=3)
-    with pkg.Context(T, FI0, "fp64") as c:
-        c.set_Y(FI0 @ W0)
-        ref = pkg.anneal(c, beta0, t0, alpha=0.9, eps=1e-6, maxloop=200, hda=True, T=T, L=3)
+    assert Ks[-1] == 512
+    T = oil_T(golden)
+    ctx = OracleCtx(orc, T, FI, Y)
+    ref = pkg.anneal(ctx, beta, temp, alpha=0.9, eps=1e-6, iter0=it, maxloop=200, hda=True,
+                     T=T, L=3)
     assert [e[1:] for e in ref.expansions] == [(8, 64), (64, 512)]
-    # the first iteration at the new K follows the expansion's last one
+    grow = [int(tr[i, 0]) for i in range(1, len(tr)) if Ks[i] != Ks[i - 1]]
     assert grow == [e[0] + 1 for e in ref.expansions]
-    n = min(len(tr), len(ref.nfree_trace))
-    # the host products Y = FI W of the two loops round differently, and A is
-    # ill-conditioned on the oil basis: the tolerance of the other driver tests
-    assert np.allclose(tr[:n, 4], ref.nfree_trace[:n], rtol=1e-5, atol=1e-6)
     f = H5File(str(tmp_path / "hda.h5"))
-    for (it, K, _), (Kx, Mx) in zip(ref.expansions, ((8, 8), (64, 8))):
-        idx = it - 1  # the temperature collection holds one entry per iteration
+    nf = f.read("NFree")
+    first = ref.expansions[0][0] - it
+    # K = 8 centres with M + 1 = 9 basis functions: A is singular and pivots
+    # are dropped, so W (not Y) is undetermined; the traces agree to 1e-6
+    np.testing.assert_allclose(nf[:first], ref.nfree_trace[:first], rtol=1e-6)
+    # after an expansion the host products Y = FI W of the two loops round
+    # differently on an ill-conditioned basis (width factor 2 is fixed by -H)
+    np.testing.assert_allclose(nf, ref.nfree_trace, rtol=1e-5, atol=1e-6)
+    for (itx, K, _), Mx in zip(ref.expansions, (8, 8)):
+        idx = itx - 1 - it  # the temperature collection holds one entry per iteration
         assert f.read(f"X.{idx}").shape == (K, 3)
         assert f.read(f"FI.{idx}").shape == (K, Mx + 1)
         assert f.read(f"Y.{idx}").shape == (K, 12)
-        assert f.read(f"W.{idx}").shape == (Mx + 1, 12)
         assert f.read(f"M.{idx}").shape == (1000, 3)
         assert f.read(f"ctemp.{idx}").shape == (K,)
-        assert f.read(f"beta.{idx}").shape == (1,)
     assert f.read("X").shape == (512, 3) and f.read("Y").shape == (512, 12)
 
 
-def test_split_form_with_linear_cooling(tmp_path, pkg, golden):
-    # -F bf16x3 -c linear: the driver's loop over the split form agrees with
-    # the package's loop from the same set-up (one library, two host loops)
-    out = run(["-i", OIL_IN, "-o", "lin.h5", "-K", "125", "-L", "3", "-M", "8", "-s", "4",
-               "-j", "40", "-n", "-c", "linear", "-e", "1e-3", "-F", "bf16x3"], tmp_path)
-    assert "Cooling Schedule = LINEAR" in " ".join(out.split())
-    tr = trace(out)
-    st = __import__("importlib").import_module(pkg.__name__ + ".gtm_setup")
-    T = golden["T_in"].astype(np.float64)
-    _, FI0, W0, beta0 = st.random_init(T, 3, 125, 8, 2.0, seed=4)
-    with pkg.Context(T, FI0, "bf16x3", solver="svd") as c:
-        c.set_Y(FI0 @ W0)
-        ref = pkg.anneal(c, beta0, st.start_temp(T, 0.99), schedule="linear", delta=0.1,
-                         eps=1e-3, maxloop=40)
-    n = min(len(tr), len(ref.nfree_trace))
-    assert n >= 10
-    assert np.allclose(tr[:n, 3], ref.temp_trace[:n], rtol=1e-6)
-    assert np.allclose(tr[:n, 4], ref.nfree_trace[:n], rtol=1e-5, atol=1e-6)
+def test_split_form_with_linear_cooling(tmp_path, pkg, orc, golden):
+    # -F bf16x3 -c linear against the oracle-served loop: the split form's
+    # stated 1e-4 (oil data are not exact in BF16: three products)
+    common = ["-K", "125", "-L", "3", "-M", "8", "-s", "4", "-G", "1", "-F", "fp64",
+              "-Q", "cholesky"]
+    X, FI, Y, beta, temp, it = start_state(tmp_path, pkg, golden, common + ["-c", "linear"],
+                                           frac=0.8)
+    run(["-i", OIL_IN, "-r", "s0.h5", "-o", "lin.h5", "-j", "40", "-n", "-p", "-c", "linear",
+         "-e", "1e-4", "-F", "bf16x3", "-Q", "cholesky", "-G", "1"], tmp_path)
     f = H5File(str(tmp_path / "lin.h5"))
+    ctx = OracleCtx(orc, oil_T(golden), FI, Y)
+    ref = pkg.anneal(ctx, beta, temp, schedule="linear", delta=0.1, eps=1e-4, iter0=it,
+                     maxloop=40)
+    # the split form's qualities carry ~1e-5, so the |diff| < eps test that
+    # ends a temperature may fire an iteration apart: compare the traces over
+    # the first temperature, and the schedule's steps over the whole run
+    temps = f.read("Temp")
+    rt = np.asarray(ref.temp_trace)
+    n = int(np.argmax(temps != temps[0])) if np.any(temps != temps[0]) else len(temps)
+    n = min(n, int(np.argmax(rt != rt[0])) if np.any(rt != rt[0]) else len(rt))
+    assert n >= 5 and np.ptp(ref.nfree_trace[:n]) > 0.1
+    np.testing.assert_allclose(f.read("NFree")[:n], ref.nfree_trace[:n], rtol=1e-4)
+    steps = np.diff(np.unique(temps)[::-1])
+    assert len(steps) >= 1 and np.allclose(steps, -0.1, rtol=1e-9)
     assert f.read("Y").shape == (125, 12) and np.all(np.isfinite(f.read("Y")))
