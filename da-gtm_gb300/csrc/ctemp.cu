@@ -381,6 +381,21 @@ CtempPlan ctemp_plan(int N, int D, int K, bool f32, bool have_t32, size_t budget
     return pl;
 }
 
+int launch_ctemp_eig(const CtempPlan &pl, int kb, int D, const double *S, void *Mg,
+                     const double *gg, double lim_scale, double *out, cudaStream_t s)
+{
+    if (pl.f32) {
+        float *M = static_cast<float *>(Mg);
+        if (D <= EIG_SMALL_D)
+            return launch_eig<256, float>(kb, D, pl.eig_in_smem, S, M, gg, lim_scale, out, s);
+        return launch_eig<512, float>(kb, D, pl.eig_in_smem, S, M, gg, lim_scale, out, s);
+    }
+    double *M = static_cast<double *>(Mg);
+    if (D <= EIG_SMALL_D)
+        return launch_eig<256, double>(kb, D, pl.eig_in_smem, S, M, gg, lim_scale, out, s);
+    return launch_eig<1024, double>(kb, D, pl.eig_in_smem, S, M, gg, lim_scale, out, s);
+}
+
 int launch_ctemp_batch(const CtempPlan &pl, const double *T64, const float *T32, const double *Y,
                        const double *tt, const double *yy, const double2 *colstat, int N, int D,
                        int K, double c, int k0, int kb, const double *gg_dev, double lim_scale,

@@ -771,8 +771,17 @@ int dgtm_next_ctemp_k(dgtm_ctx *ctx, double temp, double beta, double eps, const
     }
     const int N = ctx->N, D = ctx->D, K = ctx->K;
     const double c = ctx->isDA ? ctx->beta / (2.0 * ctx->temp) : ctx->beta / 2.0;
+    // eigenvalues at or above (temp - eps) gg 2 / beta are dropped (comm/mpicomm.c:624)
+    const double lim_scale = (temp - eps) * 2.0 / beta;
+    bool pairs = false;
+    if (ctx->precision == DGTM_BF16X3 && ctx->tc && env_int("DGTM_CTEMP_PAIRS", 1, 0, 1)) {
+        TcView v;
+        tc_view(ctx->tc, &v);
+        pairs = v.binary && v.nT == 1;
+    }
     // scratch budget and points per chunk: DGTM_CTEMP_SCRATCH_MB (default 256)
-    // and DGTM_CTEMP_CHUNK (default 16384) override them
+    // and DGTM_CTEMP_CHUNK (default 16384) override them; the pair-feature
+    // GEMM (split form, 0/1 data) takes DGTM_CTEMP_GEMM_MB (default 8192)
     const size_t budget = (size_t) env_int("DGTM_CTEMP_SCRATCH_MB", 256, 1, 1 << 20) << 20;
     const int nn_max = env_int("DGTM_CTEMP_CHUNK", 16384, 1, 1 << 30);
     const CtempPlan pl = ctemp_plan(N, D, K, ctx->precision != DGTM_FP64, ctx->T32 != nullptr,
@@ -780,7 +789,8 @@ int dgtm_next_ctemp_k(dgtm_ctx *ctx, double temp, double beta, double eps, const
     const int kb = pl.kb;
     double *scratch = nullptr, *dgg = nullptr, *dgsum = nullptr, *dout = nullptr;
     std::vector<double> out((size_t) 2 * K), gsum(K);
-    int rc = dev_alloc(&scratch, (pl.scratch_bytes + sizeof(double) - 1) / sizeof(double));
+    int rc = pairs ? DGTM_OK
+                   : dev_alloc(&scratch, (pl.scratch_bytes + sizeof(double) - 1) / sizeof(double));
     if (rc == DGTM_OK)
         rc = dev_alloc(&dgsum, K);
     if (rc == DGTM_OK)
@@ -790,9 +800,18 @@ int dgtm_next_ctemp_k(dgtm_ctx *ctx, double temp, double beta, double eps, const
     cudaError_t e = cudaSuccess;
     if (rc == DGTM_OK && gg)
         e = cudaMemcpyAsync(dgg, gg, sizeof(double) * K, cudaMemcpyHostToDevice, ctx->stream);
-    // eigenvalues at or above (temp - eps) gg 2 / beta are dropped (comm/mpicomm.c:624)
-    const double lim_scale = (temp - eps) * 2.0 / beta;
-    for (int k0 = 0; rc == DGTM_OK && e == cudaSuccess && k0 < K; k0 += kb) {
+    if (pairs && rc == DGTM_OK && e == cudaSuccess) {
+        TcView v;
+        tc_view(ctx->tc, &v);
+        const size_t gbudget = (size_t) env_int("DGTM_CTEMP_GEMM_MB", 8192, 64, 1 << 22) << 20;
+        rc = tc_ctemp_pairs(v, ctx->Y64, gg ? dgg : nullptr, lim_scale, gbudget, dgsum, dout,
+                            ctx->stream);
+        if (rc == DGTM_OK)
+            rc = tc_fetch_status(ctx->tc, ctx->stream);
+        if (rc == DGTM_OK && (e = cudaStreamSynchronize(ctx->stream)) == cudaSuccess)
+            rc = tc_check_status(ctx->tc);
+    }
+    for (int k0 = 0; !pairs && rc == DGTM_OK && e == cudaSuccess && k0 < K; k0 += kb) {
         const int nb = (K - k0 < kb) ? K - k0 : kb;
         rc = launch_ctemp_batch(pl, ctx->T64, ctx->T32, ctx->Y64, ctx->tt, ctx->yy, ctx->colstat,
                                 N, D, K, c, k0, nb, gg ? dgg + k0 : nullptr, lim_scale, scratch,

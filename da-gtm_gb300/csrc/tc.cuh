@@ -67,4 +67,13 @@ struct TcView {
 };
 void tc_view(const TcState *st, TcView *v);
 
+// The AUTO schedule's scatter as a tensor-core GEMM over pair features
+// (ctemp_tc.cu).  Needs 0/1 data (binary: every pair product exact in BF16):
+// for centres k, S1_k = sum_n R_kn (t_n - y_k)(t_n - y_k)^T and S2_k (R^2),
+// upper triangles, written per batch of centres as the CUDA-core scatter
+// writes them; then the eigen filter of ctemp.cu.  out[2 k + w] as in
+// launch_ctemp_batch; gsum[k] = row sums of R.
+int tc_ctemp_pairs(const TcView &v, const double *Y64, const double *gg_dev, double lim_scale,
+                   size_t budget, double *gsum_dev, double *out_dev, cudaStream_t s);
+
 }  // namespace dgtm

@@ -162,6 +162,10 @@ int dgtm_get_RD_block(dgtm_ctx *ctx, int k0, int nk, int n0, int nn, double *R, 
  * in FP64) and take the eigenvalues in FP32, within their stated 1e-4.
  * Scratch: DGTM_CTEMP_SCRATCH_MB (default 256) bounds the device memory of
  * one batch of centres, DGTM_CTEMP_CHUNK (default 16384) the points per chunk.
+ * The split form on 0/1 data forms S1 and S2 instead as a tensor-core GEMM of
+ * R and R^2 (split BF16) against the pair features (t_i t_j, t_i, 1), which
+ * are exact in BF16, with DGTM_CTEMP_GEMM_MB (default 8192) of scratch;
+ * DGTM_CTEMP_PAIRS=0 selects the CUDA-core scatter for those contexts too.
  * Replaces dagtm_mpi_next_ctemp and its helper (comm/mpicomm.c:562-674) with
  * dagtm_vector_max (comm/comm.c:2149-2161), called at dagtm/dagtm.cxx:1919-1934.
  */

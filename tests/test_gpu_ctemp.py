@@ -7,7 +7,10 @@ after the orthogonal block transform.  The same responsibilities go into both
 (the FP64 form reproduces the oracle's R to ~1e-12), so the critical
 temperatures agree to FP64 eigenvalue accuracy: 1e-9 relative.  The FP32 and
 split-BF16 forms form the scatter matrices and run the eigen sweeps in FP32,
-and the split form's R carries its stated error: 1e-4 relative.
+and the split form's R carries its stated error: 1e-4 relative.  On 0/1 data
+the split form forms the scatter as a tensor-core GEMM over pair features
+(R and R^2 against u_n = (t_i t_j, t_i, 1)); DGTM_CTEMP_PAIRS=0 selects the
+CUDA-core scatter instead, and the two agree centre by centre to 1e-4.
 """
 import importlib
 
@@ -84,6 +87,38 @@ def test_next_ctemp_in_chunks_and_batches(pkg, orc, monkeypatch, form, tol):
     assert whole == pytest.approx(ref, rel=tol)
     assert parts == pytest.approx(ref, rel=tol)
     np.testing.assert_allclose(parts_k, whole_k, rtol=1e-12 if form == "fp64" else 1e-4)
+
+
+@pytest.fixture(scope="module")
+def pairs_case(pkg, orc):
+    """9000 binary points in D = 166, K = 16, and the oracle's answer (its
+    2D x 2D eigenproblems are the expensive part: computed once)."""
+    T, FI, Y = problem(pkg, "binary", 9000, 166, 16, seed=9)
+    beta, temp, eps = 30.0 / 166, 4.0, 1e-6
+    ref, _ = oracle_ctemp(orc, T, Y, beta, temp, eps)
+    return T, FI, Y, beta, temp, eps, ref
+
+
+@pytest.mark.parametrize("gemm_mb", ["8192", "64"])
+def test_pair_feature_gemm_chunks_and_segments(pkg, monkeypatch, pairs_case, gemm_mb):
+    """The pair-feature GEMM over 9000 binary points: with the default budget
+    the points form one chunk of 9216 (three 4096-point accumulation segments,
+    the last ragged); with 64 MB three chunks of 4096.  Against the oracle
+    (1e-4) and, centre by centre, against the CUDA-core scatter of the same
+    form (1e-4)."""
+    T, FI, Y, beta, temp, eps, ref = pairs_case
+    monkeypatch.setenv("DGTM_CTEMP_GEMM_MB", gemm_mb)
+    with pkg.Context(T, FI, "bf16x3") as c:
+        c.set_Y(Y)
+        c.estep(beta, 1, temp)
+        got, got_k = c.next_ctemp(temp, beta, eps, per_centre=True)
+        monkeypatch.setenv("DGTM_CTEMP_PAIRS", "0")
+        simt, simt_k = c.next_ctemp(temp, beta, eps, per_centre=True)
+    print(f"pairs {got / ref - 1:.2e}, cuda cores {simt / ref - 1:.2e}, per centre "
+          f"{np.max(np.abs(got_k / simt_k - 1)):.2e}")
+    assert got == pytest.approx(ref, rel=1e-4)
+    assert simt == pytest.approx(ref, rel=1e-4)
+    np.testing.assert_allclose(got_k, simt_k, rtol=1e-4)
 
 
 def test_next_ctemp_oil(pkg, orc, golden):
