@@ -60,8 +60,9 @@ sys.path.insert(0, ROOT)
 
 METRIC = "EM iters/sec at N=1M,K=8k,D=166: FP64 plain vs BF16x3 form at stated error"
 DTYPES = {
-    "bf16x3": "bf16x3 (split BF16 products, fp32 accumulate; per point the log-sum-exp over "
-              "128-centre chunks in fp32, across chunks in fp64; fp64 M-step and beta)",
+    "bf16x3": "bf16x3 (split BF16 products, fp32 accumulate; per point the shifted sums in "
+              "fp32 with Kahan compensation, the nearest distance recomputed in fp32, "
+              "logarithms and sums over points in fp64; fp64 M-step and beta)",
     "fp64": "f64", "fp32": "f32 (fp64 reductions and M-step)"}
 WORKLOAD = dict(N=1_000_000, D=166, K=8000, L=3, M=64, s=2.0, nproto=20, seed=0)
 
