@@ -435,7 +435,7 @@ __global__ void __launch_bounds__(PG_THREADS, 1)
         }
         if (!ok)
             failed = 1;
-    } else {
+    } else if (warp >= 2) {
         // ---------------- accumulators to the running sums (one centre row per thread) ----------------
         const int q = warp & 3;
         const int row = q * 32 + lane;
