@@ -37,10 +37,12 @@ ABI_SYMBOLS = ("dgtm_version", "dgtm_last_error_string", "dgtm_ctx_create", "dgt
                "dgtm_mstep", "dgtm_get_stats", "dgtm_map", "dgtm_get_R_block", "dgtm_map_rd",
                "dgtm_get_RD_block", "dgtm_next_ctemp",
                "dgtm_next_ctemp_k", "dgtm_set_timing",
-               "dgtm_reset_timing", "dgtm_get_timing", "dgtm_get_stream", "dgtm_selftest",
+               "dgtm_reset_timing", "dgtm_get_timing", "dgtm_get_stream", "dgtm_get_path",
+               "dgtm_selftest",
                "dgtm_fe_workspace_size", "dgtm_fe_forward", "dgtm_fe_backward",
                "dgtm_fe_forward_noalloc", "dgtm_wait_probe")
 PHASES = ("estep", "estep_reduce", "mstep_pass", "mstep_solve")
+PATHS = ("cuda_cores", "split_bf16", "exact_slices")
 
 
 class DgtmError(RuntimeError):
@@ -87,6 +89,7 @@ def load_library(path: str = LIB_PATH):
         "dgtm_get_timing": (i, [vp, _dp, ctypes.POINTER(ctypes.c_longlong),
                                 ctypes.POINTER(ctypes.c_longlong)]),
         "dgtm_get_stream": (i, [vp, pp]),
+        "dgtm_get_path": (i, [vp, ctypes.POINTER(i)]),
         "dgtm_selftest": (i, [_dp, i]),
         "dgtm_fe_workspace_size": (i, [i, i, i, ctypes.POINTER(ctypes.c_size_t)]),
         "dgtm_fe_forward": (i, [vp, vp, i, i, i, d, d, vp, ctypes.c_size_t, vp, vp]),
@@ -265,6 +268,14 @@ class Context:
         nc = (ctypes.c_longlong * 4)()
         _check(load_library().dgtm_get_timing(self._h, ms, nl, nc))
         return {p: {"ms": ms[i], "launches": nl[i], "calls": nc[i]} for i, p in enumerate(PHASES)}
+
+    @property
+    def path(self) -> str:
+        """The implementation of the E-step and responsibility pass:
+        "cuda_cores", "split_bf16" or "exact_slices" (dgtm_get_path)."""
+        out = ctypes.c_int()
+        _check(load_library().dgtm_get_path(self._h, ctypes.byref(out)))
+        return PATHS[out.value]
 
     def stream(self) -> int:
         """cudaStream_t of the context, as an integer handle."""

@@ -6,6 +6,7 @@
 #include "common.cuh"
 #include "kernels.cuh"
 #include "tc.cuh"
+#include "x64.cuh"
 
 #include <math.h>
 #include <stdarg.h>
@@ -77,6 +78,8 @@ struct dgtm_ctx {
     int *hflag;
     // split-BF16 form
     TcState *tc;
+    // exact-slice FP64 form (0/1 data on sm_10x; otherwise the CUDA-core form)
+    XState *x64;
     // phase timers (dgtm_set_timing)
     int timing;
     cudaEvent_t ev[DGTM_NPHASES][2];
@@ -208,6 +211,8 @@ void free_ctx(dgtm_ctx *c)
         cudaFreeHost(c->hflag);
     if (c->tc)
         tc_destroy(c->tc);
+    if (c->x64)
+        x64_destroy(c->x64);
     for (int p = 0; p < DGTM_NPHASES; p++)
         for (int q = 0; q < 2; q++)
             if (c->ev[p][q])
@@ -330,6 +335,13 @@ int dgtm_ctx_create(int N, int D, int K, int M1, const double *T, int ldT, const
         c->nsplit = nsplit;
         c->n_per_split = ceil_div(ceil_div(N, nsplit), 64) * 64;
         c->nsplit = ceil_div(N, c->n_per_split);
+        if (precision == DGTM_FP64) {
+            const int xr = x64_create(&c->x64, N, D, K, c->sms, c->T64, c->stream);
+            if (xr != DGTM_ENOTSUP)
+                CK(xr);
+            if (c->x64)
+                c->nblk1 = x64_pass1_blocks(c->x64);
+        }
         CK(dev_alloc(&c->part, 2 * (size_t) c->nblk1));
         CK(dev_alloc(&c->Gpart, (size_t) c->nsplit * K));
         CK(dev_alloc(&c->RTpart, (size_t) c->nsplit * KD));
@@ -432,7 +444,10 @@ int dgtm_estep(dgtm_ctx *ctx, double beta, int isDA, double temp, double *llh, d
     const double c1 = beta / 2.0, c2 = beta / (2.0 * temp);
     int r, nl = 1;
     DGTM_TRY(phase_begin(ctx, DGTM_PHASE_ESTEP));
-    if (ctx->precision == DGTM_FP64) {
+    if (ctx->x64) {
+        r = x64_estep(ctx->x64, ctx->Y64, ctx->yy, ctx->tt, c1, c2, isDA, ctx->colstat, ctx->part,
+                      ctx->stream, &nl);
+    } else if (ctx->precision == DGTM_FP64) {
         Pass1Args<double> a{ctx->T64, ctx->Y64, ctx->tt, ctx->yy, ctx->N, ctx->D, ctx->K,
                             c1, c2, isDA, ctx->colstat, ctx->part};
         r = launch_pass1_simt<double>(a, ctx->stream);
@@ -452,9 +467,13 @@ int dgtm_estep(dgtm_ctx *ctx, double beta, int isDA, double temp, double *llh, d
                                   cudaMemcpyDeviceToHost, ctx->stream));
     if (ctx->tc)
         DGTM_TRY(tc_fetch_status(ctx->tc, ctx->stream));
+    if (ctx->x64)
+        DGTM_TRY(x64_fetch_status(ctx->x64, ctx->stream));
     DGTM_TRY(sync_and_check(ctx));
     if (ctx->tc)
         DGTM_TRY(tc_check_status(ctx->tc));
+    if (ctx->x64)
+        DGTM_TRY(x64_check_status(ctx->x64));
     const double S1 = ctx->hscal[0], S2 = ctx->hscal[1];
     // comm/mpicomm.c:483-497
     const int N = ctx->N, K = ctx->K, D = ctx->D;
@@ -491,7 +510,9 @@ int dgtm_mstep(dgtm_ctx *ctx, double *W, int ldW, double *Y, int ldY, double *be
     // substitution, or one eigen kernel), update_y, the beta sum, the reduction
     int npass = 1, nsmall = 4 + ((ctx->solver == DGTM_SOLVE_SVD) ? 1 : 2);
     DGTM_TRY(phase_begin(ctx, DGTM_PHASE_MSTEP_PASS));
-    if (ctx->precision == DGTM_FP64) {
+    if (ctx->x64) {
+        DGTM_TRY(x64_mstep_pass(ctx->x64, c, ctx->G, ctx->RT, ctx->stream, &npass));
+    } else if (ctx->precision == DGTM_FP64) {
         Pass2Args<double> a{ctx->T64, ctx->Y64, ctx->tt, ctx->yy, ctx->colstat, N, D, K, c,
                             ctx->n_per_split, ctx->Gpart, ctx->RTpart};
         DGTM_TRY(launch_pass2_simt<double>(a, ctx->nsplit, ctx->stream));
@@ -508,7 +529,7 @@ int dgtm_mstep(dgtm_ctx *ctx, double *W, int ldW, double *Y, int ldY, double *be
         int nr = 0;
         DGTM_TRY(tc_mstep_reduce(ctx->tc, ctx->G, ctx->RT, ctx->stream, &nr));
         nsmall += nr;
-    } else {
+    } else if (!ctx->x64) {
         DGTM_TRY(launch_reduce_slices(ctx->Gpart, ctx->RTpart, ctx->nsplit, K, D, ctx->G,
                                       ctx->RT, ctx->stream));
         nsmall += 1;
@@ -637,6 +658,17 @@ int dgtm_get_stream(dgtm_ctx *ctx, void **stream)
         return DGTM_EINVAL;
     }
     *stream = (void *) ctx->stream;
+    return DGTM_OK;
+}
+
+int dgtm_get_path(dgtm_ctx *ctx, int *path)
+{
+    DGTM_TRY(check_ctx(ctx));
+    if (!path) {
+        set_error(DGTM_EINVAL, "path is null");
+        return DGTM_EINVAL;
+    }
+    *path = ctx->x64 ? DGTM_PATH_EXACT_SLICES : ctx->tc ? DGTM_PATH_SPLIT_BF16 : DGTM_PATH_CUDA_CORES;
     return DGTM_OK;
 }
 
@@ -808,8 +840,33 @@ int dgtm_next_ctemp_k(dgtm_ctx *ctx, double temp, double beta, double eps, const
                             ctx->stream);
         if (rc == DGTM_OK)
             rc = tc_fetch_status(ctx->tc, ctx->stream);
-        if (rc == DGTM_OK && (e = cudaStreamSynchronize(ctx->stream)) == cudaSuccess)
+        if (rc == DGTM_OK)
+            e = cudaMemcpyAsync(gsum.data(), dgsum, sizeof(double) * K, cudaMemcpyDeviceToHost,
+                                ctx->stream);
+        if (rc == DGTM_OK && e == cudaSuccess && (e = cudaStreamSynchronize(ctx->stream)) == cudaSuccess)
             rc = tc_check_status(ctx->tc);
+        // A centre far from every point has all its responsibilities below the
+        // FP32 planes' 2^-126, so its scatter there is zero (row sum 0: the
+        // reference's HUGE_VAL) while the FP64 reference still forms it.  Such
+        // centres (row sum below 1e-25: any flushed tail is then 1e-13 of the
+        // rest) are redone by the CUDA-core scatter, whose R is FP64.
+        std::vector<int> redo;
+        for (int k = 0; rc == DGTM_OK && e == cudaSuccess && k < K; k++)
+            if (!(gsum[k] >= 1e-25))
+                redo.push_back(k);
+        if (!redo.empty())
+            rc = dev_alloc(&scratch, (pl.scratch_bytes + sizeof(double) - 1) / sizeof(double));
+        for (size_t i = 0; rc == DGTM_OK && i < redo.size();) {
+            const int k0 = redo[i];
+            int nb = 1;
+            while (i + nb < redo.size() && redo[i + nb] == k0 + nb && nb < kb)
+                nb++;
+            rc = launch_ctemp_batch(pl, ctx->T64, ctx->T32, ctx->Y64, ctx->tt, ctx->yy,
+                                    ctx->colstat, N, D, K, c, k0, nb, gg ? dgg + k0 : nullptr,
+                                    lim_scale, scratch, dgsum + k0, dout + (size_t) 2 * k0,
+                                    ctx->stream);
+            i += nb;
+        }
     }
     for (int k0 = 0; !pairs && rc == DGTM_OK && e == cudaSuccess && k0 < K; k0 += kb) {
         const int nb = (K - k0 < kb) ? K - k0 : kb;

@@ -201,6 +201,18 @@ int dgtm_get_timing(dgtm_ctx *ctx, double *ms, long long *launches, long long *c
  * order their own work or events against it. */
 int dgtm_get_stream(dgtm_ctx *ctx, void **stream);
 
+/* Which implementation runs the context's E-step and responsibility pass
+ * (informational; no reference counterpart).  DGTM_FP64 contexts on 0/1 data
+ * (D <= 189, K <= 60000) on an sm_10x GPU use the exact-slice path: distance
+ * products from fixed-point digit slices of the centres on the tensor cores
+ * (exact integers), exponentials and sums in double-float and 2^-48 fixed
+ * point.  Setting DGTM_X64=0 before dgtm_ctx_create keeps them on the
+ * CUDA-core FP64 kernels. */
+#define DGTM_PATH_CUDA_CORES 0
+#define DGTM_PATH_SPLIT_BF16 1
+#define DGTM_PATH_EXACT_SLICES 2
+int dgtm_get_path(dgtm_ctx *ctx, int *path);
+
 /*
  * Annealed free energy and its gradient on caller-owned device arrays, for
  * gradient-based refinement (torch.autograd) and the projection of new points:
