@@ -314,7 +314,7 @@ template <typename F>
 int run_batch(const CtempPlan &pl, const double *T64, const float *T32, const double *Y,
               const double *tt, const double *yy, const double2 *colstat, int N, int D, int K,
               double c, int k0, int kb, const double *gg_dev, double lim_scale, void *scratch,
-              double *gsum_dev, double *out_dev, cudaStream_t s)
+              double *gsum_dev, double *out_dev, double dcut, cudaStream_t s)
 {
     unsigned char *base = (unsigned char *) scratch;
     double *S = (double *) base;
@@ -330,7 +330,8 @@ int run_batch(const CtempPlan &pl, const double *T64, const float *T32, const do
     const int ntp = ((D + SC_TILE - 1) / SC_TILE) * ((D + SC_TILE - 1) / SC_TILE + 1) / 2;
     for (int n0 = 0; n0 < N; n0 += pl.nn) {
         const int nn = (N - n0 < pl.nn) ? N - n0 : pl.nn;
-        int r = launch_r_block(T64, Y, tt, yy, colstat, D, K, c, k0, kb, n0, nn, Rb, s);
+        int r = launch_r_block(T64, Y, tt, yy, colstat, D, K, c, k0, kb, n0, nn, Rb, s, nullptr,
+                               nullptr, dcut);
         if (r != DGTM_OK)
             return r;
         const F *Tc;
@@ -399,13 +400,14 @@ int launch_ctemp_eig(const CtempPlan &pl, int kb, int D, const double *S, void *
 int launch_ctemp_batch(const CtempPlan &pl, const double *T64, const float *T32, const double *Y,
                        const double *tt, const double *yy, const double2 *colstat, int N, int D,
                        int K, double c, int k0, int kb, const double *gg_dev, double lim_scale,
-                       void *scratch, double *gsum_dev, double *out_dev, cudaStream_t s)
+                       void *scratch, double *gsum_dev, double *out_dev, double dcut,
+                       cudaStream_t s)
 {
     if (pl.f32)
         return run_batch<float>(pl, T64, T32, Y, tt, yy, colstat, N, D, K, c, k0, kb, gg_dev,
-                                lim_scale, scratch, gsum_dev, out_dev, s);
+                                lim_scale, scratch, gsum_dev, out_dev, dcut, s);
     return run_batch<double>(pl, T64, T32, Y, tt, yy, colstat, N, D, K, c, k0, kb, gg_dev,
-                             lim_scale, scratch, gsum_dev, out_dev, s);
+                             lim_scale, scratch, gsum_dev, out_dev, dcut, s);
 }
 
 }  // namespace dgtm

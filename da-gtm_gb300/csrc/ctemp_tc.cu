@@ -59,9 +59,11 @@ constexpr int RP_TILES = 32;     // tiles per CTA
 constexpr int RP_BK = 128;       // centres per CTA (MMA M)
 
 struct RPParams {
-    int Kpad, Dp, n0, ntile, nc, nstage;  // chunk: points n0 .. n0 + nc, nc = 64 ntile
-    const uint32_t *Yb;                   // 2 x Kpad x Dp BF16 (as pairs)
+    int Kpad, Dp, n0, ntile, nc, nstage, N;  // chunk: points n0 .. n0 + nc, nc = 64 ntile
+    const uint32_t *Yb;                      // 2 x Kpad x Dp BF16 (as pairs)
     const float4 *colq;
+    const double *tt;                        // N: |t_n|^2
+    double dcut;                             // R = 0 where d > dcut
     uint32_t *planes;                     // 4 x Kpad x nc BF16 (as pairs): R hi, R lo, R^2 hi, R^2 lo
     int *status;
 };
@@ -220,6 +222,13 @@ __global__ void __launch_bounds__(RP_THREADS, 1)
                     const float4 c0 = cq[2 * e], c1 = cq[2 * e + 1];
                     float r0 = ex2(fmaf(__uint_as_float(va[2 * e]) - c0.x, c0.y, -c0.z));
                     float r1 = ex2(fmaf(__uint_as_float(va[2 * e + 1]) - c1.x, c1.y, -c1.z));
+                    // R = 0 where d = |t|^2 - 2 acc > dcut, as the reference's
+                    // exp(-beta d / 2) underflows there
+                    const int na = p.n0 + nl + 2 * e;
+                    if (na < p.N && __uint_as_float(va[2 * e]) < (float) (0.5 * (p.tt[na] - p.dcut)))
+                        r0 = 0.f;
+                    if (na + 1 < p.N && __uint_as_float(va[2 * e + 1]) < (float) (0.5 * (p.tt[na + 1] - p.dcut)))
+                        r1 = 0.f;
                     if (pl >= 2) {
                         r0 *= r0;
                         r1 *= r1;
@@ -511,7 +520,7 @@ __global__ void assemble_kernel(const float *__restrict__ Q, int Kpad, int DUpad
 }  // namespace
 
 int tc_ctemp_pairs(const TcView &v, const double *Y64, const double *gg_dev, double lim_scale,
-                   size_t budget, double *gsum_dev, double *out_dev, cudaStream_t s)
+                   size_t budget, double dcut, double *gsum_dev, double *out_dev, cudaStream_t s)
 {
     const int N = v.N, D = v.D, K = v.K;
     if (!v.binary || v.nT != 1 || v.npanel > 3) {
@@ -624,6 +633,9 @@ int tc_ctemp_pairs(const TcView &v, const double *Y64, const double *gg_dev, dou
         rp.nstage = rp_stages;
         rp.Yb = (const uint32_t *) v.Yb;
         rp.colq = v.colq;
+        rp.N = v.N;
+        rp.tt = v.tt;
+        rp.dcut = dcut;
         rp.planes = planes;
         rp.status = v.status;
         rpk<<<dim3(ktiles, (rp.ntile + RP_TILES - 1) / RP_TILES), RP_THREADS, rp_smem, s>>>(tmT, rp);

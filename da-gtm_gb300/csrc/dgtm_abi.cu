@@ -511,14 +511,14 @@ int dgtm_mstep(dgtm_ctx *ctx, double *W, int ldW, double *Y, int ldY, double *be
     int npass = 1, nsmall = 4 + ((ctx->solver == DGTM_SOLVE_SVD) ? 1 : 2);
     DGTM_TRY(phase_begin(ctx, DGTM_PHASE_MSTEP_PASS));
     if (ctx->x64) {
-        DGTM_TRY(x64_mstep_pass(ctx->x64, c, ctx->G, ctx->RT, ctx->stream, &npass));
+        DGTM_TRY(x64_mstep_pass(ctx->x64, c, ctx->G, ctx->RT, ctx->stream, &npass));  // cut: pass 1
     } else if (ctx->precision == DGTM_FP64) {
         Pass2Args<double> a{ctx->T64, ctx->Y64, ctx->tt, ctx->yy, ctx->colstat, N, D, K, c,
-                            ctx->n_per_split, ctx->Gpart, ctx->RTpart};
+                            ctx->n_per_split, ctx->Gpart, ctx->RTpart, ref_dcut(ctx->beta)};
         DGTM_TRY(launch_pass2_simt<double>(a, ctx->nsplit, ctx->stream));
     } else if (ctx->precision == DGTM_FP32) {
         Pass2Args<float> a{ctx->T32, ctx->Y32, ctx->tt, ctx->yy, ctx->colstat, N, D, K, c,
-                           ctx->n_per_split, ctx->Gpart, ctx->RTpart};
+                           ctx->n_per_split, ctx->Gpart, ctx->RTpart, ref_dcut(ctx->beta)};
         DGTM_TRY(launch_pass2_simt<float>(a, ctx->nsplit, ctx->stream));
     } else {
         DGTM_TRY(tc_mstep_pass(ctx->tc, ctx->colstat, c, ctx->stream, &npass));
@@ -746,10 +746,12 @@ int r_block_impl(dgtm_ctx *ctx, int k0, int nk, int n0, int nn, double *R, int l
     const double c = ctx->isDA ? ctx->beta / (2.0 * ctx->temp) : ctx->beta / 2.0;
     double *dR = nullptr;
     DGTM_TRY(dev_alloc(&dR, (size_t) nk * nn));
+    // R_kn = 0 where the reference's exp(-beta d / 2) underflows
+    const double dcut = ref_dcut(ctx->beta);
     int r = rd ? launch_r_block(ctx->T64, ctx->Yprev, ctx->tt, ctx->yyprev, ctx->colstat, ctx->D,
-                                ctx->K, c, k0, nk, n0, nn, dR, ctx->stream, ctx->Y64, ctx->yy)
+                                ctx->K, c, k0, nk, n0, nn, dR, ctx->stream, ctx->Y64, ctx->yy, dcut)
                : launch_r_block(ctx->T64, ctx->Y64, ctx->tt, ctx->yy, ctx->colstat, ctx->D, ctx->K,
-                                c, k0, nk, n0, nn, dR, ctx->stream);
+                                c, k0, nk, n0, nn, dR, ctx->stream, nullptr, nullptr, dcut);
     cudaError_t e = cudaSuccess;
     if (r == DGTM_OK)
         e = copy_rows(R, sizeof(double) * (size_t) ldR, dR, sizeof(double) * nn,
@@ -836,8 +838,8 @@ int dgtm_next_ctemp_k(dgtm_ctx *ctx, double temp, double beta, double eps, const
         TcView v;
         tc_view(ctx->tc, &v);
         const size_t gbudget = (size_t) env_int("DGTM_CTEMP_GEMM_MB", 8192, 64, 1 << 22) << 20;
-        rc = tc_ctemp_pairs(v, ctx->Y64, gg ? dgg : nullptr, lim_scale, gbudget, dgsum, dout,
-                            ctx->stream);
+        rc = tc_ctemp_pairs(v, ctx->Y64, gg ? dgg : nullptr, lim_scale, gbudget, ref_dcut(ctx->beta),
+                            dgsum, dout, ctx->stream);
         if (rc == DGTM_OK)
             rc = tc_fetch_status(ctx->tc, ctx->stream);
         if (rc == DGTM_OK)
@@ -864,7 +866,7 @@ int dgtm_next_ctemp_k(dgtm_ctx *ctx, double temp, double beta, double eps, const
             rc = launch_ctemp_batch(pl, ctx->T64, ctx->T32, ctx->Y64, ctx->tt, ctx->yy,
                                     ctx->colstat, N, D, K, c, k0, nb, gg ? dgg + k0 : nullptr,
                                     lim_scale, scratch, dgsum + k0, dout + (size_t) 2 * k0,
-                                    ctx->stream);
+                                    ref_dcut(ctx->beta), ctx->stream);
             i += nb;
         }
     }
@@ -872,7 +874,8 @@ int dgtm_next_ctemp_k(dgtm_ctx *ctx, double temp, double beta, double eps, const
         const int nb = (K - k0 < kb) ? K - k0 : kb;
         rc = launch_ctemp_batch(pl, ctx->T64, ctx->T32, ctx->Y64, ctx->tt, ctx->yy, ctx->colstat,
                                 N, D, K, c, k0, nb, gg ? dgg + k0 : nullptr, lim_scale, scratch,
-                                dgsum + k0, dout + (size_t) 2 * k0, ctx->stream);
+                                dgsum + k0, dout + (size_t) 2 * k0, ref_dcut(ctx->beta),
+                                ctx->stream);
     }
     if (rc == DGTM_OK && e == cudaSuccess)
         e = cudaMemcpyAsync(out.data(), dout, sizeof(double) * 2 * K, cudaMemcpyDeviceToHost,

@@ -317,7 +317,7 @@ __global__ void __launch_bounds__(NT) pass2_simt_kernel(Pass2Args<F> a)
                             dd = ((double) (F(-2) * acc[i][j]) + yyk[i]) + ttn;
                         else
                             dd = (double) ((F(-2) * acc[i][j] + (F) yyk[i]) + (F) ttn);
-                        r = fexp<F>((F) (-a.c * (dd - dmn) - lsn));
+                        r = (dd > a.dcut) ? F(0) : fexp<F>((F) (-a.c * (dd - dmn) - lsn));
                     }
                 }
                 g[i] += (double) r;
@@ -513,7 +513,7 @@ __global__ void r_block_kernel(const double *__restrict__ T, const double *__res
                                const double *__restrict__ tt, const double *__restrict__ yy,
                                const double2 *__restrict__ colstat, int D, int K, double c,
                                int k0, int nk, int n0, int nn, const double *__restrict__ Y2,
-                               const double *__restrict__ yy2, double *__restrict__ R)
+                               const double *__restrict__ yy2, double dcut, double *__restrict__ R)
 {
     const size_t total = (size_t) nk * nn;
     for (size_t i = blockIdx.x * (size_t) blockDim.x + threadIdx.x; i < total;
@@ -528,7 +528,7 @@ __global__ void r_block_kernel(const double *__restrict__ T, const double *__res
             for (int d = 0; d < D; d++)
                 dot += Y[(size_t) k * D + d] * T[(size_t) n * D + d];
             const double dd = ((-2.0 * dot) + yy[k]) + tt[n];
-            r = exp(-c * (dd - cs.x) - cs.y);
+            r = (dd > dcut) ? 0.0 : exp(-c * (dd - cs.x) - cs.y);
         }
         if (Y2) {
             double dot = 0.0;
@@ -563,13 +563,13 @@ int launch_map(const double *T, const double *Y, const double *tt, const double 
 
 int launch_r_block(const double *T, const double *Y, const double *tt, const double *yy,
                    const double2 *colstat, int D, int K, double c, int k0, int nk, int n0, int nn,
-                   double *R, cudaStream_t s, const double *Y2, const double *yy2)
+                   double *R, cudaStream_t s, const double *Y2, const double *yy2, double dcut)
 {
     size_t blocks = ((size_t) nk * nn + 255) / 256;
     if (blocks > 8192)
         blocks = 8192;
     r_block_kernel<<<(unsigned) blocks, 256, 0, s>>>(T, Y, tt, yy, colstat, D, K, c, k0, nk, n0,
-                                                    nn, Y2, yy2, R);
+                                                    nn, Y2, yy2, dcut, R);
     DGTM_CUDA_TRY(cudaGetLastError());
     return DGTM_OK;
 }

@@ -1907,6 +1907,7 @@ void tc_view(const TcState *st, TcView *v)
     v->Tb = st->Tb;
     v->Yb = st->Yb;
     v->colq = st->colq;
+    v->tt = st->tt;
     v->status = st->status;
 }
 

@@ -208,7 +208,9 @@ struct X1Params {
     const double *tt;
     double2 *colstat;  // N: (d_ref, log s_n)
     float4 *refq;      // Npad: the reference centre's four slice partials
-    float4 *lsq;       // Npad: (-log s_n as a double-float, flag, 0); flag 1: zero column, 2: padding
+    float4 *lsq;       // Npad: (-log s_n as a double-float, flag, cut); flag 1: zero column,
+                       // 2: padding; R_kn = 0 where I_kn - I_ref < cut (d_kn > dcut)
+    double dcut;       // the reference's exp(-beta d / 2) underflows beyond it
     double *part;      // 2 per CTA
     int *status;
 };
@@ -491,7 +493,9 @@ __global__ void __launch_bounds__(X1_THREADS, 1)
             p.colstat[n] = make_double2(dstar, lsn);
             p.refq[n] = make_float4(r0, r1, r2, r3);
             const df::f2x L = df::from_double(flag != 0.f ? 0.0 : lsel);
-            p.lsq[n] = make_float4(-L.h, -L.l, flag, 0.f);
+            // d_kn > dcut <=> acc_kn < (|t_n|^2 - dcut) / 2 <=> I_kn - I_ref below this
+            const double cut = fmax(ldexp(0.5 * (p.tt[n] - p.dcut), p.sc->F) - Iref, -1e38);
+            p.lsq[n] = make_float4(-L.h, -L.l, flag, (float) cut);
         } else if (n < p.Npad) {
             p.refq[n] = make_float4(0.f, 0.f, 0.f, 0.f);
             p.lsq[n] = make_float4(0.f, 0.f, 2.f, 0.f);
@@ -852,7 +856,9 @@ __global__ void __launch_bounds__(X2_THREADS, 1)
                         if (flag == 0) {
                             const df::f2x dI = df::sum4(fmaf(fu(va[c]), 0x1p40f, -R0), fmaf(fu(va[8 + c]), 0x1p24f, -R1),
                                                         fmaf(fu(va[16 + c]), 256.f, -R2), fu(va[24 + c]) - rq.w);
-                            df::fixed48_parts(df::exp_df(df::add(df::mul(dI, kc), nls), tab), tp, bt);
+                            // R = 0 where the reference's exp(-beta d / 2) underflows
+                            if (!(dI.h < lq.w))
+                                df::fixed48_parts(df::exp_df(df::add(df::mul(dI, kc), nls), tab), tp, bt);
                         } else if (flag == 1) {
                             // comm/mpicomm.c:382-389: R = 1/K
                             tp = (uint32_t) (rinvK >> 24);
@@ -1149,6 +1155,7 @@ int x64_estep(XState *st, const double *Y64, const double *yy, const double *tt,
     p.two_temps = isDA && (c1 != c2);
     p.c1 = c1;
     p.c2 = c2;
+    p.dcut = ref_dcut(2.0 * c1);
     p.sc = st->sc;
     p.tt = tt;
     p.colstat = colstat;

@@ -32,7 +32,15 @@ struct Pass2Args {
     int n_per_split;
     double *Gpart;       // nsplit x K
     double *RTpart;      // nsplit x K x D
+    // R_kn = 0 where d_kn > dcut: the reference forms exp(-beta d / 2) first,
+    // which is 0 beyond 745.13 / (beta/2) (ref_dcut); no cut by default
+    double dcut = 1e300;
 };
+
+// The distance beyond which the reference's responsibility is exactly 0:
+// exp(-beta d / 2) underflows in FP64 (comm/mpicomm.c:326-336 scales D by
+// -beta/2 and exponentiates before tempering and normalising).
+inline double ref_dcut(double beta) { return 745.1332191019412 / (0.5 * beta); }
 
 template <typename F> int launch_pass1_simt(const Pass1Args<F> &a, cudaStream_t s);
 // own = true: statistics indexed by the owner rows (see estep_simt.cu).
@@ -50,7 +58,7 @@ int launch_map(const double *T, const double *Y, const double *tt, const double 
 int launch_r_block(const double *T, const double *Y, const double *tt, const double *yy,
                    const double2 *colstat, int D, int K, double c, int k0, int nk, int n0, int nn,
                    double *R, cudaStream_t s, const double *Y2 = nullptr,
-                   const double *yy2 = nullptr);
+                   const double *yy2 = nullptr, double dcut = 1e300);
 
 // ---- M-step (FP64, all forms) ---------------------------------------------------
 // Sum nsplit slices in a fixed order: G[k] = sum_s Gpart[s][k], RT = sum_s RTpart[s].
@@ -96,10 +104,12 @@ CtempPlan ctemp_plan(int N, int D, int K, bool f32, bool have_t32, size_t budget
 // eigenvalue of 2 S1 (w = 0) / 2 (S1 - S2) (w = 1) below lim_scale * gg_i
 // (eigenvalues at or above it count as 0).  gg_dev null: gg = gsum.  T32: the
 // context's FP32 copy of T, or null (an FP32 plan then converts each chunk).
+// R is the FP64 R of the R blocks, 0 where d > dcut (ref_dcut).
 int launch_ctemp_batch(const CtempPlan &pl, const double *T64, const float *T32, const double *Y,
                        const double *tt, const double *yy, const double2 *colstat, int N, int D,
                        int K, double c, int k0, int kb, const double *gg_dev, double lim_scale,
-                       void *scratch, double *gsum_dev, double *out_dev, cudaStream_t s);
+                       void *scratch, double *gsum_dev, double *out_dev, double dcut,
+                       cudaStream_t s);
 // yy = |y|^2 for a given Y.
 int launch_norms(const double *X, int rows, int D, double *out, cudaStream_t s);
 // out[r] = |x_r|^2 in FP64 for an FP32 row-major matrix (rows x D).

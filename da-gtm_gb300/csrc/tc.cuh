@@ -63,6 +63,7 @@ struct TcView {
     const void *Tb;       // nT x Npad x Dp BF16: data pieces, columns D..D+2 = 1
     const void *Yb;       // 2 x Kpad x Dp BF16: centre pieces, -|y|^2/2 at D..D+2 of hi
     const float4 *colq;   // Npad: (m, scale, log2 s) of the last E-step
+    const double *tt;     // N: |t_n|^2
     int *status;          // bounded-wait status word
 };
 void tc_view(const TcState *st, TcView *v);
@@ -73,7 +74,8 @@ void tc_view(const TcState *st, TcView *v);
 // upper triangles, written per batch of centres as the CUDA-core scatter
 // writes them; then the eigen filter of ctemp.cu.  out[2 k + w] as in
 // launch_ctemp_batch; gsum[k] = row sums of R.
+// R_kn = 0 where d_kn > dcut (the reference's exp(-beta d / 2) underflows).
 int tc_ctemp_pairs(const TcView &v, const double *Y64, const double *gg_dev, double lim_scale,
-                   size_t budget, double *gsum_dev, double *out_dev, cudaStream_t s);
+                   size_t budget, double dcut, double *gsum_dev, double *out_dev, cudaStream_t s);
 
 }  // namespace dgtm

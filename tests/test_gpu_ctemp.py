@@ -121,14 +121,16 @@ def test_pair_feature_gemm_chunks_and_segments(pkg, monkeypatch, pairs_case, gem
     np.testing.assert_allclose(got_k, simt_k, rtol=1e-4)
 
 
-def test_pair_feature_gemm_far_centres(pkg, orc, monkeypatch):
-    """Two centres far from every point: their responsibilities (~1e-90) are
-    below the split form's FP32 planes, so the pair-feature GEMM sees a zero
-    row; they are redone from FP64 responsibilities and match the oracle's
-    centre by centre."""
+@pytest.mark.parametrize("far,finite", [(6.0, True), (8.0, False)])
+def test_pair_feature_gemm_far_centres(pkg, orc, monkeypatch, far, finite):
+    """A centre far from every point.  At 6 (beta d / 2 ~ 470) its
+    responsibilities (~1e-52) are below the split form's FP32 planes, so the
+    pair-feature GEMM sees a zero row: it is redone from FP64 responsibilities
+    and matches the oracle.  At 8 (beta d / 2 ~ 865) the reference's
+    exp(-beta d / 2) underflows, its responsibilities are exactly 0 and
+    comm/mpicomm.c:574-577 makes the critical temperature HUGE_VAL: so here."""
     T, FI, Y = problem(pkg, "binary", 3000, 166, 16, seed=13)
-    Y[3] = 8.0
-    Y[9] = 8.5
+    Y[9] = far
     beta, temp, eps = 30.0 / 166, 4.0, 1e-6
     ref, R = oracle_ctemp(orc, T, Y, beta, temp, eps)
     with pkg.Context(T, FI, "bf16x3") as c:
@@ -137,11 +139,17 @@ def test_pair_feature_gemm_far_centres(pkg, orc, monkeypatch):
         got, got_k = c.next_ctemp(temp, beta, eps, per_centre=True)
         monkeypatch.setenv("DGTM_CTEMP_PAIRS", "0")
         simt, simt_k = c.next_ctemp(temp, beta, eps, per_centre=True)
-    assert R[3].sum() > 0.0 and R[3].max() < 1e-60
-    assert np.all(np.isfinite(got_k)) and np.all(np.isfinite(simt_k))
-    assert got_k[3] == simt_k[3] and got_k[9] == simt_k[9]  # the same FP64-R scatter
-    np.testing.assert_allclose(got_k, simt_k, rtol=1e-4)
-    assert got == pytest.approx(ref, rel=1e-4)
+    assert got_k[9] == simt_k[9]  # both from the same FP64-R scatter
+    if finite:
+        assert 0.0 < R[9].sum() < 1e-40
+        assert np.all(np.isfinite(got_k)) and np.isfinite(got)
+        np.testing.assert_allclose(got_k, simt_k, rtol=1e-4)
+        assert got == pytest.approx(ref, rel=1e-4)
+    else:
+        assert R[9].sum() == 0.0 and ref == np.inf
+        assert got == simt == np.inf and got_k[9] == np.inf
+        keep = np.arange(16) != 9
+        np.testing.assert_allclose(got_k[keep], simt_k[keep], rtol=1e-4)
 
 
 def test_next_ctemp_oil(pkg, orc, golden):

@@ -4,15 +4,16 @@ qualities, the M-step of comm/comm.c:1299-1348) and against the CUDA-core
 FP64 form of the same library (DGTM_X64=0).
 
 Distances are exact integers from the tensor cores (fixed-point digit slices
-of the centres on a 2^-F grid, 2^-52 of the largest centre value), the
-exponentials and the per-point sums are double-float (~2^-47) and 2^-48 fixed
-point.  Tolerances are the FP64 form's: 1e-12 on the qualities, G and R T,
+of the centres on a 2^-F grid, 2^-52 of the largest centre value or |y|^2/2m),
+the exponentials double-float (~2^-47), the per-point sums 128-bit fixed point
+at 2^-63 and the responsibilities of R T 2^-48 fixed point.  Tolerances are the FP64 form's: 1e-12 on the qualities, G and R T,
 1e-13 absolute on R, 1e-9 on beta and the new centres.
 
 Shapes cover the three panel counts (D = 20, 100, 166, 189: 1, 2 and 3
 panels of 64, and 3 columns of -|y|^2/2 pieces at D = 189), ragged N and K,
 several 16384-point units and 256-point segments per centre block, both
-temperatures of the E-step, and the zero-column fallback.
+temperatures of the E-step, the zero-column fallback and the reference's
+underflow of exp(-beta d / 2).
 """
 import importlib
 
@@ -154,3 +155,30 @@ def test_zero_column_fallback_exact_slices(pkg, orc):
             assert nfree == pytest.approx(o["nfree"], rel=1e-12)
         else:
             assert llh == pytest.approx(o["llh"], rel=1e-12)
+
+
+@pytest.mark.parametrize("x64", ["1", "0"])
+def test_reference_underflow_rule(pkg, orc, monkeypatch, x64):
+    """The reference forms exp(-beta d / 2) before tempering
+    (comm/mpicomm.c:326-336): a responsibility whose beta d / 2 exceeds 745.13
+    is exactly 0 there.  A centre that far from every point has R = 0, G = 0,
+    and a critical temperature of HUGE_VAL; both FP64 paths follow."""
+    monkeypatch.setenv("DGTM_X64", x64)
+    N, D, K = 2000, 166, 24
+    T, FI, Y = problem(N, D, K, seed=7)
+    Y[5] = 8.0
+    beta, temp = 30.0 / D, 4.0
+    o = oracle_step(orc, T, Y, FI, beta, 1, temp)
+    assert o["R"][5].max() == 0.0
+    with pkg.Context(T, FI, "fp64") as c:
+        assert c.path == ("exact_slices" if x64 == "1" else "cuda_cores")
+        c.set_Y(Y)
+        llh, nfree = c.estep(beta, 1, temp)
+        R = c.R_block(0, K, 0, N)
+        ct = c.next_ctemp(temp, beta, 1e-6)
+        c.mstep()
+        G, RT = c.get_stats()
+    assert np.all(R[5] == 0.0) and G[5] == 0.0 and np.all(RT[5] == 0.0)
+    assert np.max(np.abs(R - o["R"])) <= 1e-13
+    assert rel(G, o["G"]) <= 1e-12 and rel(RT, o["RT"]) <= 1e-12
+    assert ct == orc.next_ctemp(T, Y, o["R"], o["G"], temp, beta, 1e-6) == np.inf
