@@ -397,6 +397,41 @@ int launch_ctemp_eig(const CtempPlan &pl, int kb, int D, const double *S, void *
     return launch_eig<1024, double>(kb, D, pl.eig_in_smem, S, M, gg, lim_scale, out, s);
 }
 
+namespace {
+
+__global__ void gather_centres_kernel(const double *__restrict__ Y, const double *__restrict__ yy,
+                                      const double *__restrict__ gg, const int *__restrict__ idx,
+                                      int n, int D, double *__restrict__ Ys, double *__restrict__ yys,
+                                      double *__restrict__ ggs)
+{
+    const size_t total = (size_t) n * D;
+    for (size_t i = blockIdx.x * (size_t) blockDim.x + threadIdx.x; i < total;
+         i += (size_t) gridDim.x * blockDim.x) {
+        const int r = (int) (i / D), d = (int) (i % D);
+        const int k = idx[r];
+        Ys[i] = Y[(size_t) k * D + d];
+        if (d == 0) {
+            yys[r] = yy[k];
+            if (gg)
+                ggs[r] = gg[k];
+        }
+    }
+}
+
+}  // namespace
+
+int launch_gather_centres(const double *Y, const double *yy, const double *gg, const int *idx,
+                          int n, int D, double *Ys, double *yys, double *ggs, cudaStream_t s)
+{
+    size_t blocks = ((size_t) n * D + 255) / 256;
+    if (blocks > 4096)
+        blocks = 4096;
+    gather_centres_kernel<<<(unsigned) (blocks ? blocks : 1), 256, 0, s>>>(Y, yy, gg, idx, n, D, Ys,
+                                                                          yys, ggs);
+    DGTM_CUDA_TRY(cudaGetLastError());
+    return DGTM_OK;
+}
+
 int launch_ctemp_batch(const CtempPlan &pl, const double *T64, const float *T32, const double *Y,
                        const double *tt, const double *yy, const double2 *colstat, int N, int D,
                        int K, double c, int k0, int kb, const double *gg_dev, double lim_scale,

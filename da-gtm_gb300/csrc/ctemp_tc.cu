@@ -64,6 +64,7 @@ struct RPParams {
     const float4 *colq;
     const double *tt;                        // N: |t_n|^2
     double dcut;                             // R = 0 where d > dcut
+    float *dmin;                             // Kpad: each centre's least distance (FP32)
     uint32_t *planes;                     // 4 x Kpad x nc BF16 (as pairs): R hi, R lo, R^2 hi, R^2 lo
     int *status;
 };
@@ -197,6 +198,7 @@ __global__ void __launch_bounds__(RP_THREADS, 1)
         }
         const size_t plane = (size_t) p.Kpad * p.nc / 2;  // uint32 per plane
         uint32_t *out = p.planes + ((size_t) k * p.nc) / 2;
+        float dm = INFINITY;  // this row's least distance over its points
         bool ok = true;
         for (int j = 0; j < ntl; j++) {
             const int b = j & 1;
@@ -212,6 +214,12 @@ __global__ void __launch_bounds__(RP_THREADS, 1)
             mbar_arrive(&s_free[b]);
             const int nl = (j0 + j) * RP_TILE + g * 32;  // point within the chunk
             const float4 *cq = p.colq + p.n0 + nl;
+#pragma unroll 8
+            for (int e = 0; e < 32; e++) {
+                const int na = p.n0 + nl + e;
+                if (na < p.N)
+                    dm = fminf(dm, (float) p.tt[na] - 2.0f * __uint_as_float(va[e]));
+            }
 #pragma unroll
             for (int pl = 0; pl < 4; pl++) {
                 // plane pl: R hi, R lo, R^2 hi, R^2 lo; one plane at a time keeps
@@ -242,6 +250,9 @@ __global__ void __launch_bounds__(RP_THREADS, 1)
                     dst[i] = make_uint4(w[4 * i], w[4 * i + 1], w[4 * i + 2], w[4 * i + 3]);
             }
         }
+        // non-negative floats order like their bit patterns
+        if (dm < INFINITY)
+            atomicMin((int *) &p.dmin[k], __float_as_int(fmaxf(dm, 0.f)));
         if (!ok)
             failed = 1;
     }
@@ -520,7 +531,8 @@ __global__ void assemble_kernel(const float *__restrict__ Q, int Kpad, int DUpad
 }  // namespace
 
 int tc_ctemp_pairs(const TcView &v, const double *Y64, const double *gg_dev, double lim_scale,
-                   size_t budget, double dcut, double *gsum_dev, double *out_dev, cudaStream_t s)
+                   size_t budget, double dcut, double *gsum_dev, double *out_dev, float *dmin_dev,
+                   cudaStream_t s)
 {
     const int N = v.N, D = v.D, K = v.K;
     if (!v.binary || v.nT != 1 || v.npanel > 3) {
@@ -586,6 +598,8 @@ int tc_ctemp_pairs(const TcView &v, const double *Y64, const double *gg_dev, dou
         e = cudaMemcpyAsync(pairs, h.data(), sizeof(ushort2) * npair, cudaMemcpyHostToDevice, s);
         if (e == cudaSuccess)
             e = cudaMemsetAsync(Q, 0, qbytes, s);
+        if (e == cudaSuccess)  // 0x7F7F7F7F: 3.4e38, above every distance
+            e = cudaMemsetAsync(dmin_dev, 0x7F, sizeof(float) * (size_t) Kpad, s);
         if (e == cudaSuccess)
             e = cudaStreamSynchronize(s);  // the host table is freed here
     }
@@ -636,6 +650,7 @@ int tc_ctemp_pairs(const TcView &v, const double *Y64, const double *gg_dev, dou
         rp.N = v.N;
         rp.tt = v.tt;
         rp.dcut = dcut;
+        rp.dmin = dmin_dev;
         rp.planes = planes;
         rp.status = v.status;
         rpk<<<dim3(ktiles, (rp.ntile + RP_TILES - 1) / RP_TILES), RP_THREADS, rp_smem, s>>>(tmT, rp);

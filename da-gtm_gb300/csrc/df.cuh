@@ -231,6 +231,25 @@ DF_HD uint64_t fixed48(f2x e)
     return ((uint64_t) top << 24) + (uint64_t) bot;
 }
 
+// round(E 2^48) for 0 <= E < 2 as fixed48, and the rounding remainder
+// E 2^48 - round(E 2^48) in [-1/2, 1/2] to ~2^-24 of itself: a sum of many
+// terms is exact to 2^-48 in the integers plus the FP32 sum of remainders.
+DF_HD uint64_t fixed48r(f2x e, float &rem)
+{
+    const float z = mul_rn(e.h, 16777216.0f);  // exact
+    const float zf = floorf(z);
+    const float lz = mul_rn(e.l, 16777216.0f);
+    const bool dec = (zf == z) && (lz < 0.f);
+    const uint32_t top = (uint32_t) zf - (dec ? 1u : 0u);
+    // the fraction above the top, exactly: fs + fe
+    float fs, fe;
+    two_sum(dec ? 1.0f : sub_rn(z, zf), lz, fs, fe);
+    const float scaled = mul_rn(fs, 16777216.0f);  // exact
+    const float bf = rintf(scaled);
+    rem = fmaf(fe, 16777216.0f, sub_rn(scaled, bf));
+    return ((uint64_t) top << 24) + (uint64_t) (uint32_t) bf;
+}
+
 // round(v 2^63) for an FP32 |v| < 2, from its bits (exact for |v| >= 2^-40;
 // below 2^-126 it is 0)
 DF_HD int64_t scaled63(float v)

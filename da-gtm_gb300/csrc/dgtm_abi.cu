@@ -834,48 +834,93 @@ int dgtm_next_ctemp_k(dgtm_ctx *ctx, double temp, double beta, double eps, const
     cudaError_t e = cudaSuccess;
     if (rc == DGTM_OK && gg)
         e = cudaMemcpyAsync(dgg, gg, sizeof(double) * K, cudaMemcpyHostToDevice, ctx->stream);
+    // centres redone by the CUDA-core scatter (below), and their results
+    std::vector<int> redo;
+    std::vector<double> out_sel, gsum_sel;
+    const double dcut = ref_dcut(ctx->beta);
     if (pairs && rc == DGTM_OK && e == cudaSuccess) {
         TcView v;
         tc_view(ctx->tc, &v);
         const size_t gbudget = (size_t) env_int("DGTM_CTEMP_GEMM_MB", 8192, 64, 1 << 22) << 20;
-        rc = tc_ctemp_pairs(v, ctx->Y64, gg ? dgg : nullptr, lim_scale, gbudget, ref_dcut(ctx->beta),
-                            dgsum, dout, ctx->stream);
+        float *ddmin = nullptr;
+        std::vector<float> dmin(K);
+        rc = dev_alloc(&ddmin, (size_t) v.Kpad);
+        if (rc == DGTM_OK)
+            rc = tc_ctemp_pairs(v, ctx->Y64, gg ? dgg : nullptr, lim_scale, gbudget, dcut, dgsum, dout,
+                                ddmin, ctx->stream);
         if (rc == DGTM_OK)
             rc = tc_fetch_status(ctx->tc, ctx->stream);
         if (rc == DGTM_OK)
             e = cudaMemcpyAsync(gsum.data(), dgsum, sizeof(double) * K, cudaMemcpyDeviceToHost,
                                 ctx->stream);
+        if (rc == DGTM_OK && e == cudaSuccess)
+            e = cudaMemcpyAsync(dmin.data(), ddmin, sizeof(float) * K, cudaMemcpyDeviceToHost,
+                                ctx->stream);
         if (rc == DGTM_OK && e == cudaSuccess && (e = cudaStreamSynchronize(ctx->stream)) == cudaSuccess)
             rc = tc_check_status(ctx->tc);
-        // A centre far from every point has all its responsibilities below the
-        // FP32 planes' 2^-126, so its scatter there is zero (row sum 0: the
-        // reference's HUGE_VAL) while the FP64 reference still forms it.  Such
-        // centres (row sum below 1e-25: any flushed tail is then 1e-13 of the
-        // rest) are redone by the CUDA-core scatter, whose R is FP64.
-        std::vector<int> redo;
+        cudaFree(ddmin);
+        // A centre far from every point can have all its responsibilities below
+        // the FP32 planes' 2^-126: its scatter there is zero (row sum 0) while
+        // the FP64 reference still forms it.  Such centres (row sum below 1e-25:
+        // a flushed tail is then 1e-13 of the rest) are redone by the CUDA-core
+        // scatter, whose R is FP64, unless every point is beyond the reference's
+        // own cut (then its row sum is 0 there too: HUGE_VAL).  FP32 distances
+        // carry ~1e-5: centres within 1e-3 of the cut are redone.
         for (int k = 0; rc == DGTM_OK && e == cudaSuccess && k < K; k++)
-            if (!(gsum[k] >= 1e-25))
+            if (!(gsum[k] >= 1e-25) && (double) dmin[k] <= dcut * (1.0 + 1e-3))
                 redo.push_back(k);
-        if (!redo.empty())
-            rc = dev_alloc(&scratch, (pl.scratch_bytes + sizeof(double) - 1) / sizeof(double));
-        for (size_t i = 0; rc == DGTM_OK && i < redo.size();) {
-            const int k0 = redo[i];
-            int nb = 1;
-            while (i + nb < redo.size() && redo[i + nb] == k0 + nb && nb < kb)
-                nb++;
-            rc = launch_ctemp_batch(pl, ctx->T64, ctx->T32, ctx->Y64, ctx->tt, ctx->yy,
-                                    ctx->colstat, N, D, K, c, k0, nb, gg ? dgg + k0 : nullptr,
-                                    lim_scale, scratch, dgsum + k0, dout + (size_t) 2 * k0,
-                                    ref_dcut(ctx->beta), ctx->stream);
-            i += nb;
+    }
+    if (!redo.empty()) {
+        // the redone centres packed into one batch (one pass over the points)
+        const int ns = (int) redo.size();
+        int *didx = nullptr;
+        double *Ys = nullptr, *yys = nullptr, *ggs = nullptr, *gs = nullptr, *os = nullptr;
+        rc = dev_alloc(&scratch, (pl.scratch_bytes + sizeof(double) - 1) / sizeof(double));
+        if (rc == DGTM_OK)
+            rc = dev_alloc(&didx, (size_t) ns);
+        if (rc == DGTM_OK)
+            rc = dev_alloc(&Ys, (size_t) ns * D);
+        if (rc == DGTM_OK)
+            rc = dev_alloc(&yys, (size_t) ns);
+        if (rc == DGTM_OK && gg)
+            rc = dev_alloc(&ggs, (size_t) ns);
+        if (rc == DGTM_OK)
+            rc = dev_alloc(&gs, (size_t) ns);
+        if (rc == DGTM_OK)
+            rc = dev_alloc(&os, (size_t) 2 * ns);
+        if (rc == DGTM_OK)
+            e = cudaMemcpyAsync(didx, redo.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, ctx->stream);
+        if (rc == DGTM_OK && e == cudaSuccess)
+            rc = launch_gather_centres(ctx->Y64, ctx->yy, gg ? dgg : nullptr, didx, ns, D, Ys, yys,
+                                       ggs, ctx->stream);
+        for (int k0 = 0; rc == DGTM_OK && e == cudaSuccess && k0 < ns; k0 += kb) {
+            const int nb = (ns - k0 < kb) ? ns - k0 : kb;
+            rc = launch_ctemp_batch(pl, ctx->T64, ctx->T32, Ys, ctx->tt, yys, ctx->colstat, N, D, K,
+                                    c, k0, nb, ggs ? ggs + k0 : nullptr, lim_scale, scratch, gs + k0,
+                                    os + (size_t) 2 * k0, dcut, ctx->stream);
         }
+        out_sel.resize((size_t) 2 * ns);
+        gsum_sel.resize((size_t) ns);
+        if (rc == DGTM_OK && e == cudaSuccess)
+            e = cudaMemcpyAsync(out_sel.data(), os, sizeof(double) * 2 * ns, cudaMemcpyDeviceToHost,
+                                ctx->stream);
+        if (rc == DGTM_OK && e == cudaSuccess)
+            e = cudaMemcpyAsync(gsum_sel.data(), gs, sizeof(double) * ns, cudaMemcpyDeviceToHost,
+                                ctx->stream);
+        if (rc == DGTM_OK && e == cudaSuccess)
+            e = cudaStreamSynchronize(ctx->stream);
+        cudaFree(didx);
+        cudaFree(Ys);
+        cudaFree(yys);
+        cudaFree(ggs);
+        cudaFree(gs);
+        cudaFree(os);
     }
     for (int k0 = 0; !pairs && rc == DGTM_OK && e == cudaSuccess && k0 < K; k0 += kb) {
         const int nb = (K - k0 < kb) ? K - k0 : kb;
         rc = launch_ctemp_batch(pl, ctx->T64, ctx->T32, ctx->Y64, ctx->tt, ctx->yy, ctx->colstat,
                                 N, D, K, c, k0, nb, gg ? dgg + k0 : nullptr, lim_scale, scratch,
-                                dgsum + k0, dout + (size_t) 2 * k0, ref_dcut(ctx->beta),
-                                ctx->stream);
+                                dgsum + k0, dout + (size_t) 2 * k0, dcut, ctx->stream);
     }
     if (rc == DGTM_OK && e == cudaSuccess)
         e = cudaMemcpyAsync(out.data(), dout, sizeof(double) * 2 * K, cudaMemcpyDeviceToHost,
@@ -894,6 +939,12 @@ int dgtm_next_ctemp_k(dgtm_ctx *ctx, double temp, double beta, double eps, const
     if (e != cudaSuccess) {
         set_error(DGTM_ECUDA, "dgtm_next_ctemp: %s", cudaGetErrorString(e));
         return DGTM_ECUDA;
+    }
+    for (size_t i = 0; i < redo.size(); i++) {
+        const size_t k = (size_t) redo[i];
+        out[2 * k] = out_sel[2 * i];
+        out[2 * k + 1] = out_sel[2 * i + 1];
+        gsum[k] = gsum_sel[i];
     }
     // comm/mpicomm.c:582-585, 625-627, 664-669
     double cmax = -HUGE_VAL;

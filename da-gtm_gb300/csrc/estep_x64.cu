@@ -27,9 +27,9 @@
 // the data tiles live in tensor memory as the MMA A operand; Y's digit
 // slices stream through a TMA ring in 32-centre chunks; each point's thread
 // keeps a reference centre (the running maximum of acc) and the sums
-// s_n = sum_k exp(-c (d_kn - d_ref)) at temperature 1 and at `temp` in 2^-63
-// fixed point (128 bits: exact, order-independent), rescaled when the
-// reference moves.  Output: the column statistics (d_ref, log s_n) in FP64,
+// s_n = sum_k exp(-c (d_kn - d_ref)) at temperature 1 and at `temp` as 2^-48
+// integers (uint64: exact, order-independent) plus the FP32 sum of each
+// term's exact rounding remainder, rescaled when the reference moves.  Output: the column statistics (d_ref, log s_n) in FP64,
 // the reference's slice partials, and the per-CTA quality terms.
 //
 // Pass 2 (persistent; units of 16 centres x up to 16384 points): per
@@ -73,7 +73,7 @@ constexpr int PANEL = 64;          // BF16 per 128-byte swizzle row
 constexpr int SMEM_LIMIT = 227 * 1024;
 constexpr int NPAD_ALIGN = 256;
 constexpr int KPAD_ALIGN = 128;
-constexpr int X_MAXK = 60000;      // R T unit sums and per-point 2^-63 sums stay in 64 / 128 bits
+constexpr int X_MAXK = 60000;      // per-point sums of K terms below 2^48 (1 + 2^-7) stay in 64 bits
 
 // pass 1
 constexpr int X1_THREADS = 320;    // warp 0 TMA, warp 1 MMA, warps 2-9 statistics
@@ -215,15 +215,25 @@ struct X1Params {
     int *status;
 };
 
-// (hi, lo) *= E for a 128-bit sum at 2^-63 and a double-float factor E <= 1
-// (rare: when a point's reference centre moves; FP64, 2^-53)
-__device__ __forceinline__ void x_rescale(uint64_t &hi, uint64_t &lo, df::f2x e)
-{
-    const double v = df::acc128_value(hi, lo) * df::to_double(e);
-    const double h = floor(0.5 * v);
-    hi = (uint64_t) h;
-    lo = (uint64_t) ldexp(v - 2.0 * h, 63);
-}
+// A per-point sum: 2^-48 integers plus the FP32 sum of the terms' exact
+// rounding remainders (df::fixed48r), so every term counts to ~2^-72.
+struct XSum {
+    unsigned long long i = 0ull;
+    float r = 0.f;
+    __device__ __forceinline__ void add(df::f2x e)
+    {
+        float rem;
+        i += df::fixed48r(e, rem);
+        r += rem;
+    }
+    __device__ __forceinline__ double value() const { return ldexp((double) i + (double) r, -48); }
+    // s *= E <= 1 (rare: when a point's reference centre moves; FP64, 2^-53)
+    __device__ __forceinline__ void scale(df::f2x e)
+    {
+        i = (unsigned long long) llrint(((double) i + (double) r) * df::to_double(e));
+        r = 0.f;
+    }
+};
 
 template <int NP>
 __global__ void __launch_bounds__(X1_THREADS, 1)
@@ -396,9 +406,8 @@ __global__ void __launch_bounds__(X1_THREADS, 1)
         // the reference centre's slice partials (and the first three scaled)
         float r0 = 0.f, r1 = 0.f, r2 = 0.f, r3 = 0.f, R0 = 0.f, R1 = 0.f, R2 = 0.f;
         bool have = false;
-        // s_n at temperature 1 and at `temp`: 128-bit sums at 2^-63 (each term
-        // rounded by at most 2^-64, the order of addition immaterial)
-        uint64_t s1h = 0, s1l = 0, s2h = 0, s2l = 0;
+        // s_n at temperature 1 and at `temp`
+        XSum s1, s2;
         bool ok = true;
         for (int c = 0; c < p.nchunk; c++) {
             if (!mbar_wait(&acc_full[g], (uint32_t) (c & 1), p.status, 46)) {
@@ -439,9 +448,9 @@ __global__ void __launch_bounds__(X1_THREADS, 1)
                     if (dI.h > 0.f) {
                         // the sums move to the new reference: s *= exp(-2c dI 2^-F)
                         const df::f2x nd = {-dI.h, -dI.l};
-                        x_rescale(s1h, s1l, df::exp_df(df::mul(nd, k1), tab));
+                        s1.scale(df::exp_df(df::mul(nd, k1), tab));
                         if (p.two_temps)
-                            x_rescale(s2h, s2l, df::exp_df(df::mul(nd, k2), tab));
+                            s2.scale(df::exp_df(df::mul(nd, k2), tab));
                         take = true;
                     }
                 }
@@ -462,9 +471,9 @@ __global__ void __launch_bounds__(X1_THREADS, 1)
                     // exact slice differences (each below 2^24), then 48 bits of their sum
                     const df::f2x dI = df::sum4(fmaf(fu(v[j]), 0x1p40f, -R0), fmaf(fu(v[32 + j]), 0x1p24f, -R1),
                                                 fmaf(fu(v[64 + j]), 256.f, -R2), fu(v[96 + j]) - r3);
-                    df::acc128(s1h, s1l, df::fixed63(df::exp_df(df::mul(dI, k1), tab)));
+                    s1.add(df::exp_df(df::mul(dI, k1), tab));
                     if (p.two_temps)
-                        df::acc128(s2h, s2l, df::fixed63(df::exp_df(df::mul(dI, k2), tab)));
+                        s2.add(df::exp_df(df::mul(dI, k2), tab));
                 }
             }
         }
@@ -472,8 +481,8 @@ __global__ void __launch_bounds__(X1_THREADS, 1)
         if (ok && n < p.N) {
             const double Iref = (double) r0 * 0x1p40 + (double) r1 * 0x1p24 + (double) r2 * 256.0 + (double) r3;
             const double dstar = p.tt[n] - 2.0 * Iref * inv;
-            const double ls1 = log(df::acc128_value(s1h, s1l));
-            const double ls2 = p.two_temps ? log(df::acc128_value(s2h, s2l)) : ls1;
+            const double ls1 = log(s1.value());
+            const double ls2 = p.two_temps ? log(s2.value()) : ls1;
             const double lsel = p.isDA ? ls2 : ls1;
             t1 = -p.c1 * dstar + ls1;
             t2 = p.isDA ? (-p.c2 * dstar + ls2) : 0.0;

@@ -110,6 +110,9 @@ int launch_ctemp_batch(const CtempPlan &pl, const double *T64, const float *T32,
                        int K, double c, int k0, int kb, const double *gg_dev, double lim_scale,
                        void *scratch, double *gsum_dev, double *out_dev, double dcut,
                        cudaStream_t s);
+// Rows idx[0..n) of Y (K x D), and of yy and gg (gg may be null), packed.
+int launch_gather_centres(const double *Y, const double *yy, const double *gg, const int *idx,
+                          int n, int D, double *Ys, double *yys, double *ggs, cudaStream_t s);
 // yy = |y|^2 for a given Y.
 int launch_norms(const double *X, int rows, int D, double *out, cudaStream_t s);
 // out[r] = |x_r|^2 in FP64 for an FP32 row-major matrix (rows x D).

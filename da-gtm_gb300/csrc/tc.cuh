@@ -74,8 +74,10 @@ void tc_view(const TcState *st, TcView *v);
 // upper triangles, written per batch of centres as the CUDA-core scatter
 // writes them; then the eigen filter of ctemp.cu.  out[2 k + w] as in
 // launch_ctemp_batch; gsum[k] = row sums of R.
-// R_kn = 0 where d_kn > dcut (the reference's exp(-beta d / 2) underflows).
+// R_kn = 0 where d_kn > dcut (the reference's exp(-beta d / 2) underflows);
+// dmin (Kpad floats): each centre's least distance to a point (FP32).
 int tc_ctemp_pairs(const TcView &v, const double *Y64, const double *gg_dev, double lim_scale,
-                   size_t budget, double dcut, double *gsum_dev, double *out_dev, cudaStream_t s);
+                   size_t budget, double dcut, double *gsum_dev, double *out_dev, float *dmin,
+                   cudaStream_t s);
 
 }  // namespace dgtm

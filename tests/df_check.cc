@@ -149,6 +149,28 @@ int main()
         ssum += ld(e);
     }
     printf("fixed63 max_abs_units %.3Lf\n", gmax);
+
+    // fixed48r: the integers plus the FP32 sum of remainders against the
+    // long-double sum of 60000 terms below 1 (the largest K), several times
+    long double rmax = 0.0L;
+    for (int rep = 0; rep < 20; rep++) {
+        uint64_t si = 0;
+        float sr = 0.f;
+        long double ls = 0.0L;
+        for (int i = 0; i < 60000; i++) {
+            const double ed = (i % 2) ? uniform() : ldexp(uniform(), -(int) (next_u64() % 45));
+            const f2x e = from_double(ed);
+            float r;
+            si += fixed48r(e, r);
+            sr += r;
+            ls += ld(e);
+        }
+        const long double got = ldexpl((long double) si + (long double) sr, -48);
+        const long double relr = fabsl(got - ls) / ls;
+        if (relr > rmax)
+            rmax = relr;
+    }
+    printf("fixed48r sum_rel %.3Le\n", rmax);
     printf("acc128 sum_rel %.3Le\n", fabsl((long double) acc128_value(hi, lo) - ssum) / ssum);
     return 0;
 }
