@@ -62,8 +62,8 @@ struct RPParams {
     int Kpad, Dp, n0, ntile, nc, nstage, N;  // chunk: points n0 .. n0 + nc, nc = 64 ntile
     const uint32_t *Yb;                      // 2 x Kpad x Dp BF16 (as pairs)
     const float4 *colq;
-    const double *tt;                        // N: |t_n|^2
-    double dcut;                             // R = 0 where d > dcut
+    const float *hcut;                       // N: (|t_n|^2 - dcut) / 2; R = 0 where acc below it
+    float dcut;
     float *dmin;                             // Kpad: each centre's least distance (FP32)
     uint32_t *planes;                     // 4 x Kpad x nc BF16 (as pairs): R hi, R lo, R^2 hi, R^2 lo
     int *status;
@@ -198,7 +198,7 @@ __global__ void __launch_bounds__(RP_THREADS, 1)
         }
         const size_t plane = (size_t) p.Kpad * p.nc / 2;  // uint32 per plane
         uint32_t *out = p.planes + ((size_t) k * p.nc) / 2;
-        float dm = INFINITY;  // this row's least distance over its points
+        float mx = -INFINITY;  // this row's largest acc - hcut over its points
         bool ok = true;
         for (int j = 0; j < ntl; j++) {
             const int b = j & 1;
@@ -214,11 +214,14 @@ __global__ void __launch_bounds__(RP_THREADS, 1)
             mbar_arrive(&s_free[b]);
             const int nl = (j0 + j) * RP_TILE + g * 32;  // point within the chunk
             const float4 *cq = p.colq + p.n0 + nl;
-#pragma unroll 8
+            // acc_kn below hcut_n: d_kn > dcut, where the reference's
+            // exp(-beta d / 2) underflows (padding points: +inf, R = 0 anyway)
+            float hc[32];
+#pragma unroll
             for (int e = 0; e < 32; e++) {
                 const int na = p.n0 + nl + e;
-                if (na < p.N)
-                    dm = fminf(dm, (float) p.tt[na] - 2.0f * __uint_as_float(va[e]));
+                hc[e] = (na < p.N) ? p.hcut[na] : INFINITY;
+                mx = fmaxf(mx, __uint_as_float(va[e]) - hc[e]);
             }
 #pragma unroll
             for (int pl = 0; pl < 4; pl++) {
@@ -230,12 +233,9 @@ __global__ void __launch_bounds__(RP_THREADS, 1)
                     const float4 c0 = cq[2 * e], c1 = cq[2 * e + 1];
                     float r0 = ex2(fmaf(__uint_as_float(va[2 * e]) - c0.x, c0.y, -c0.z));
                     float r1 = ex2(fmaf(__uint_as_float(va[2 * e + 1]) - c1.x, c1.y, -c1.z));
-                    // R = 0 where d = |t|^2 - 2 acc > dcut, as the reference's
-                    // exp(-beta d / 2) underflows there
-                    const int na = p.n0 + nl + 2 * e;
-                    if (na < p.N && __uint_as_float(va[2 * e]) < (float) (0.5 * (p.tt[na] - p.dcut)))
+                    if (__uint_as_float(va[2 * e]) < hc[2 * e])
                         r0 = 0.f;
-                    if (na + 1 < p.N && __uint_as_float(va[2 * e + 1]) < (float) (0.5 * (p.tt[na + 1] - p.dcut)))
+                    if (__uint_as_float(va[2 * e + 1]) < hc[2 * e + 1])
                         r1 = 0.f;
                     if (pl >= 2) {
                         r0 *= r0;
@@ -250,9 +250,10 @@ __global__ void __launch_bounds__(RP_THREADS, 1)
                     dst[i] = make_uint4(w[4 * i], w[4 * i + 1], w[4 * i + 2], w[4 * i + 3]);
             }
         }
-        // non-negative floats order like their bit patterns
-        if (dm < INFINITY)
-            atomicMin((int *) &p.dmin[k], __float_as_int(fmaxf(dm, 0.f)));
+        // d_min = dcut - 2 max(acc - hcut); non-negative floats order like
+        // their bit patterns
+        if (mx > -INFINITY)
+            atomicMin((int *) &p.dmin[k], __float_as_int(fmaxf(p.dcut - 2.0f * mx, 0.f)));
         if (!ok)
             failed = 1;
     }
@@ -279,6 +280,14 @@ RPKernel rplanes_for(int np, int kl)
     DGTM_RP(3, 1) DGTM_RP(3, 2) DGTM_RP(3, 3) DGTM_RP(3, 4)
 #undef DGTM_RP
     return nullptr;
+}
+
+// (|t_n|^2 - dcut) / 2 in FP32: acc_kn below it means d_kn > dcut
+__global__ void hcut_kernel(const double *__restrict__ tt, int N, double dcut, float *__restrict__ h)
+{
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n < N)
+        h[n] = (float) (0.5 * (tt[n] - dcut));
 }
 
 // ---------------------------------------------------------------------------
@@ -566,6 +575,7 @@ int tc_ctemp_pairs(const TcView &v, const double *Y64, const double *gg_dev, dou
     uint32_t *planes = nullptr;
     __nv_bfloat16 *U = nullptr;
     ushort2 *pairs = nullptr;
+    float *hcut = nullptr;
     void *sbuf = nullptr;
     int rc = DGTM_OK;
     cudaError_t e = cudaMalloc((void **) &Q, qbytes);
@@ -577,12 +587,15 @@ int tc_ctemp_pairs(const TcView &v, const double *Y64, const double *gg_dev, dou
         e = cudaMalloc((void **) &pairs, sizeof(ushort2) * (size_t) npair);
     if (e == cudaSuccess)
         e = cudaMalloc(&sbuf, s_at + mg_bytes + 256);
+    if (e == cudaSuccess)
+        e = cudaMalloc((void **) &hcut, sizeof(float) * (size_t) N);
     auto cleanup = [&]() {
         cudaFree(Q);
         cudaFree(planes);
         cudaFree(U);
         cudaFree(pairs);
         cudaFree(sbuf);
+        cudaFree(hcut);
     };
     if (e != cudaSuccess) {
         cleanup();
@@ -600,6 +613,10 @@ int tc_ctemp_pairs(const TcView &v, const double *Y64, const double *gg_dev, dou
             e = cudaMemsetAsync(Q, 0, qbytes, s);
         if (e == cudaSuccess)  // 0x7F7F7F7F: 3.4e38, above every distance
             e = cudaMemsetAsync(dmin_dev, 0x7F, sizeof(float) * (size_t) Kpad, s);
+        if (e == cudaSuccess) {
+            hcut_kernel<<<(N + 255) / 256, 256, 0, s>>>(v.tt, N, dcut, hcut);
+            e = cudaGetLastError();
+        }
         if (e == cudaSuccess)
             e = cudaStreamSynchronize(s);  // the host table is freed here
     }
@@ -648,8 +665,8 @@ int tc_ctemp_pairs(const TcView &v, const double *Y64, const double *gg_dev, dou
         rp.Yb = (const uint32_t *) v.Yb;
         rp.colq = v.colq;
         rp.N = v.N;
-        rp.tt = v.tt;
-        rp.dcut = dcut;
+        rp.hcut = hcut;
+        rp.dcut = (float) dcut;
         rp.dmin = dmin_dev;
         rp.planes = planes;
         rp.status = v.status;
