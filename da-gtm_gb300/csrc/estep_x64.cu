@@ -33,16 +33,16 @@
 // the reference's slice partials, and the per-CTA quality terms.
 //
 // Pass 2 (persistent; units of 16 centres x up to 16384 points): per
-// 128-point tile, MMA 1 (M = 128 points, N = 16 centres) gives the slice
-// partials; eight warps form R_kn = exp(-c (d_kn - d_ref) - log s_n) in
-// 2^-48 fixed point and write its six base-256 digits (again paired by 256)
-// to shared memory; MMA 2 (M = 128 data dimensions, A = the same T tile read
-// MN-major, B = the R digits, K = 128 points) accumulates R T and, through
-// the ones in the padding columns, G.  Sums of 256 points of 16-bit digit
-// pairs stay below 2^24: exact.  Every 256 points the accumulators are
-// moved to per-thread uint64 sums; at the unit's end these go to global
-// uint64 accumulators (high and low 24-bit parts: exact, order-independent).
-// A last kernel forms G and R T in FP64.
+// 128-point tile, MMA 1 (M = 128 points, N = 112: the seven slices of the
+// 16 centres side by side) gives the slice partials; eight warps form
+// R_kn = exp(-c (d_kn - d_ref) - log s_n) in 2^-48 fixed point and write its
+// six base-256 digits side by side (96 rows) to shared memory; MMA 2 (M = 128
+// data dimensions, A = the same T tile read MN-major, N = 96, K = 128
+// points) accumulates R T and, through the ones in the padding columns, G,
+// one accumulator per digit.  A digit sum over a whole unit stays below
+// 2^22: exact.  At the unit's end the six sums of each (dimension, centre)
+// go to global uint64 accumulators (high and low 24-bit parts: exact,
+// order-independent).  A last kernel forms G and R T in FP64.
 //
 // The oracle's FP64 sums round in their own order; this form's results are
 // the exact values for the rounded centres to ~2^-47 relative, which is the
@@ -86,13 +86,14 @@ constexpr int X1_TPANEL = X1_TILE * 128;
 // pass 2
 constexpr int X2_THREADS = 320;    // warp 0 TMA, warp 1 MMA, warps 2-9 responsibilities
 constexpr int X2_TILE = 128;       // points per tile (MMA 1 M, MMA 2 K)
-constexpr int X2_NC = 16;          // centres per unit (MMA N)
-constexpr int X2_UNIT_TILES = 128; // 16384 points: unit sums below 2^14 x 2^48
-constexpr int X2_SEG = 2;          // tiles per exact R T segment (256 points)
+constexpr int X2_NC = 16;          // centres per unit
+constexpr int X2_UNIT_TILES = 128; // 16384 points: digit sums below 2^22, unit sums below 2^62
+constexpr int X2_N1 = XS * X2_NC;  // MMA 1 N: the seven slices side by side (112)
+constexpr int X2_N2 = 6 * X2_NC;   // MMA 2 N: the six digits of R side by side (96)
 constexpr int X2_TPANEL = X2_TILE * 128;  // 16 KB
-constexpr int X2_YPANEL = X2_NC * 128;    // 2 KB
-constexpr int X2_RSLICE = 2 * X2_YPANEL;  // one R digit slice: 16 centres x 128 points
-constexpr int X2_RBUF = 6 * X2_RSLICE;    // 24 KB
+constexpr int X2_YPANEL = X2_N1 * 128;    // 14 KB: 112 rows (slice, centre) x 64 depths
+constexpr int X2_RPANEL = X2_N2 * 128;    // 12 KB: 96 rows (digit, centre) x 64 points
+constexpr int X2_RBUF = 2 * X2_RPANEL;    // one tile's R digits
 constexpr int X2_CONST = X2_TILE * 32;    // per-point constants of a tile: refq, lsq
 
 __host__ __device__ constexpr int rup(int a, int b) { return (a + b - 1) / b * b; }
@@ -415,65 +416,72 @@ __global__ void __launch_bounds__(X1_THREADS, 1)
                 break;
             }
             tc_fence_after();
-            uint32_t v[4 * X1_NC];
-            {
-                const uint32_t col = lane_base + (uint32_t) (X1_ACC + g * 4 * X1_NC);
-                tmem_ld32p(col, v);
-                tmem_ld32p(col + 32, v + 32);
-                tmem_ld32p(col + 64, v + 64);
-                tmem_ld32p(col + 96, v + 96);
-                tmem_ld_wait();
-            }
-            tc_fence_before();
-            mbar_arrive(&acc_empty[g]);
             const int nvalid = min(X1_NC, p.K - c * X1_NC);  // padding centres are skipped
-            // the chunk's largest acc, approximately (FP32 of the top two partials)
-            float best = -INFINITY, b0 = 0.f, b1 = 0.f, b2 = 0.f, b3 = 0.f;
+            const uint32_t col = lane_base + (uint32_t) (X1_ACC + g * 4 * X1_NC);
+            // Eight centres at a time (4 x 8 partials in registers), so that
+            // several exponential chains fit beside them; the accumulator is
+            // released after the last batch is read (the tensor pipe is idle
+            // far longer than the next chunk's MMAs take).
 #pragma unroll
-            for (int j = 0; j < X1_NC; j++) {
-                const float a = fmaf(fu(v[j]), 0x1p40f, fu(v[32 + j]) * 0x1p24f);
-                if (j < nvalid && a > best) {
-                    best = a;
-                    b0 = fu(v[j]);
-                    b1 = fu(v[32 + j]);
-                    b2 = fu(v[64 + j]);
-                    b3 = fu(v[96 + j]);
+            for (int bt = 0; bt < X1_NC / 8; bt++) {
+                uint32_t v[32];
+                tmem_ld8p(col + (uint32_t) (8 * bt), v);
+                tmem_ld8p(col + (uint32_t) (X1_NC + 8 * bt), v + 8);
+                tmem_ld8p(col + (uint32_t) (2 * X1_NC + 8 * bt), v + 16);
+                tmem_ld8p(col + (uint32_t) (3 * X1_NC + 8 * bt), v + 24);
+                tmem_ld_wait();
+                if (bt == X1_NC / 8 - 1) {
+                    tc_fence_before();
+                    mbar_arrive(&acc_empty[g]);
                 }
-            }
-            if (nvalid > 0) {
-                bool take = !have;
-                if (have) {
-                    const df::f2x dI = df::sum4(fmaf(b0, 0x1p40f, -R0), fmaf(b1, 0x1p24f, -R1),
-                                                fmaf(b2, 256.f, -R2), b3 - r3);
-                    if (dI.h > 0.f) {
-                        // the sums move to the new reference: s *= exp(-2c dI 2^-F)
-                        const df::f2x nd = {-dI.h, -dI.l};
-                        s1.scale(df::exp_df(df::mul(nd, k1), tab));
-                        if (p.two_temps)
-                            s2.scale(df::exp_df(df::mul(nd, k2), tab));
-                        take = true;
+                // the batch's largest acc, approximately (FP32 of the top two partials)
+                float best = -INFINITY, b0 = 0.f, b1 = 0.f, b2 = 0.f, b3 = 0.f;
+#pragma unroll
+                for (int j = 0; j < 8; j++) {
+                    const float a = fmaf(fu(v[j]), 0x1p40f, fu(v[8 + j]) * 0x1p24f);
+                    if (8 * bt + j < nvalid && a > best) {
+                        best = a;
+                        b0 = fu(v[j]);
+                        b1 = fu(v[8 + j]);
+                        b2 = fu(v[16 + j]);
+                        b3 = fu(v[24 + j]);
                     }
                 }
-                if (take) {
-                    r0 = b0;
-                    r1 = b1;
-                    r2 = b2;
-                    r3 = b3;
-                    R0 = b0 * 0x1p40f;
-                    R1 = b1 * 0x1p24f;
-                    R2 = b2 * 256.f;
-                    have = true;
+                if (best > -INFINITY) {
+                    bool take = !have;
+                    if (have) {
+                        const df::f2x dI = df::sum4(fmaf(b0, 0x1p40f, -R0), fmaf(b1, 0x1p24f, -R1),
+                                                    fmaf(b2, 256.f, -R2), b3 - r3);
+                        if (dI.h > 0.f) {
+                            // the sums move to the new reference: s *= exp(-2c dI 2^-F)
+                            const df::f2x nd = {-dI.h, -dI.l};
+                            s1.scale(df::exp_df(df::mul(nd, k1), tab));
+                            if (p.two_temps)
+                                s2.scale(df::exp_df(df::mul(nd, k2), tab));
+                            take = true;
+                        }
+                    }
+                    if (take) {
+                        r0 = b0;
+                        r1 = b1;
+                        r2 = b2;
+                        r3 = b3;
+                        R0 = b0 * 0x1p40f;
+                        R1 = b1 * 0x1p24f;
+                        R2 = b2 * 256.f;
+                        have = true;
+                    }
                 }
-            }
 #pragma unroll
-            for (int j = 0; j < X1_NC; j++) {
-                if (j < nvalid) {
-                    // exact slice differences (each below 2^24), then 48 bits of their sum
-                    const df::f2x dI = df::sum4(fmaf(fu(v[j]), 0x1p40f, -R0), fmaf(fu(v[32 + j]), 0x1p24f, -R1),
-                                                fmaf(fu(v[64 + j]), 256.f, -R2), fu(v[96 + j]) - r3);
-                    s1.add(df::exp_df(df::mul(dI, k1), tab));
-                    if (p.two_temps)
-                        s2.add(df::exp_df(df::mul(dI, k2), tab));
+                for (int j = 0; j < 8; j++) {
+                    if (8 * bt + j < nvalid) {
+                        // exact slice differences (each below 2^24), then 48 bits of their sum
+                        const df::f2x dI = df::sum4(fmaf(fu(v[j]), 0x1p40f, -R0), fmaf(fu(v[8 + j]), 0x1p24f, -R1),
+                                                    fmaf(fu(v[16 + j]), 256.f, -R2), fu(v[24 + j]) - r3);
+                        s1.add(df::exp_df(df::mul(dI, k1), tab));
+                        if (p.two_temps)
+                            s2.add(df::exp_df(df::mul(dI, k2), tab));
+                    }
                 }
             }
         }
@@ -575,12 +583,6 @@ __device__ __forceinline__ uint32_t bf16_small(uint32_t v)
     return __float_as_uint(__uint_as_float(0x4B000000u | v) - 8388608.0f) >> 16;
 }
 
-// ... and of 256 v
-__device__ __forceinline__ uint32_t bf16_small256(uint32_t v)
-{
-    return __float_as_uint((__uint_as_float(0x4B000000u | v) - 8388608.0f) * 256.0f) >> 16;
-}
-
 template <int NP>
 __global__ void __launch_bounds__(X2_THREADS, 1)
     x_pass2_kernel(const __grid_constant__ CUtensorMap tmY, const __grid_constant__ CUtensorMap tmT,
@@ -589,13 +591,14 @@ __global__ void __launch_bounds__(X2_THREADS, 1)
     constexpr int DP = NP * PANEL;
     constexpr int KS = 4 * NP;
     constexpr int TSTAGE = NP * X2_TPANEL + X2_CONST;
-    constexpr int YBYTES = XS * NP * X2_YPANEL;
+    constexpr int YBYTES = NP * X2_YPANEL;
     constexpr int NBLK = (DP > 128) ? 2 : 1;       // 128-dimension blocks of R T
     constexpr int MB1 = (DP > 128) ? DP - 128 : 0; // first dimension of block 1
-    constexpr int S_COL = 0;                       // 2 buffers x 4 accumulators x 16
-    constexpr int RT_COL = 128;                    // 2 buffers x 3 pairs x NBLK x 16
-    constexpr int RT_BUF = 3 * NBLK * X2_NC;
-    static_assert(RT_COL + 2 * RT_BUF <= 512, "tensor memory plan");
+    constexpr int S_COL = 0;                       // 2 buffers of 112 (slice, centre), 128 apart
+    constexpr int S_STRIDE = 128;
+    constexpr int RT_COL = 256;                    // NBLK blocks x 96 (digit, centre)
+    static_assert(X2_N1 <= S_STRIDE && 2 * S_STRIDE <= RT_COL && RT_COL + NBLK * X2_N2 <= 512,
+                  "tensor memory plan");
     static_assert(MB1 % PANEL == 0, "block 1 starts on a panel");
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char *base = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
@@ -612,12 +615,12 @@ __global__ void __launch_bounds__(X2_THREADS, 1)
     uint64_t *s_empty = bars + 6;     // 2
     uint64_t *r_full = bars + 8;      // 2
     uint64_t *r_empty = bars + 10;    // 2
-    uint64_t *rt_full = bars + 12;    // 2
-    uint64_t *rt_free = bars + 14;    // 2
-    uint64_t *y_full = bars + 16;
-    uint64_t *y_empty = bars + 17;
-    uint64_t *drain = bars + 18;
-    uint32_t *tmem_sh = (uint32_t *) (bars + 19);
+    uint64_t *rt_full = bars + 12;
+    uint64_t *rt_free = bars + 13;
+    uint64_t *y_full = bars + 14;
+    uint64_t *y_empty = bars + 15;
+    uint64_t *drain = bars + 16;
+    uint32_t *tmem_sh = (uint32_t *) (bars + 17);
     float2 *tab = (float2 *) (tmem_sh + 2);
     __shared__ int failed;
 
@@ -637,9 +640,9 @@ __global__ void __launch_bounds__(X2_THREADS, 1)
             mbar_init(&s_empty[b], 256);
             mbar_init(&r_full[b], 256);
             mbar_init(&r_empty[b], 1);
-            mbar_init(&rt_full[b], 1);
-            mbar_init(&rt_free[b], 256);
         }
+        mbar_init(rt_full, 1);
+        mbar_init(rt_free, 256);
         mbar_init(y_full, 1);
         mbar_init(y_empty, 1);
         mbar_init(drain, 1);
@@ -667,12 +670,13 @@ __global__ void __launch_bounds__(X2_THREADS, 1)
                 ok = false;
                 break;
             }
+            // slice sl of the unit's 16 centres into rows 16 sl .. 16 sl + 15 of each panel
             mbar_expect_tx(y_full, (uint32_t) YBYTES);
 #pragma unroll
             for (int sl = 0; sl < XS; sl++)
 #pragma unroll
                 for (int pn = 0; pn < NP; pn++)
-                    tma_load_2d(Ybuf + (sl * NP + pn) * X2_YPANEL, &tmY, y_full, PANEL * pn,
+                    tma_load_2d(Ybuf + pn * X2_YPANEL + sl * X2_NC * 128, &tmY, y_full, PANEL * pn,
                                 sl * p.Kpad + kb * X2_NC);
             for (int t = t0; t < t1; t++, jt++) {
                 if (jt >= 2 && !mbar_wait(&t_empty[s], ph ^ 1u, p.status, 52)) {
@@ -697,13 +701,13 @@ __global__ void __launch_bounds__(X2_THREADS, 1)
             failed = 1;
     } else if (warp == 1) {
         // ---------------- MMA issuer ----------------
-        const uint32_t id1 = idesc_bf16(X2_TILE, X2_NC, 0, 0);  // points x centres, both K-major
-        const uint32_t id2 = idesc_bf16(128, X2_NC, 1, 0);      // dimensions x centres, A MN-major
+        const uint32_t id1 = idesc_bf16(X2_TILE, X2_N1, 0, 0);  // points x (slice, centre)
+        const uint32_t id2 = idesc_bf16(128, X2_N2, 1, 0);      // dimensions x (digit, centre), A MN-major
         const uint64_t tdesc_k = sdesc_sw128(smem_u32(Tst), 16, 1024);
         const uint64_t tdesc_mn = sdesc_sw128(smem_u32(Tst), X2_TPANEL, 1024);
         const uint64_t ydesc = sdesc_sw128(smem_u32(Ybuf), 16, 1024);
         const uint64_t rdesc = sdesc_sw128(smem_u32(Rbuf), 16, 1024);
-        int jt = 0, s = 0, sp = 0, nunit = 0, gseg = 0;
+        int jt = 0, s = 0, sp = 0, nunit = 0;
         uint32_t ph = 0;
         bool ok = true;
         for (int v = blockIdx.x; ok && v < p.nunits; v += gridDim.x, nunit++) {
@@ -716,7 +720,7 @@ __global__ void __launch_bounds__(X2_THREADS, 1)
             tc_fence_after();
             for (int t = t0; t <= t1; t++) {
                 if (t < t1) {
-                    // MMA 1: the slice partials of tile jt (M = 128 points, N = 16 centres)
+                    // MMA 1: the seven slice partials of tile jt (M = 128 points, N = 112)
                     const int b = jt & 1;
                     if (!mbar_wait_w(&t_full[s], ph, p.status, 54) ||
                         (jt >= 2 && !mbar_wait_w(&s_empty[b], (uint32_t) (((jt - 2) >> 1) & 1), p.status, 55))) {
@@ -724,53 +728,43 @@ __global__ void __launch_bounds__(X2_THREADS, 1)
                         break;
                     }
                     tc_fence_after();
-                    const uint32_t d = tmem + (uint32_t) (S_COL + b * 4 * X2_NC);
+                    const uint32_t d = tmem + (uint32_t) (S_COL + b * S_STRIDE);
                     const uint64_t ad = tdesc_k + (uint64_t) ((s * TSTAGE) >> 4);
 #pragma unroll
-                    for (int sl = 0; sl < XS; sl++)
-#pragma unroll
-                        for (int ks = 0; ks < KS; ks++)
-                            mma_ss_w(d + (uint32_t) ((sl >> 1) * X2_NC),
-                                     ad + (uint64_t) ((ks / 4) * (X2_TPANEL >> 4) + 2 * (ks % 4)),
-                                     ydesc + (uint64_t) ((sl * NP + ks / 4) * (X2_YPANEL >> 4) + 2 * (ks % 4)),
-                                     id1, ((sl & 1) || ks) ? 1u : 0u);
+                    for (int ks = 0; ks < KS; ks++)
+                        mma_ss_w(d, ad + (uint64_t) ((ks / 4) * (X2_TPANEL >> 4) + 2 * (ks % 4)),
+                                 ydesc + (uint64_t) ((ks / 4) * (X2_YPANEL >> 4) + 2 * (ks % 4)), id1,
+                                 ks ? 1u : 0u);
                     mma_commit_w(&s_full[b]);
                     if (t == t1 - 1)
                         mma_commit_w(y_empty);  // the unit's centre slices are read
                 }
                 if (t > t0) {
-                    // MMA 2: R T of tile jt - 1 (M = 128 dimensions, N = 16 centres, K = 128 points)
-                    const int j = jt - 1, rb = j & 1, u = t - 1 - t0;
-                    const bool seg_start = (u % X2_SEG) == 0;
-                    const int sb = gseg & 1;
+                    // MMA 2: R T of tile jt - 1 (M = 128 dimensions, N = 96, K = 128 points)
+                    const int j = jt - 1, rb = j & 1;
+                    const bool first = (t - 1 == t0);
                     if (!mbar_wait_w(&r_full[rb], (uint32_t) ((j >> 1) & 1), p.status, 56) ||
-                        (seg_start && gseg >= 2 &&
-                         !mbar_wait_w(&rt_free[sb], (uint32_t) (((gseg - 2) >> 1) & 1), p.status, 57))) {
+                        (first && nunit > 0 &&
+                         !mbar_wait_w(rt_free, (uint32_t) ((nunit - 1) & 1), p.status, 57))) {
                         ok = false;
                         break;
                     }
                     tc_fence_after();
                     const uint64_t ad = tdesc_mn + (uint64_t) ((sp * TSTAGE) >> 4);
                     const uint64_t bd = rdesc + (uint64_t) ((rb * X2_RBUF) >> 4);
-                    const uint32_t d = tmem + (uint32_t) (RT_COL + sb * RT_BUF);
 #pragma unroll
-                    for (int sd = 0; sd < 6; sd++)
+                    for (int mb = 0; mb < NBLK; mb++)
 #pragma unroll
-                        for (int mb = 0; mb < NBLK; mb++)
-#pragma unroll
-                            for (int kk = 0; kk < X2_TILE / 16; kk++)
-                                mma_ss_w(d + (uint32_t) (((sd >> 1) * NBLK + mb) * X2_NC),
-                                         ad + (uint64_t) ((mb ? (MB1 / PANEL) * (X2_TPANEL >> 4) : 0) +
-                                                          kk * (2048 >> 4)),
-                                         bd + (uint64_t) (sd * (X2_RSLICE >> 4) + (kk >> 2) * (X2_YPANEL >> 4) +
-                                                          2 * (kk & 3)),
-                                         id2, (!seg_start || (sd & 1) || kk) ? 1u : 0u);
+                        for (int kk = 0; kk < X2_TILE / 16; kk++)
+                            mma_ss_w(tmem + (uint32_t) (RT_COL + mb * X2_N2),
+                                     ad + (uint64_t) ((mb ? (MB1 / PANEL) * (X2_TPANEL >> 4) : 0) +
+                                                      kk * (2048 >> 4)),
+                                     bd + (uint64_t) ((kk >> 2) * (X2_RPANEL >> 4) + 2 * (kk & 3)), id2,
+                                     (!first || kk) ? 1u : 0u);
                     mma_commit_w(&t_empty[sp]);
                     mma_commit_w(&r_empty[rb]);
-                    if ((u % X2_SEG) == X2_SEG - 1 || t == t1) {
-                        mma_commit_w(&rt_full[sb]);
-                        gseg++;
-                    }
+                    if (t == t1)
+                        mma_commit_w(rt_full);  // the unit's R T is complete
                 }
                 if (t < t1) {
                     sp = s;
@@ -785,50 +779,21 @@ __global__ void __launch_bounds__(X2_THREADS, 1)
         if (!ok)
             failed = 1;
     } else if (warp >= 2) {
-        // ---------------- responsibilities (R digits) and the R T sums ----------------
+        // ---------------- responsibilities (R digits) and the unit's R T ----------------
         const int q = warp & 3, g = (warp - 2) >> 2;
         const uint32_t lane_base = tmem + ((uint32_t) (q * 32) << 16);
         const int pt = q * 32 + lane;  // point within a tile (digits), row of R T (drain)
         const double inv = p.sc->inv;
         const df::f2x kc = df::from_double(2.0 * p.c * inv);
         const unsigned long long rinvK = ((1ull << 48) + (unsigned long long) (p.K / 2)) / (unsigned long long) p.K;
-        // drain ownership: block g, rows 32 q + lane; dimension dim
+        // drain ownership: block g, rows 32 q + lane, dimension dim
         const int mb = g;
         const int dim = (mb == 0 ? 0 : MB1) + pt;
         const bool own = (mb < NBLK) && (mb == 0 ? (q * 32 < DP) : (q * 32 >= 256 - DP));
-        unsigned long long acc[X2_NC];
-#pragma unroll
-        for (int c = 0; c < X2_NC; c++)
-            acc[c] = 0ull;
-        int jt = 0, s = 0, gseg = 0;
+        int jt = 0, s = 0, nunit = 0;
         uint32_t ph = 0;
         bool ok = true;
-        auto drain_seg = [&](int gs) -> bool {
-            const int sb = gs & 1;
-            if (!mbar_wait(&rt_full[sb], (uint32_t) ((gs >> 1) & 1), p.status, 58))
-                return false;
-            tc_fence_after();
-            if (own) {
-                uint32_t w[3 * X2_NC];
-                const uint32_t col = lane_base + (uint32_t) (RT_COL + sb * RT_BUF);
-                tmem_ld16p(col + (uint32_t) ((0 * NBLK + mb) * X2_NC), w);
-                tmem_ld16p(col + (uint32_t) ((1 * NBLK + mb) * X2_NC), w + X2_NC);
-                tmem_ld16p(col + (uint32_t) ((2 * NBLK + mb) * X2_NC), w + 2 * X2_NC);
-                tmem_ld_wait();
-#pragma unroll
-                for (int c = 0; c < X2_NC; c++) {
-                    // exact integers below 2^24
-                    const unsigned long long a01 = (unsigned long long) __float2uint_rz(fu(w[c]));
-                    const unsigned long long a23 = (unsigned long long) __float2uint_rz(fu(w[X2_NC + c]));
-                    const unsigned long long a45 = (unsigned long long) __float2uint_rz(fu(w[2 * X2_NC + c]));
-                    acc[c] += (a01 << 32) + (a23 << 16) + a45;
-                }
-            }
-            tc_fence_before();
-            mbar_arrive(&rt_free[sb]);
-            return true;
-        };
-        for (int v = blockIdx.x; ok && v < p.nunits; v += gridDim.x) {
+        for (int v = blockIdx.x; ok && v < p.nunits; v += gridDim.x, nunit++) {
             int kb, t0, t1;
             x_unit(p, v, kb, t0, t1);
             for (int t = t0; t < t1; t++, jt++) {
@@ -839,13 +804,13 @@ __global__ void __launch_bounds__(X2_THREADS, 1)
                     break;
                 }
                 tc_fence_after();
-                uint32_t va[4 * 8];
+                // this group's 8 centres of the seven slices: columns 16 sl + 8 g
+                uint32_t va[XS * 8];
                 {
-                    const uint32_t col = lane_base + (uint32_t) (S_COL + b * 4 * X2_NC + 8 * g);
-                    tmem_ld8p(col, va);
-                    tmem_ld8p(col + X2_NC, va + 8);
-                    tmem_ld8p(col + 2 * X2_NC, va + 16);
-                    tmem_ld8p(col + 3 * X2_NC, va + 24);
+                    const uint32_t col = lane_base + (uint32_t) (S_COL + b * S_STRIDE + 8 * g);
+#pragma unroll
+                    for (int sl = 0; sl < XS; sl++)
+                        tmem_ld8p(col + (uint32_t) (sl * X2_NC), va + 8 * sl);
                     tmem_ld_wait();
                 }
                 tc_fence_before();
@@ -856,15 +821,25 @@ __global__ void __launch_bounds__(X2_THREADS, 1)
                 const float R0 = rq.x * 0x1p40f, R1 = rq.y * 0x1p24f, R2 = rq.z * 256.f;
                 const df::f2x nls = {lq.x, lq.y};  // -log s_n
                 const int flag = (int) lq.z;
-                uint32_t top[8], bot[8];
+                // the R buffer of tile jt is free once MMA 2 of tile jt - 2 completed
+                if (jt >= 2 && !mbar_wait(&r_empty[b], (uint32_t) (((jt - 2) >> 1) & 1), p.status, 61)) {
+                    ok = false;
+                    break;
+                }
+                unsigned char *rbp = Rbuf + b * X2_RBUF + (pt >> 6) * X2_RPANEL;
 #pragma unroll
                 for (int c = 0; c < 8; c++) {
                     uint32_t tp = 0u, bt = 0u;
                     const int k = kb * X2_NC + 8 * g + c;
                     if (k < p.K) {
                         if (flag == 0) {
-                            const df::f2x dI = df::sum4(fmaf(fu(va[c]), 0x1p40f, -R0), fmaf(fu(va[8 + c]), 0x1p24f, -R1),
-                                                        fmaf(fu(va[16 + c]), 256.f, -R2), fu(va[24 + c]) - rq.w);
+                            // slices side by side: the even one is stored times 256, so
+                            // each pair is an exact FP32 sum
+                            const float a01 = fu(va[c]) + fu(va[8 + c]);
+                            const float a23 = fu(va[16 + c]) + fu(va[24 + c]);
+                            const float a45 = fu(va[32 + c]) + fu(va[40 + c]);
+                            const df::f2x dI = df::sum4(fmaf(a01, 0x1p40f, -R0), fmaf(a23, 0x1p24f, -R1),
+                                                        fmaf(a45, 256.f, -R2), fu(va[48 + c]) - rq.w);
                             // R = 0 where the reference's exp(-beta d / 2) underflows
                             if (!(dI.h < lq.w))
                                 df::fixed48_parts(df::exp_df(df::add(df::mul(dI, kc), nls), tab), tp, bt);
@@ -882,40 +857,18 @@ __global__ void __launch_bounds__(X2_THREADS, 1)
                             bt = (1u << 24) - 1u;
                         }
                     }
-                    top[c] = tp;
-                    bot[c] = bt;
-                }
-                // the R buffer of tile jt is free once MMA 2 of tile jt - 2 completed
-                if (jt >= 2 && !mbar_wait(&r_empty[b], (uint32_t) (((jt - 2) >> 1) & 1), p.status, 61)) {
-                    ok = false;
-                    break;
-                }
-                // digit d of R (pairs: 256 d0 + d1, 256 d2 + d3, 256 d4 + d5) at row
-                // 8 g + c, column pt of slice d (K-major, 128-byte swizzle)
-                unsigned char *rb = Rbuf + b * X2_RBUF + (pt >> 6) * X2_YPANEL;
-#pragma unroll
-                for (int c = 0; c < 8; c++) {
+                    // digit d of R at row 16 d + 8 g + c, column pt (K-major, 128-byte swizzle)
                     const int cr = 8 * g + c;
-                    unsigned char *rowp = rb + cr * 128 + ((((pt & 63) >> 3) ^ (cr & 7)) << 4) + (pt & 7) * 2;
-                    const uint32_t tp = top[c], bt = bot[c];
-                    *(uint16_t *) (rowp + 0 * X2_RSLICE) = (uint16_t) bf16_small256(tp >> 16);
-                    *(uint16_t *) (rowp + 1 * X2_RSLICE) = (uint16_t) bf16_small((tp >> 8) & 255u);
-                    *(uint16_t *) (rowp + 2 * X2_RSLICE) = (uint16_t) bf16_small256(tp & 255u);
-                    *(uint16_t *) (rowp + 3 * X2_RSLICE) = (uint16_t) bf16_small(bt >> 16);
-                    *(uint16_t *) (rowp + 4 * X2_RSLICE) = (uint16_t) bf16_small256((bt >> 8) & 255u);
-                    *(uint16_t *) (rowp + 5 * X2_RSLICE) = (uint16_t) bf16_small(bt & 255u);
+                    unsigned char *rowp = rbp + cr * 128 + ((((pt & 63) >> 3) ^ (cr & 7)) << 4) + (pt & 7) * 2;
+                    *(uint16_t *) (rowp + 0 * X2_NC * 128) = (uint16_t) bf16_small(tp >> 16);
+                    *(uint16_t *) (rowp + 1 * X2_NC * 128) = (uint16_t) bf16_small((tp >> 8) & 255u);
+                    *(uint16_t *) (rowp + 2 * X2_NC * 128) = (uint16_t) bf16_small(tp & 255u);
+                    *(uint16_t *) (rowp + 3 * X2_NC * 128) = (uint16_t) bf16_small(bt >> 16);
+                    *(uint16_t *) (rowp + 4 * X2_NC * 128) = (uint16_t) bf16_small((bt >> 8) & 255u);
+                    *(uint16_t *) (rowp + 5 * X2_NC * 128) = (uint16_t) bf16_small(bt & 255u);
                 }
                 fence_proxy_async_smem();
                 mbar_arrive(&r_full[b]);
-                // a segment that ended with the previous tile (the unit's last
-                // segment is moved after the loop)
-                if (t > t0 && (((t - 1 - t0) % X2_SEG) == X2_SEG - 1)) {
-                    if (!drain_seg(gseg)) {
-                        ok = false;
-                        break;
-                    }
-                    gseg++;
-                }
                 if (++s == 2) {
                     s = 0;
                     ph ^= 1u;
@@ -923,24 +876,42 @@ __global__ void __launch_bounds__(X2_THREADS, 1)
             }
             if (!ok)
                 break;
-            if (!drain_seg(gseg)) {
+            // the unit's R T: six exact digit sums per (dimension, centre), to
+            // the global accumulators (exact, order-independent)
+            if (!mbar_wait(rt_full, (uint32_t) (nunit & 1), p.status, 58)) {
                 ok = false;
                 break;
             }
-            gseg++;
-            // the unit's sums into the global accumulators (exact)
-            if (own && dim < DP) {
+            tc_fence_after();
+            if (own) {
+                unsigned long long acc[X2_NC];
 #pragma unroll
-                for (int c = 0; c < X2_NC; c++) {
-                    const int k = kb * X2_NC + c;
-                    if (k < p.K) {
-                        unsigned long long *dst = p.RTacc + (size_t) k * DP + dim;
-                        atomicAdd(dst, acc[c] >> 24);
-                        atomicAdd(dst + (size_t) p.Kpad * DP, acc[c] & 0xFFFFFFull);
-                    }
+                for (int c = 0; c < X2_NC; c++)
                     acc[c] = 0ull;
+                const uint32_t col = lane_base + (uint32_t) (RT_COL + mb * X2_N2);
+#pragma unroll
+                for (int dg = 0; dg < 6; dg++) {
+                    uint32_t w[X2_NC];
+                    tmem_ld16p(col + (uint32_t) (dg * X2_NC), w);
+                    tmem_ld_wait();
+#pragma unroll
+                    for (int c = 0; c < X2_NC; c++)
+                        acc[c] += (unsigned long long) __float2uint_rz(fu(w[c])) << (8 * (5 - dg));
+                }
+                if (dim < DP) {
+#pragma unroll
+                    for (int c = 0; c < X2_NC; c++) {
+                        const int k = kb * X2_NC + c;
+                        if (k < p.K) {
+                            unsigned long long *dst = p.RTacc + (size_t) k * DP + dim;
+                            atomicAdd(dst, acc[c] >> 24);
+                            atomicAdd(dst + (size_t) p.Kpad * DP, acc[c] & 0xFFFFFFull);
+                        }
+                    }
                 }
             }
+            tc_fence_before();
+            mbar_arrive(rt_free);
         }
         if (!ok)
             failed = 1;
@@ -1096,7 +1067,7 @@ int x64_create(XState **out, int N, int D, int K, int sms, const double *T64, cu
     st->nunits = ((st->ntiles + X2_UNIT_TILES - 1) / X2_UNIT_TILES) * st->kblocks;
     st->grid2 = st->nunits < sms ? st->nunits : sms;
     st->smem2 = 1024 + 2 * (size_t) (st->npanel * X2_TPANEL + X2_CONST) + 2 * (size_t) X2_RBUF +
-                (size_t) XS * st->npanel * X2_YPANEL + 20 * 8 + 8 + 512;
+                (size_t) st->npanel * X2_YPANEL + 17 * 8 + 8 + 512;
     if (nslot < 16 || st->smem2 > (size_t) SMEM_LIMIT || !st->pass1 || !st->pass2) {
         set_error(DGTM_ENOTSUP, "x64_create: no shared-memory plan (D = %d)", D);
         return fail(DGTM_ENOTSUP);
