@@ -121,9 +121,10 @@ def _p(a: np.ndarray):
 
 
 def selftest():
-    """Largest errors of the three tensor-core operand configurations (0 = exact)."""
-    errs = (ctypes.c_double * 3)()
-    _check(load_library().dgtm_selftest(errs, 3))
+    """Largest errors of the three tensor-core operand configurations (0 = exact),
+    then the number of packed double-float lanes that differ from the scalar ones."""
+    errs = (ctypes.c_double * 4)()
+    _check(load_library().dgtm_selftest(errs, 4))
     return list(errs)
 
 

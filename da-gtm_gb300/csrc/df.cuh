@@ -176,13 +176,13 @@ DF_HD f2x exp_df(f2x x, const TAB &tab)
     // exp(r) - 1 = r + r^2/2 + r^3/6 + r^4 (1/24 + r/120)
     float r2h, r2l;
     two_prod(rh, rh, r2h, r2l);
-    r2l = fmaf(2.0f * rh, rl, r2l);
+    r2l = fmaf(mul_rn(2.0f, rh), rl, r2l);
     float t3, e3;
     two_prod(rh, r2h, t3, e3);  // r^3 = t3 + e3 (+ rh r2l)
     e3 = fmaf(rh, r2l, e3);
     const float r4 = mul_rn(t3, rh);
-    const float c = fmaf(t3, SIXTH_H, fmaf(e3, SIXTH_H, mul_rn(t3, SIXTH_L))) +
-                    r4 * fmaf(rh, 1.0f / 120.0f, 1.0f / 24.0f);
+    const float c = fmaf(r4, fmaf(rh, 1.0f / 120.0f, 1.0f / 24.0f),
+                         fmaf(t3, SIXTH_H, fmaf(e3, SIXTH_H, mul_rn(t3, SIXTH_L))));
     float ph, pl;
     two_sum(rh, mul_rn(0.5f, r2h), ph, pl);
     pl = add_rn(pl, add_rn(add_rn(rl, mul_rn(0.5f, r2l)), c));

@@ -49,6 +49,7 @@
 // reference's own accuracy (FP64 sums over D, K and N).
 #include "common.cuh"
 #include "df.cuh"
+#include "df2.cuh"
 #include "kernels.cuh"
 #include "sm100.cuh"
 #include "x64.cuh"
@@ -404,6 +405,7 @@ __global__ void __launch_bounds__(X1_THREADS, 1)
         const int n = n0 + g * X1_TILE + row;
         const double inv = p.sc->inv;
         const df::f2x k1 = df::from_double(2.0 * p.c1 * inv), k2 = df::from_double(2.0 * p.c2 * inv);
+        const df2::x2 k12 = df2::pack(k1, k2), k11 = df2::pack(k1, k1);
         // the reference centre's slice partials (and the first three scaled)
         float r0 = 0.f, r1 = 0.f, r2 = 0.f, r3 = 0.f, R0 = 0.f, R1 = 0.f, R2 = 0.f;
         bool have = false;
@@ -472,15 +474,35 @@ __global__ void __launch_bounds__(X1_THREADS, 1)
                         have = true;
                     }
                 }
+                // exact slice differences (each below 2^24), then 48 bits of their sum
+                auto delta = [&](int j) {
+                    return df::sum4(fmaf(fu(v[j]), 0x1p40f, -R0), fmaf(fu(v[8 + j]), 0x1p24f, -R1),
+                                    fmaf(fu(v[16 + j]), 256.f, -R2), fu(v[24 + j]) - r3);
+                };
+                if (p.two_temps) {
+                    // the two temperatures of a pair in the two lanes
 #pragma unroll
-                for (int j = 0; j < 8; j++) {
-                    if (8 * bt + j < nvalid) {
-                        // exact slice differences (each below 2^24), then 48 bits of their sum
-                        const df::f2x dI = df::sum4(fmaf(fu(v[j]), 0x1p40f, -R0), fmaf(fu(v[8 + j]), 0x1p24f, -R1),
-                                                    fmaf(fu(v[16 + j]), 256.f, -R2), fu(v[24 + j]) - r3);
-                        s1.add(df::exp_df(df::mul(dI, k1), tab));
-                        if (p.two_temps)
-                            s2.add(df::exp_df(df::mul(dI, k2), tab));
+                    for (int j = 0; j < 8; j++) {
+                        if (8 * bt + j < nvalid) {
+                            const df::f2x dI = delta(j);
+                            const df2::x2 e = df2::exp_df(df2::mul(df2::pack(dI, dI), k12), tab);
+                            s1.add(df2::lane0(e));
+                            s2.add(df2::lane1(e));
+                        }
+                    }
+                } else {
+                    // two pairs in the two lanes
+#pragma unroll
+                    for (int j = 0; j < 8; j += 2) {
+                        const bool va0 = 8 * bt + j < nvalid, va1 = 8 * bt + j + 1 < nvalid;
+                        if (va0) {
+                            const df::f2x z = {0.f, 0.f};
+                            const df2::x2 e =
+                                df2::exp_df(df2::mul(df2::pack(delta(j), va1 ? delta(j + 1) : z), k11), tab);
+                            s1.add(df2::lane0(e));
+                            if (va1)
+                                s1.add(df2::lane1(e));
+                        }
                     }
                 }
             }
@@ -827,45 +849,57 @@ __global__ void __launch_bounds__(X2_THREADS, 1)
                     break;
                 }
                 unsigned char *rbp = Rbuf + b * X2_RBUF + (pt >> 6) * X2_RPANEL;
+                const df2::x2 kc2 = df2::pack(kc, kc), nls2 = df2::pack(nls, nls);
+                // two centres at a time: their exponentials in the two lanes
 #pragma unroll
-                for (int c = 0; c < 8; c++) {
-                    uint32_t tp = 0u, bt = 0u;
-                    const int k = kb * X2_NC + 8 * g + c;
-                    if (k < p.K) {
-                        if (flag == 0) {
-                            // slices side by side: the even one is stored times 256, so
-                            // each pair is an exact FP32 sum
-                            const float a01 = fu(va[c]) + fu(va[8 + c]);
-                            const float a23 = fu(va[16 + c]) + fu(va[24 + c]);
-                            const float a45 = fu(va[32 + c]) + fu(va[40 + c]);
-                            const df::f2x dI = df::sum4(fmaf(a01, 0x1p40f, -R0), fmaf(a23, 0x1p24f, -R1),
-                                                        fmaf(a45, 256.f, -R2), fu(va[48 + c]) - rq.w);
-                            // R = 0 where the reference's exp(-beta d / 2) underflows
-                            if (!(dI.h < lq.w))
-                                df::fixed48_parts(df::exp_df(df::add(df::mul(dI, kc), nls), tab), tp, bt);
-                        } else if (flag == 1) {
-                            // comm/mpicomm.c:382-389: R = 1/K
-                            tp = (uint32_t) (rinvK >> 24);
-                            bt = (uint32_t) (rinvK & 0xFFFFFFull);
-                        }
-                        if (bt >= (1u << 24)) {
-                            tp += 1u;
-                            bt -= 1u << 24;
-                        }
-                        if (tp >= (1u << 24)) {  // R = 1: just below 2^48
-                            tp = (1u << 24) - 1u;
-                            bt = (1u << 24) - 1u;
-                        }
+                for (int c = 0; c < 8; c += 2) {
+                    df::f2x dI[2];
+#pragma unroll
+                    for (int h = 0; h < 2; h++) {
+                        // slices side by side: the even one is stored times 256, so
+                        // each pair is an exact FP32 sum
+                        const int cc = c + h;
+                        const float a01 = fu(va[cc]) + fu(va[8 + cc]);
+                        const float a23 = fu(va[16 + cc]) + fu(va[24 + cc]);
+                        const float a45 = fu(va[32 + cc]) + fu(va[40 + cc]);
+                        dI[h] = df::sum4(fmaf(a01, 0x1p40f, -R0), fmaf(a23, 0x1p24f, -R1), fmaf(a45, 256.f, -R2),
+                                         fu(va[48 + cc]) - rq.w);
                     }
-                    // digit d of R at row 16 d + 8 g + c, column pt (K-major, 128-byte swizzle)
-                    const int cr = 8 * g + c;
-                    unsigned char *rowp = rbp + cr * 128 + ((((pt & 63) >> 3) ^ (cr & 7)) << 4) + (pt & 7) * 2;
-                    *(uint16_t *) (rowp + 0 * X2_NC * 128) = (uint16_t) bf16_small(tp >> 16);
-                    *(uint16_t *) (rowp + 1 * X2_NC * 128) = (uint16_t) bf16_small((tp >> 8) & 255u);
-                    *(uint16_t *) (rowp + 2 * X2_NC * 128) = (uint16_t) bf16_small(tp & 255u);
-                    *(uint16_t *) (rowp + 3 * X2_NC * 128) = (uint16_t) bf16_small(bt >> 16);
-                    *(uint16_t *) (rowp + 4 * X2_NC * 128) = (uint16_t) bf16_small((bt >> 8) & 255u);
-                    *(uint16_t *) (rowp + 5 * X2_NC * 128) = (uint16_t) bf16_small(bt & 255u);
+                    const df2::x2 e =
+                        df2::exp_df(df2::add(df2::mul(df2::pack(dI[0], dI[1]), kc2), nls2), tab);
+#pragma unroll
+                    for (int h = 0; h < 2; h++) {
+                        const int cc = c + h;
+                        uint32_t tp = 0u, bt = 0u;
+                        const int k = kb * X2_NC + 8 * g + cc;
+                        if (k < p.K) {
+                            // R = 0 where the reference's exp(-beta d / 2) underflows
+                            if (flag == 0 && !(dI[h].h < lq.w)) {
+                                df::fixed48_parts(h ? df2::lane1(e) : df2::lane0(e), tp, bt);
+                            } else if (flag == 1) {
+                                // comm/mpicomm.c:382-389: R = 1/K
+                                tp = (uint32_t) (rinvK >> 24);
+                                bt = (uint32_t) (rinvK & 0xFFFFFFull);
+                            }
+                            if (bt >= (1u << 24)) {
+                                tp += 1u;
+                                bt -= 1u << 24;
+                            }
+                            if (tp >= (1u << 24)) {  // R = 1: just below 2^48
+                                tp = (1u << 24) - 1u;
+                                bt = (1u << 24) - 1u;
+                            }
+                        }
+                        // digit d of R at row 16 d + 8 g + cc, column pt (K-major, 128-byte swizzle)
+                        const int cr = 8 * g + cc;
+                        unsigned char *rowp = rbp + cr * 128 + ((((pt & 63) >> 3) ^ (cr & 7)) << 4) + (pt & 7) * 2;
+                        *(uint16_t *) (rowp + 0 * X2_NC * 128) = (uint16_t) bf16_small(tp >> 16);
+                        *(uint16_t *) (rowp + 1 * X2_NC * 128) = (uint16_t) bf16_small((tp >> 8) & 255u);
+                        *(uint16_t *) (rowp + 2 * X2_NC * 128) = (uint16_t) bf16_small(tp & 255u);
+                        *(uint16_t *) (rowp + 3 * X2_NC * 128) = (uint16_t) bf16_small(bt >> 16);
+                        *(uint16_t *) (rowp + 4 * X2_NC * 128) = (uint16_t) bf16_small((bt >> 8) & 255u);
+                        *(uint16_t *) (rowp + 5 * X2_NC * 128) = (uint16_t) bf16_small(bt & 255u);
+                    }
                 }
                 fence_proxy_async_smem();
                 mbar_arrive(&r_full[b]);

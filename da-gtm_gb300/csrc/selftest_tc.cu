@@ -8,6 +8,8 @@
 //              responsibilities never leave the SM).
 // Each launch is one CTA of 128 threads; every wait is bounded.
 #include "common.cuh"
+#include "df.cuh"
+#include "df2.cuh"
 #include "sm100.cuh"
 
 #include <cuda.h>
@@ -24,6 +26,42 @@ using namespace sm100;
 namespace {
 
 constexpr int ST_M = 128;
+
+__device__ __forceinline__ bool same_bits(df::f2x a, df::f2x b)
+{
+    return __float_as_uint(a.h) == __float_as_uint(b.h) && __float_as_uint(a.l) == __float_as_uint(b.l);
+}
+
+// The packed double-float operations (df2.cuh) against the scalar ones
+// (df.cuh), lane by lane, bitwise: n argument pairs spread over [-45.5, 1]
+// with full low parts, table edges and the cut; counts the mismatching lanes.
+__global__ void df2_check_kernel(int n, unsigned long long *mismatch)
+{
+    __shared__ float2 tab[64];
+    if (threadIdx.x < 64) {
+        float h, l;
+        df::exp_table_entry(threadIdx.x, h, l);
+        tab[threadIdx.x] = make_float2(h, l);
+    }
+    __syncthreads();
+    unsigned long long bad = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const unsigned ua = (unsigned) i * 2654435761u, ub = (unsigned) i * 40503u + 12345u;
+        double xa = -45.5 + 46.5 * (double) (ua >> 8) / 16777216.0;
+        double xb = (i & 3) ? -45.5 + 46.5 * (double) (ub >> 8) / 16777216.0
+                            : -(double) (i % 2900) / 64.0 + 1e-9 * ((double) (ub & 1023) - 512.0);
+        const df::f2x a = df::from_double(xa), b = df::from_double(xb);
+        const df2::x2 e = df2::exp_df(df2::pack(a, b), tab);
+        bad += !same_bits(df2::lane0(e), df::exp_df(a, tab));
+        bad += !same_bits(df2::lane1(e), df::exp_df(b, tab));
+        const df2::x2 m = df2::mul(df2::pack(a, b), df2::pack(b, a));
+        bad += !same_bits(df2::lane0(m), df::mul(a, b)) + !same_bits(df2::lane1(m), df::mul(b, a));
+        const df2::x2 s = df2::add(df2::pack(a, b), df2::pack(b, a));
+        bad += !same_bits(df2::lane0(s), df::add(a, b)) + !same_bits(df2::lane1(s), df::add(b, a));
+    }
+    if (bad)
+        atomicAdd(mismatch, bad);
+}
 
 __global__ void __launch_bounds__(128) selftest_kernel(const __grid_constant__ CUtensorMap ta,
                                                        const __grid_constant__ CUtensorMap tb,
@@ -207,6 +245,25 @@ extern "C" int dgtm_selftest(double *errs, int nerrs)
     if (!errs || nerrs < 3) {
         set_error(DGTM_EINVAL, "dgtm_selftest needs room for 3 results");
         return DGTM_EINVAL;
+    }
+    if (nerrs >= 4) {
+        // the packed double-float operations against the scalar ones
+        unsigned long long *dm = nullptr, hm = 0;
+        cudaError_t e = cudaMalloc((void **) &dm, sizeof(unsigned long long));
+        if (e == cudaSuccess)
+            e = cudaMemset(dm, 0, sizeof(unsigned long long));
+        if (e == cudaSuccess) {
+            df2_check_kernel<<<256, 256>>>(1 << 20, dm);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess)
+            e = cudaMemcpy(&hm, dm, sizeof(hm), cudaMemcpyDeviceToHost);
+        cudaFree(dm);
+        if (e != cudaSuccess) {
+            set_error(DGTM_ECUDA, "selftest: %s", cudaGetErrorString(e));
+            return DGTM_ECUDA;
+        }
+        errs[3] = (double) hm;
     }
     // host data: A 128 x 128, B0 256 x 128 (K-major), B1 32 x 192 (MN-major)
     std::vector<uint16_t> hA(128 * 128), hB0(256 * 128), hB1(32 * 192);

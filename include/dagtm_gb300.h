@@ -270,7 +270,10 @@ int dgtm_fe_forward_noalloc(const float *Y, const float *T, int N, int K, int D,
  * Diagnostic: runs the three tensor-core operand configurations the split-BF16
  * kernels rely on (K-major x K-major from shared memory; K-major x MN-major;
  * tensor-memory A x MN-major) on small integer matrices and writes the largest
- * absolute error against a host product to errs[0..2] (0 when correct).
+ * absolute error against a host product to errs[0..2] (0 when correct).  With
+ * nerrs >= 4, errs[3] is the number of lanes in which the packed (f32x2)
+ * double-float exp, add and mul of the exact-slice FP64 form differ bitwise
+ * from the scalar ones over 2^20 argument pairs (0 when correct).
  * No reference counterpart (the reference has no GPU code).
  */
 int dgtm_selftest(double *errs, int nerrs);
