@@ -446,6 +446,7 @@ def main_gb300(args):
     e2e_ms = max_over_ranks(e2e_ms, world)
     e2e_value = whole_job_rate(max(1, args.e2e_steps), e2e_ms, world)
     nT = 1 if bf16_exact(T) else 2
+    exact_slices = ctx.path == "exact_slices"
     ctx.close()
 
     peaks, peak_src = measured_peaks()
@@ -461,6 +462,16 @@ def main_gb300(args):
         peak_note = (f"bf16 dense burst ({peak_src}) / 3: three BF16 products stand for one "
                      "canonical FP32-accurate product")
         tensor_util = issued / (per_launch_ms / 1000.0) / 1e12 / burst
+    elif form == "fp64" and exact_slices:
+        # the exact-slice form: integer distance products on the tensor cores,
+        # double-float epilogues on the FP32 pipe; the FP64 pipe's nominal
+        # peak is the ceiling of an FP64-pipe implementation, so frac is the
+        # gain over that ceiling (and may exceed 1)
+        peak = 1.25
+        peak_note = ("fp64 pipe nominal (1.25 TFLOP/s): the ceiling of an FP64-pipe form; this "
+                     "form runs on the tensor and FP32 pipes, frac > 1 is the gain over it")
+        slices = 7 if dom == "estep" else 7 + 6  # distance slices (+ R digits in pass 2)
+        tensor_util = slices * 2.0 * K * N * D / (per_launch_ms / 1000.0) / 1e12 / burst
     else:
         peak = 1.25 if form == "fp64" else 75.0
         peak_note = f"{form} nominal (no measured {form} peak)"
@@ -491,9 +502,10 @@ def main_gb300(args):
         c64, ms64, ph64, _, _, rec64 = run_form(torch, pkg, "fp64", T, FI, Y0, beta0, temp0,
                                                 args.fp64_steps, 1, rank, world, stream_cls,
                                                 probe=want_err)
+        path64 = c64.path
         c64.close()
         fp64 = {"value": world * args.fp64_steps / (ms64 / 1000.0), "unit": "EM iters/s",
-                "ms_per_step": ms64 / args.fp64_steps, "steps": args.fp64_steps}
+                "ms_per_step": ms64 / args.fp64_steps, "steps": args.fp64_steps, "path": path64}
         if want_err:
             errors = form_errors(rec, rec64, N, D, float((T * T).sum()))
     cpu = None
@@ -511,6 +523,8 @@ def main_gb300(args):
             "config": {"workload": f"DA-GTM EM iteration, N={N}, D={D}, K={K} (20^3), "
                                    f"M=64 (4^3) + bias, {form} form",
                        "N": N, "D": D, "K": K, "M": 64, "L": 3, "form": form,
+                       "path": "exact_slices" if exact_slices else ("split_bf16" if form == "bf16x3"
+                                                                     else "cuda_cores"),
                        "temp": temp0, "l2": "inputs larger than L2 (no flush)",
                        "parallelism": f"replicas x{world}"},
             "e2e": {"value": e2e_value, "unit": "EM iters/s", "h2d_bytes_per_step": h2d,

@@ -479,8 +479,22 @@ __global__ void __launch_bounds__(X1_THREADS, 1)
                     return df::sum4(fmaf(fu(v[j]), 0x1p40f, -R0), fmaf(fu(v[8 + j]), 0x1p24f, -R1),
                                     fmaf(fu(v[16 + j]), 256.f, -R2), fu(v[24 + j]) - r3);
                 };
-                if (p.two_temps) {
-                    // the two temperatures of a pair in the two lanes
+                if (p.two_temps && 8 * bt + 8 <= nvalid) {
+                    // a full batch, straight-line code (one basic block, so the
+                    // eight chains can overlap): the two temperatures of a pair
+                    // in the two lanes
+                    df2::x2 e[8];
+#pragma unroll
+                    for (int j = 0; j < 8; j++) {
+                        const df::f2x dI = delta(j);
+                        e[j] = df2::exp_df(df2::mul(df2::pack(dI, dI), k12), tab);
+                    }
+#pragma unroll
+                    for (int j = 0; j < 8; j++) {
+                        s1.add(df2::lane0(e[j]));
+                        s2.add(df2::lane1(e[j]));
+                    }
+                } else if (p.two_temps) {
 #pragma unroll
                     for (int j = 0; j < 8; j++) {
                         if (8 * bt + j < nvalid) {
@@ -850,23 +864,26 @@ __global__ void __launch_bounds__(X2_THREADS, 1)
                 }
                 unsigned char *rbp = Rbuf + b * X2_RBUF + (pt >> 6) * X2_RPANEL;
                 const df2::x2 kc2 = df2::pack(kc, kc), nls2 = df2::pack(nls, nls);
-                // two centres at a time: their exponentials in the two lanes
+                // two centres at a time in the two lanes; all eight exponentials
+                // first, in one basic block (the guards act on the results)
+                df::f2x dI[8];
+                df2::x2 e4[4];
+#pragma unroll
+                for (int cc = 0; cc < 8; cc++) {
+                    // slices side by side: the even one is stored times 256, so
+                    // each pair is an exact FP32 sum
+                    const float a01 = fu(va[cc]) + fu(va[8 + cc]);
+                    const float a23 = fu(va[16 + cc]) + fu(va[24 + cc]);
+                    const float a45 = fu(va[32 + cc]) + fu(va[40 + cc]);
+                    dI[cc] = df::sum4(fmaf(a01, 0x1p40f, -R0), fmaf(a23, 0x1p24f, -R1), fmaf(a45, 256.f, -R2),
+                                      fu(va[48 + cc]) - rq.w);
+                }
+#pragma unroll
+                for (int c = 0; c < 8; c += 2)
+                    e4[c / 2] = df2::exp_df(df2::add(df2::mul(df2::pack(dI[c], dI[c + 1]), kc2), nls2), tab);
 #pragma unroll
                 for (int c = 0; c < 8; c += 2) {
-                    df::f2x dI[2];
-#pragma unroll
-                    for (int h = 0; h < 2; h++) {
-                        // slices side by side: the even one is stored times 256, so
-                        // each pair is an exact FP32 sum
-                        const int cc = c + h;
-                        const float a01 = fu(va[cc]) + fu(va[8 + cc]);
-                        const float a23 = fu(va[16 + cc]) + fu(va[24 + cc]);
-                        const float a45 = fu(va[32 + cc]) + fu(va[40 + cc]);
-                        dI[h] = df::sum4(fmaf(a01, 0x1p40f, -R0), fmaf(a23, 0x1p24f, -R1), fmaf(a45, 256.f, -R2),
-                                         fu(va[48 + cc]) - rq.w);
-                    }
-                    const df2::x2 e =
-                        df2::exp_df(df2::add(df2::mul(df2::pack(dI[0], dI[1]), kc2), nls2), tab);
+                    const df2::x2 e = e4[c / 2];
 #pragma unroll
                     for (int h = 0; h < 2; h++) {
                         const int cc = c + h;
@@ -874,7 +891,7 @@ __global__ void __launch_bounds__(X2_THREADS, 1)
                         const int k = kb * X2_NC + 8 * g + cc;
                         if (k < p.K) {
                             // R = 0 where the reference's exp(-beta d / 2) underflows
-                            if (flag == 0 && !(dI[h].h < lq.w)) {
+                            if (flag == 0 && !(dI[cc].h < lq.w)) {
                                 df::fixed48_parts(h ? df2::lane1(e) : df2::lane0(e), tp, bt);
                             } else if (flag == 1) {
                                 // comm/mpicomm.c:382-389: R = 1/K
