@@ -189,8 +189,12 @@ DF_HD f2x exp_df(f2x x, const TAB &tab)
 {
     if (!(x.h >= EXP_CUT))
         return {0.f, 0.f};
-    const float kf = rint_small(mul_rn(x.h, EXP_INV));  // |x EXP_INV| < 2^13
-    const int k = int_small(kf);
+    // k = rint(x.h 64/ln2) from the exact product in one FMA (|x EXP_INV| < 2^13):
+    // the packed form issues the same FMA, so both pick the same k on the
+    // arguments whose product lies within a rounding of a half-integer
+    const float kplus = fmaf(x.h, EXP_INV, MAGIC);
+    const float kf = sub_rn(kplus, MAGIC);
+    const int k = float_bits(kplus) - 0x4B400000;
     // r = x - k ln2/64 (exact r1; k L2 split exactly; k L3 rounded far below 2^-52)
     const float r1 = fmaf(-kf, EXP_L1, x.h);
     float p2, e2;
