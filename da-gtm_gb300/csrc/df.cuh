@@ -119,36 +119,6 @@ DF_HD f2x sum4(float u, float v, float w1, float w2)
     return add(a, b);
 }
 
-// ---------------------------------------------------------------- conversions
-// Rounding and float -> int conversions through the FP32 adder and the
-// integer unit (x + 1.5 2^23 has its integer part in the low mantissa bits),
-// instead of the slower conversion instructions; valid for |x| < 2^22.
-constexpr float MAGIC = 12582912.0f;  // 1.5 2^23
-
-DF_HD int float_bits(float x)
-{
-#if defined(__CUDA_ARCH__)
-    return __float_as_int(x);
-#else
-    int b;
-    memcpy(&b, &x, 4);
-    return b;
-#endif
-}
-
-// round to nearest (ties to even), |x| < 2^22
-DF_HD float rint_small(float x) { return sub_rn(add_rn(x, MAGIC), MAGIC); }
-
-// the integer of an integral float, |x| < 2^22
-DF_HD int int_small(float x) { return float_bits(add_rn(x, MAGIC)) - 0x4B400000; }
-
-// floor, |x| < 2^22
-DF_HD float floor_small(float x)
-{
-    const float f = rint_small(x);
-    return (f > x) ? sub_rn(f, 1.0f) : f;
-}
-
 // FP64 value -> double-float (48 of its 53 bits)
 DF_HD f2x from_double(double x)
 {
@@ -189,12 +159,8 @@ DF_HD f2x exp_df(f2x x, const TAB &tab)
 {
     if (!(x.h >= EXP_CUT))
         return {0.f, 0.f};
-    // k = rint(x.h 64/ln2) from the exact product in one FMA (|x EXP_INV| < 2^13):
-    // the packed form issues the same FMA, so both pick the same k on the
-    // arguments whose product lies within a rounding of a half-integer
-    const float kplus = fmaf(x.h, EXP_INV, MAGIC);
-    const float kf = sub_rn(kplus, MAGIC);
-    const int k = float_bits(kplus) - 0x4B400000;
+    const float kf = rintf(mul_rn(x.h, EXP_INV));
+    const int k = (int) kf;
     // r = x - k ln2/64 (exact r1; k L2 split exactly; k L3 rounded far below 2^-52)
     const float r1 = fmaf(-kf, EXP_L1, x.h);
     float p2, e2;
@@ -242,44 +208,46 @@ DF_HD f2x exp_df(f2x x, const TAB &tab)
 }
 
 // ---------------------------------------------------------------- fixed point
-// round(E 2^48) for 0 <= E < 2 (E a normalised double-float), built from
-// 20 + 14 + 14 bit pieces so that every conversion stays within the FP32
-// adder's integer range; rem receives the rounding remainder E 2^48 - result
-// in [-1/2, 1/2] (to 2^-10 of a unit).  A sum of many terms is exact to
-// 2^-48 in the integers plus the FP32 sum of the remainders.
-DF_HD uint64_t fixed48r(f2x e, float &rem)
+// round(E 2^48) for 0 <= E < 2 (E a normalised double-float), as a 24-bit top
+// and a bottom in [0, 2^24] whose sum top 2^24 + bottom is the result.
+DF_HD void fixed48_parts(f2x e, uint32_t &top, uint32_t &bot)
 {
-    const float z = mul_rn(e.h, 1048576.0f);   // E_h 2^20 < 2^21, exact
-    const float zf = floor_small(z);
-    const float lz = mul_rn(e.l, 1048576.0f);  // |lz| <= ulp(z) / 2
-    // z an integer and the low part negative: the top is z - 1
+    const float z = mul_rn(e.h, 16777216.0f);  // exact
+    const float zf = floorf(z);
+    const float lz = mul_rn(e.l, 16777216.0f);  // |lz| <= ulp(z) / 2
+    // z an integer and the low part negative: the top is z - 1 (in integers:
+    // above 2^24, z - 1 is not an FP32 number)
     const bool dec = (zf == z) && (lz < 0.f);
-    const float top = dec ? sub_rn(zf, 1.0f) : zf;
-    // the fraction above the top, exactly: fs + fe, fs in [0, 1]
-    float fs, fe;
-    two_sum(dec ? 1.0f : sub_rn(z, zf), lz, fs, fe);
-    const float y = mul_rn(fs, 16384.0f);      // exact
-    const float y1 = floor_small(y);
-    // the last 14 bits and below: (y - y1) 2^14 + fe 2^28, |w| < 2^15
-    const float w = fmaf(fe, 268435456.0f, mul_rn(sub_rn(y, y1), 16384.0f));
-    const float b2 = rint_small(w);
-    rem = sub_rn(w, b2);
-    return ((uint64_t) (uint32_t) int_small(top) << 28) + ((uint64_t) (uint32_t) int_small(y1) << 14) +
-           (uint64_t) (int64_t) int_small(b2);
+    top = (uint32_t) zf - (dec ? 1u : 0u);
+    // in [0, 1]: the fraction of E 2^24 above the top
+    const float frac = dec ? add_rn(1.0f, lz) : add_rn(sub_rn(z, zf), lz);
+    bot = (uint32_t) rintf(mul_rn(frac, 16777216.0f));
 }
 
 DF_HD uint64_t fixed48(f2x e)
 {
-    float rem;
-    return fixed48r(e, rem);
+    uint32_t top, bot;
+    fixed48_parts(e, top, bot);
+    return ((uint64_t) top << 24) + (uint64_t) bot;
 }
 
-// fixed48 as a 24-bit top and a 24-bit bottom (top 2^24 + bottom)
-DF_HD void fixed48_parts(f2x e, uint32_t &top, uint32_t &bot)
+// round(E 2^48) for 0 <= E < 2 as fixed48, and the rounding remainder
+// E 2^48 - round(E 2^48) in [-1/2, 1/2] to ~2^-24 of itself: a sum of many
+// terms is exact to 2^-48 in the integers plus the FP32 sum of remainders.
+DF_HD uint64_t fixed48r(f2x e, float &rem)
 {
-    const uint64_t v = fixed48(e);
-    top = (uint32_t) (v >> 24);
-    bot = (uint32_t) (v & 0xFFFFFFull);
+    const float z = mul_rn(e.h, 16777216.0f);  // exact
+    const float zf = floorf(z);
+    const float lz = mul_rn(e.l, 16777216.0f);
+    const bool dec = (zf == z) && (lz < 0.f);
+    const uint32_t top = (uint32_t) zf - (dec ? 1u : 0u);
+    // the fraction above the top, exactly: fs + fe
+    float fs, fe;
+    two_sum(dec ? 1.0f : sub_rn(z, zf), lz, fs, fe);
+    const float scaled = mul_rn(fs, 16777216.0f);  // exact
+    const float bf = rintf(scaled);
+    rem = fmaf(fe, 16777216.0f, sub_rn(scaled, bf));
+    return ((uint64_t) top << 24) + (uint64_t) (uint32_t) bf;
 }
 
 // round(v 2^63) for an FP32 |v| < 2, from its bits (exact for |v| >= 2^-40;

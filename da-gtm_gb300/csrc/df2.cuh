@@ -93,10 +93,10 @@ __device__ __forceinline__ x2 exp_df(x2 x, const TAB &tab)
 {
     using namespace df;
     const float xh0 = f2_lo(x.h), xh1 = f2_hi(x.h);
-    // k = rint(x.h 64/ln2) and its integer from one FMA with 1.5 2^23, as in df::exp_df
-    const f2 kplus = fma2(x.h, splat(EXP_INV), splat(MAGIC));
-    const f2 kf = f2_sub(kplus, splat(MAGIC));
-    const int k0 = __float_as_int(f2_lo(kplus)) - 0x4B400000, k1 = __float_as_int(f2_hi(kplus)) - 0x4B400000;
+    const f2 km = f2_mul(x.h, splat(EXP_INV));
+    const float kf0 = rintf(f2_lo(km)), kf1 = rintf(f2_hi(km));
+    const f2 kf = f2_pack(kf0, kf1);
+    const int k0 = (int) kf0, k1 = (int) kf1;
     const f2 r1 = fma2(neg2(kf), splat(EXP_L1), x.h);
     f2 p2, e2;
     two_prod(kf, splat(EXP_L2), p2, e2);
