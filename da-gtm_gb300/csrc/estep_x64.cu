@@ -237,7 +237,8 @@ struct XSum {
     }
 };
 
-template <int NP>
+// TWO: the sums at both temperatures (annealing with temp != 1), else at one
+template <int NP, bool TWO>
 __global__ void __launch_bounds__(X1_THREADS, 1)
     x_pass1_kernel(const __grid_constant__ CUtensorMap tmY, const __grid_constant__ CUtensorMap tmT,
                    const X1Params p)
@@ -405,7 +406,8 @@ __global__ void __launch_bounds__(X1_THREADS, 1)
         const int n = n0 + g * X1_TILE + row;
         const double inv = p.sc->inv;
         const df::f2x k1 = df::from_double(2.0 * p.c1 * inv), k2 = df::from_double(2.0 * p.c2 * inv);
-        const df2::x2 k12 = df2::pack(k1, k2), k11 = df2::pack(k1, k1);
+        // lanes: the two temperatures of one centre (TWO), else two centres
+        const df2::x2 kk = df2::pack(k1, TWO ? k2 : k1);
         // the reference centre's slice partials (and the first three scaled)
         float r0 = 0.f, r1 = 0.f, r2 = 0.f, r3 = 0.f, R0 = 0.f, R1 = 0.f, R2 = 0.f;
         bool have = false;
@@ -423,8 +425,10 @@ __global__ void __launch_bounds__(X1_THREADS, 1)
             // Eight centres at a time (4 x 8 partials in registers), so that
             // several exponential chains fit beside them; the accumulator is
             // released after the last batch is read (the tensor pipe is idle
-            // far longer than the next chunk's MMAs take).
-#pragma unroll
+            // far longer than the next chunk's MMAs take).  The batch loop is
+            // not unrolled: one copy of its eight exponentials keeps the
+            // kernel inside the instruction cache.
+#pragma unroll 1
             for (int bt = 0; bt < X1_NC / 8; bt++) {
                 uint32_t v[32];
                 tmem_ld8p(col + (uint32_t) (8 * bt), v);
@@ -436,12 +440,13 @@ __global__ void __launch_bounds__(X1_THREADS, 1)
                     tc_fence_before();
                     mbar_arrive(&acc_empty[g]);
                 }
+                const int nv = nvalid - 8 * bt;  // valid centres in this batch (padding after them)
                 // the batch's largest acc, approximately (FP32 of the top two partials)
                 float best = -INFINITY, b0 = 0.f, b1 = 0.f, b2 = 0.f, b3 = 0.f;
 #pragma unroll
                 for (int j = 0; j < 8; j++) {
                     const float a = fmaf(fu(v[j]), 0x1p40f, fu(v[8 + j]) * 0x1p24f);
-                    if (8 * bt + j < nvalid && a > best) {
+                    if (j < nv && a > best) {
                         best = a;
                         b0 = fu(v[j]);
                         b1 = fu(v[8 + j]);
@@ -457,9 +462,10 @@ __global__ void __launch_bounds__(X1_THREADS, 1)
                         if (dI.h > 0.f) {
                             // the sums move to the new reference: s *= exp(-2c dI 2^-F)
                             const df::f2x nd = {-dI.h, -dI.l};
-                            s1.scale(df::exp_df(df::mul(nd, k1), tab));
-                            if (p.two_temps)
-                                s2.scale(df::exp_df(df::mul(nd, k2), tab));
+                            const df2::x2 e = df2::exp_df(df2::mul(df2::pack(nd, nd), kk), tab);
+                            s1.scale(df2::lane0(e));
+                            if (TWO)
+                                s2.scale(df2::lane1(e));
                             take = true;
                         }
                     }
@@ -479,44 +485,38 @@ __global__ void __launch_bounds__(X1_THREADS, 1)
                     return df::sum4(fmaf(fu(v[j]), 0x1p40f, -R0), fmaf(fu(v[8 + j]), 0x1p24f, -R1),
                                     fmaf(fu(v[16 + j]), 256.f, -R2), fu(v[24 + j]) - r3);
                 };
-                if (p.two_temps && 8 * bt + 8 <= nvalid) {
-                    // a full batch, straight-line code (one basic block, so the
-                    // eight chains can overlap): the two temperatures of a pair
-                    // in the two lanes
+                // straight-line code (one basic block, so the chains overlap);
+                // a padding centre's exponential is masked to 0, which adds
+                // nothing to the sums
+                if (TWO) {
                     df2::x2 e[8];
 #pragma unroll
                     for (int j = 0; j < 8; j++) {
                         const df::f2x dI = delta(j);
-                        e[j] = df2::exp_df(df2::mul(df2::pack(dI, dI), k12), tab);
+                        e[j] = df2::exp_df(df2::mul(df2::pack(dI, dI), kk), tab);
+                        const uint64_t keep = (j < nv) ? ~0ull : 0ull;
+                        e[j].h.v &= keep;
+                        e[j].l.v &= keep;
                     }
 #pragma unroll
                     for (int j = 0; j < 8; j++) {
                         s1.add(df2::lane0(e[j]));
                         s2.add(df2::lane1(e[j]));
                     }
-                } else if (p.two_temps) {
-#pragma unroll
-                    for (int j = 0; j < 8; j++) {
-                        if (8 * bt + j < nvalid) {
-                            const df::f2x dI = delta(j);
-                            const df2::x2 e = df2::exp_df(df2::mul(df2::pack(dI, dI), k12), tab);
-                            s1.add(df2::lane0(e));
-                            s2.add(df2::lane1(e));
-                        }
-                    }
                 } else {
-                    // two pairs in the two lanes
+                    df2::x2 e[4];
 #pragma unroll
                     for (int j = 0; j < 8; j += 2) {
-                        const bool va0 = 8 * bt + j < nvalid, va1 = 8 * bt + j + 1 < nvalid;
-                        if (va0) {
-                            const df::f2x z = {0.f, 0.f};
-                            const df2::x2 e =
-                                df2::exp_df(df2::mul(df2::pack(delta(j), va1 ? delta(j + 1) : z), k11), tab);
-                            s1.add(df2::lane0(e));
-                            if (va1)
-                                s1.add(df2::lane1(e));
-                        }
+                        e[j / 2] = df2::exp_df(df2::mul(df2::pack(delta(j), delta(j + 1)), kk), tab);
+                        const uint64_t keep =
+                            ((j < nv) ? 0x00000000FFFFFFFFull : 0ull) | ((j + 1 < nv) ? 0xFFFFFFFF00000000ull : 0ull);
+                        e[j / 2].h.v &= keep;
+                        e[j / 2].l.v &= keep;
+                    }
+#pragma unroll
+                    for (int j = 0; j < 4; j++) {
+                        s1.add(df2::lane0(e[j]));
+                        s1.add(df2::lane1(e[j]));
                     }
                 }
             }
@@ -526,7 +526,7 @@ __global__ void __launch_bounds__(X1_THREADS, 1)
             const double Iref = (double) r0 * 0x1p40 + (double) r1 * 0x1p24 + (double) r2 * 256.0 + (double) r3;
             const double dstar = p.tt[n] - 2.0 * Iref * inv;
             const double ls1 = log(s1.value());
-            const double ls2 = p.two_temps ? log(s2.value()) : ls1;
+            const double ls2 = TWO ? log(s2.value()) : ls1;
             const double lsel = p.isDA ? ls2 : ls1;
             t1 = -p.c1 * dstar + ls1;
             t2 = p.isDA ? (-p.c2 * dstar + ls2) : 0.0;
@@ -587,9 +587,13 @@ __global__ void __launch_bounds__(X1_THREADS, 1)
 
 using X1Kernel = void (*)(const CUtensorMap, const CUtensorMap, const X1Params);
 
+template <bool TWO>
 X1Kernel pass1_for(int np)
 {
-    return np == 1 ? x_pass1_kernel<1> : np == 2 ? x_pass1_kernel<2> : np == 3 ? x_pass1_kernel<3> : nullptr;
+    return np == 1   ? x_pass1_kernel<1, TWO>
+           : np == 2 ? x_pass1_kernel<2, TWO>
+           : np == 3 ? x_pass1_kernel<3, TWO>
+                     : nullptr;
 }
 
 // ---------------------------------------------------------------------------
@@ -1026,7 +1030,7 @@ struct XState {
     float4 *refq = nullptr, *lsq = nullptr;
     unsigned long long *RTacc = nullptr;
     int *status = nullptr, *hstatus = nullptr;
-    X1Kernel pass1 = nullptr;
+    X1Kernel pass1 = nullptr, pass1_two = nullptr;  // one temperature, two
     X2Kernel pass2 = nullptr;
     CUtensorMap tmT, tmY1, tmY2;
 };
@@ -1100,7 +1104,8 @@ int x64_create(XState **out, int N, int D, int K, int sms, const double *T64, cu
     st->Dp = st->npanel * PANEL;
     st->Npad = rup(N, NPAD_ALIGN);
     st->Kpad = rup(K, KPAD_ALIGN);
-    st->pass1 = pass1_for(st->npanel);
+    st->pass1 = pass1_for<false>(st->npanel);
+    st->pass1_two = pass1_for<true>(st->npanel);
     st->pass2 = pass2_for(st->npanel);
     // pass 1: the ring of digit slices (at least the staged data tiles plus a chunk)
     st->nchunk = (K + X1_NC - 1) / X1_NC;
@@ -1119,7 +1124,7 @@ int x64_create(XState **out, int N, int D, int K, int sms, const double *T64, cu
     st->grid2 = st->nunits < sms ? st->nunits : sms;
     st->smem2 = 1024 + 2 * (size_t) (st->npanel * X2_TPANEL + X2_CONST) + 2 * (size_t) X2_RBUF +
                 (size_t) st->npanel * X2_YPANEL + 17 * 8 + 8 + 512;
-    if (nslot < 16 || st->smem2 > (size_t) SMEM_LIMIT || !st->pass1 || !st->pass2) {
+    if (nslot < 16 || st->smem2 > (size_t) SMEM_LIMIT || !st->pass1 || !st->pass1_two || !st->pass2) {
         set_error(DGTM_ENOTSUP, "x64_create: no shared-memory plan (D = %d)", D);
         return fail(DGTM_ENOTSUP);
     }
@@ -1145,6 +1150,8 @@ int x64_create(XState **out, int N, int D, int K, int sms, const double *T64, cu
     e = cudaGetLastError();
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(st->pass1, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) st->smem1);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(st->pass1_two, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) st->smem1);
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(st->pass2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) st->smem2);
     if (e != cudaSuccess) {
@@ -1194,7 +1201,7 @@ int x64_estep(XState *st, const double *Y64, const double *yy, const double *tt,
     p.lsq = st->lsq;
     p.part = part;
     p.status = st->status;
-    st->pass1<<<st->blocks1, X1_THREADS, st->smem1, s>>>(st->tmY1, st->tmT, p);
+    (p.two_temps ? st->pass1_two : st->pass1)<<<st->blocks1, X1_THREADS, st->smem1, s>>>(st->tmY1, st->tmT, p);
     DGTM_CUDA_TRY(cudaGetLastError());
     *nlaunch = 3;
     return DGTM_OK;
