@@ -76,6 +76,15 @@ __device__ __forceinline__ x2 add(x2 a, x2 b)
     return {s1, s2};
 }
 
+// df::sum4 lane by lane
+__device__ __forceinline__ x2 sum4(f2 u, f2 v, f2 w1, f2 w2)
+{
+    x2 a, b;
+    two_sum(u, v, a.h, a.l);
+    two_sum(w1, w2, b.h, b.l);
+    return add(a, b);
+}
+
 // df::mul lane by lane
 __device__ __forceinline__ x2 mul(x2 a, x2 b)
 {

@@ -80,6 +80,7 @@ constexpr int X_MAXK = 60000;      // per-point sums of K terms below 2^48 (1 + 
 constexpr int X1_THREADS = 320;    // warp 0 TMA, warp 1 MMA, warps 2-9 statistics
 constexpr int X1_TILE = 128;       // points per tile; two tiles per CTA
 constexpr int X1_NC = 32;          // centres per chunk (MMA N)
+constexpr int X1_XB = 4;           // centres per statistics batch (4: measured faster than 8)
 constexpr int X1_ACC = 256;        // TMEM column of the accumulators (2 tiles x 4 x 32)
 constexpr int X1_YPANEL = X1_NC * 128;
 constexpr int X1_TPANEL = X1_TILE * 128;
@@ -422,36 +423,36 @@ __global__ void __launch_bounds__(X1_THREADS, 1)
             tc_fence_after();
             const int nvalid = min(X1_NC, p.K - c * X1_NC);  // padding centres are skipped
             const uint32_t col = lane_base + (uint32_t) (X1_ACC + g * 4 * X1_NC);
-            // Eight centres at a time (4 x 8 partials in registers), so that
-            // several exponential chains fit beside them; the accumulator is
+            // X1_XB centres at a time (4 x X1_XB partials in registers), so
+            // that several exponential chains fit beside them; the accumulator is
             // released after the last batch is read (the tensor pipe is idle
             // far longer than the next chunk's MMAs take).  The batch loop is
             // not unrolled: one copy of its eight exponentials keeps the
             // kernel inside the instruction cache.
+            constexpr int B = X1_XB;
 #pragma unroll 1
-            for (int bt = 0; bt < X1_NC / 8; bt++) {
-                uint32_t v[32];
-                tmem_ld8p(col + (uint32_t) (8 * bt), v);
-                tmem_ld8p(col + (uint32_t) (X1_NC + 8 * bt), v + 8);
-                tmem_ld8p(col + (uint32_t) (2 * X1_NC + 8 * bt), v + 16);
-                tmem_ld8p(col + (uint32_t) (3 * X1_NC + 8 * bt), v + 24);
+            for (int bt = 0; bt < X1_NC / B; bt++) {
+                uint32_t v[4 * B];
+#pragma unroll
+                for (int sl = 0; sl < 4; sl++)
+                    tmem_ldp<B>(col + (uint32_t) (sl * X1_NC + B * bt), v + B * sl);
                 tmem_ld_wait();
-                if (bt == X1_NC / 8 - 1) {
+                if (bt == X1_NC / B - 1) {
                     tc_fence_before();
                     mbar_arrive(&acc_empty[g]);
                 }
-                const int nv = nvalid - 8 * bt;  // valid centres in this batch (padding after them)
+                const int nv = nvalid - B * bt;  // valid centres in this batch (padding after them)
                 // the batch's largest acc, approximately (FP32 of the top two partials)
                 float best = -INFINITY, b0 = 0.f, b1 = 0.f, b2 = 0.f, b3 = 0.f;
 #pragma unroll
-                for (int j = 0; j < 8; j++) {
-                    const float a = fmaf(fu(v[j]), 0x1p40f, fu(v[8 + j]) * 0x1p24f);
+                for (int j = 0; j < B; j++) {
+                    const float a = fmaf(fu(v[j]), 0x1p40f, fu(v[B + j]) * 0x1p24f);
                     if (j < nv && a > best) {
                         best = a;
                         b0 = fu(v[j]);
-                        b1 = fu(v[8 + j]);
-                        b2 = fu(v[16 + j]);
-                        b3 = fu(v[24 + j]);
+                        b1 = fu(v[B + j]);
+                        b2 = fu(v[2 * B + j]);
+                        b3 = fu(v[3 * B + j]);
                     }
                 }
                 if (best > -INFINITY) {
@@ -480,41 +481,49 @@ __global__ void __launch_bounds__(X1_THREADS, 1)
                         have = true;
                     }
                 }
-                // exact slice differences (each below 2^24), then 48 bits of their sum
-                auto delta = [&](int j) {
-                    return df::sum4(fmaf(fu(v[j]), 0x1p40f, -R0), fmaf(fu(v[8 + j]), 0x1p24f, -R1),
-                                    fmaf(fu(v[16 + j]), 256.f, -R2), fu(v[24 + j]) - r3);
+                // exact slice differences (each below 2^24), then 48 bits of
+                // their sum: centres j and j + 1 in the two lanes
+                auto delta2 = [&](int j) {
+                    auto pair = [&](int i) { return df2::f2_pack(fu(v[i]), fu(v[i + 1])); };
+                    return df2::sum4(df2::fma2(pair(j), df2::splat(0x1p40f), df2::splat(-R0)),
+                                     df2::fma2(pair(B + j), df2::splat(0x1p24f), df2::splat(-R1)),
+                                     df2::fma2(pair(2 * B + j), df2::splat(256.f), df2::splat(-R2)),
+                                     df2::f2_sub(pair(3 * B + j), df2::splat(r3)));
                 };
                 // straight-line code (one basic block, so the chains overlap);
                 // a padding centre's exponential is masked to 0, which adds
                 // nothing to the sums
                 if (TWO) {
-                    df2::x2 e[8];
+                    df2::x2 e[B];
 #pragma unroll
-                    for (int j = 0; j < 8; j++) {
-                        const df::f2x dI = delta(j);
-                        e[j] = df2::exp_df(df2::mul(df2::pack(dI, dI), kk), tab);
-                        const uint64_t keep = (j < nv) ? ~0ull : 0ull;
-                        e[j].h.v &= keep;
-                        e[j].l.v &= keep;
+                    for (int j = 0; j < B; j += 2) {
+                        const df2::x2 d = delta2(j);
+                        const df::f2x d0 = df2::lane0(d), d1 = df2::lane1(d);
+                        e[j] = df2::exp_df(df2::mul(df2::pack(d0, d0), kk), tab);
+                        e[j + 1] = df2::exp_df(df2::mul(df2::pack(d1, d1), kk), tab);
+                        const uint64_t keep0 = (j < nv) ? ~0ull : 0ull, keep1 = (j + 1 < nv) ? ~0ull : 0ull;
+                        e[j].h.v &= keep0;
+                        e[j].l.v &= keep0;
+                        e[j + 1].h.v &= keep1;
+                        e[j + 1].l.v &= keep1;
                     }
 #pragma unroll
-                    for (int j = 0; j < 8; j++) {
+                    for (int j = 0; j < B; j++) {
                         s1.add(df2::lane0(e[j]));
                         s2.add(df2::lane1(e[j]));
                     }
                 } else {
-                    df2::x2 e[4];
+                    df2::x2 e[B / 2];
 #pragma unroll
-                    for (int j = 0; j < 8; j += 2) {
-                        e[j / 2] = df2::exp_df(df2::mul(df2::pack(delta(j), delta(j + 1)), kk), tab);
+                    for (int j = 0; j < B; j += 2) {
+                        e[j / 2] = df2::exp_df(df2::mul(delta2(j), kk), tab);
                         const uint64_t keep =
                             ((j < nv) ? 0x00000000FFFFFFFFull : 0ull) | ((j + 1 < nv) ? 0xFFFFFFFF00000000ull : 0ull);
                         e[j / 2].h.v &= keep;
                         e[j / 2].l.v &= keep;
                     }
 #pragma unroll
-                    for (int j = 0; j < 4; j++) {
+                    for (int j = 0; j < B / 2; j++) {
                         s1.add(df2::lane0(e[j]));
                         s1.add(df2::lane1(e[j]));
                     }
@@ -870,21 +879,24 @@ __global__ void __launch_bounds__(X2_THREADS, 1)
                 const df2::x2 kc2 = df2::pack(kc, kc), nls2 = df2::pack(nls, nls);
                 // two centres at a time in the two lanes; all eight exponentials
                 // first, in one basic block (the guards act on the results)
-                df::f2x dI[8];
+                df2::x2 dI[4];  // centres c and c + 1 in the two lanes
                 df2::x2 e4[4];
 #pragma unroll
-                for (int cc = 0; cc < 8; cc++) {
+                for (int c = 0; c < 8; c += 2) {
+                    auto pair = [&](int i) { return df2::f2_pack(fu(va[i]), fu(va[i + 1])); };
                     // slices side by side: the even one is stored times 256, so
                     // each pair is an exact FP32 sum
-                    const float a01 = fu(va[cc]) + fu(va[8 + cc]);
-                    const float a23 = fu(va[16 + cc]) + fu(va[24 + cc]);
-                    const float a45 = fu(va[32 + cc]) + fu(va[40 + cc]);
-                    dI[cc] = df::sum4(fmaf(a01, 0x1p40f, -R0), fmaf(a23, 0x1p24f, -R1), fmaf(a45, 256.f, -R2),
-                                      fu(va[48 + cc]) - rq.w);
+                    const df2::f2 a01 = df2::f2_add(pair(c), pair(8 + c));
+                    const df2::f2 a23 = df2::f2_add(pair(16 + c), pair(24 + c));
+                    const df2::f2 a45 = df2::f2_add(pair(32 + c), pair(40 + c));
+                    dI[c / 2] = df2::sum4(df2::fma2(a01, df2::splat(0x1p40f), df2::splat(-R0)),
+                                          df2::fma2(a23, df2::splat(0x1p24f), df2::splat(-R1)),
+                                          df2::fma2(a45, df2::splat(256.f), df2::splat(-R2)),
+                                          df2::f2_sub(pair(48 + c), df2::splat(rq.w)));
                 }
 #pragma unroll
                 for (int c = 0; c < 8; c += 2)
-                    e4[c / 2] = df2::exp_df(df2::add(df2::mul(df2::pack(dI[c], dI[c + 1]), kc2), nls2), tab);
+                    e4[c / 2] = df2::exp_df(df2::add(df2::mul(dI[c / 2], kc2), nls2), tab);
 #pragma unroll
                 for (int c = 0; c < 8; c += 2) {
                     const df2::x2 e = e4[c / 2];
@@ -895,7 +907,8 @@ __global__ void __launch_bounds__(X2_THREADS, 1)
                         const int k = kb * X2_NC + 8 * g + cc;
                         if (k < p.K) {
                             // R = 0 where the reference's exp(-beta d / 2) underflows
-                            if (flag == 0 && !(dI[cc].h < lq.w)) {
+                            const float dh = h ? df2::f2_hi(dI[c / 2].h) : df2::f2_lo(dI[c / 2].h);
+                            if (flag == 0 && !(dh < lq.w)) {
                                 df::fixed48_parts(h ? df2::lane1(e) : df2::lane0(e), tp, bt);
                             } else if (flag == 1) {
                                 // comm/mpicomm.c:382-389: R = 1/K

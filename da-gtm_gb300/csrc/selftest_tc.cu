@@ -58,6 +58,13 @@ __global__ void df2_check_kernel(int n, unsigned long long *mismatch)
         bad += !same_bits(df2::lane0(m), df::mul(a, b)) + !same_bits(df2::lane1(m), df::mul(b, a));
         const df2::x2 s = df2::add(df2::pack(a, b), df2::pack(b, a));
         bad += !same_bits(df2::lane0(s), df::add(a, b)) + !same_bits(df2::lane1(s), df::add(b, a));
+        // four FP32 values of mixed size and sign, as the slice differences are
+        const float u0 = a.h * 1048576.f, v0 = -b.h * 262144.f, w0 = a.l * 1073741824.f,
+                    z0 = (float) (int) (ub & 0xFFFFFu) - 524288.f;
+        const df2::x2 q = df2::sum4(df2::f2_pack(u0, v0), df2::f2_pack(v0, u0), df2::f2_pack(w0, z0),
+                                    df2::f2_pack(z0, w0));
+        bad += !same_bits(df2::lane0(q), df::sum4(u0, v0, w0, z0)) +
+               !same_bits(df2::lane1(q), df::sum4(v0, u0, z0, w0));
     }
     if (bad)
         atomicAdd(mismatch, bad);

@@ -315,6 +315,24 @@ __device__ __forceinline__ void tmem_ld8p(uint32_t taddr, uint32_t *r)
                  : "r"(taddr));
 }
 
+__device__ __forceinline__ void tmem_ld4p(uint32_t taddr, uint32_t *r)
+{
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(taddr));
+}
+
+// a batch of W consecutive columns: W = 4 or 8
+template <int W>
+__device__ __forceinline__ void tmem_ldp(uint32_t taddr, uint32_t *r)
+{
+    static_assert(W == 4 || W == 8, "batch width");
+    if constexpr (W == 8)
+        tmem_ld8p(taddr, r);
+    else
+        tmem_ld4p(taddr, r);
+}
+
 __device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 __device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t (&r)[16])

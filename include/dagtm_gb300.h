@@ -272,8 +272,9 @@ int dgtm_fe_forward_noalloc(const float *Y, const float *T, int N, int K, int D,
  * tensor-memory A x MN-major) on small integer matrices and writes the largest
  * absolute error against a host product to errs[0..2] (0 when correct).  With
  * nerrs >= 4, errs[3] is the number of lanes in which the packed (f32x2)
- * double-float exp, add and mul of the exact-slice FP64 form differ bitwise
- * from the scalar ones over 2^20 argument pairs (0 when correct).
+ * double-float exp, add, mul and four-term sum of the exact-slice FP64 form
+ * differ bitwise from the scalar ones over 2^20 argument pairs (0 when
+ * correct).
  * No reference counterpart (the reference has no GPU code).
  */
 int dgtm_selftest(double *errs, int nerrs);
