@@ -229,6 +229,16 @@ struct XSum {
         i += df::fixed48r(e, rem);
         r += rem;
     }
+    // adds a batch sum 0 <= E < 2^SH+1: df::fixed48r of E 2^-SH (exact
+    // scaling), so the integers step by 2^SH and the remainders are exact
+    template <int SH>
+    __device__ __forceinline__ void add_batch(df::f2x e)
+    {
+        float rem;
+        constexpr float inv = 1.0f / (float) (1 << SH);
+        i += df::fixed48r({e.h * inv, e.l * inv}, rem) << SH;
+        r += rem * (float) (1 << SH);
+    }
     __device__ __forceinline__ double value() const { return ldexp((double) i + (double) r, -48); }
     // s *= E <= 1 (rare: when a point's reference centre moves; FP64, 2^-53)
     __device__ __forceinline__ void scale(df::f2x e)
@@ -492,7 +502,11 @@ __global__ void __launch_bounds__(X1_THREADS, 1)
                 };
                 // straight-line code (one basic block, so the chains overlap);
                 // a padding centre's exponential is masked to 0, which adds
-                // nothing to the sums
+                // nothing to the sums.  The batch's terms (each at most 1 plus the FP32
+                // pre-scan's error) are summed as double-floats (relative error
+                // 3 2^-48 per add, no cancellation) and go to the fixed-point
+                // sums once.
+                constexpr int SH = (B == 8) ? 3 : 2;  // batch sums below 2^(SH + 1)
                 if (TWO) {
                     df2::x2 e[B];
 #pragma unroll
@@ -508,10 +522,12 @@ __global__ void __launch_bounds__(X1_THREADS, 1)
                         e[j + 1].l.v &= keep1;
                     }
 #pragma unroll
-                    for (int j = 0; j < B; j++) {
-                        s1.add(df2::lane0(e[j]));
-                        s2.add(df2::lane1(e[j]));
-                    }
+                    for (int w = 1; w < B; w *= 2)
+#pragma unroll
+                        for (int j = 0; j < B; j += 2 * w)
+                            e[j] = df2::add(e[j], e[j + w]);
+                    s1.add_batch<SH>(df2::lane0(e[0]));
+                    s2.add_batch<SH>(df2::lane1(e[0]));
                 } else {
                     df2::x2 e[B / 2];
 #pragma unroll
@@ -523,10 +539,11 @@ __global__ void __launch_bounds__(X1_THREADS, 1)
                         e[j / 2].l.v &= keep;
                     }
 #pragma unroll
-                    for (int j = 0; j < B / 2; j++) {
-                        s1.add(df2::lane0(e[j]));
-                        s1.add(df2::lane1(e[j]));
-                    }
+                    for (int w = 1; w < B / 2; w *= 2)
+#pragma unroll
+                        for (int j = 0; j < B / 2; j += 2 * w)
+                            e[j] = df2::add(e[j], e[j + w]);
+                    s1.add_batch<SH>(df::add(df2::lane0(e[0]), df2::lane1(e[0])));
                 }
             }
         }
