@@ -85,8 +85,8 @@ struct P1Params {
 
 // lowest j in block B (columns 32 B .. 32 B + 31) with v[j] == mx; the block
 // is known to hold mx.  Constant indices keep v in registers.
-template <int B>
-__device__ __forceinline__ int first_equal(const uint32_t (&v)[P1_BK], float mx)
+template <int B, int NV>
+__device__ __forceinline__ int first_equal(const uint32_t (&v)[NV], float mx)
 {
     int j0 = 32 * B + 31;
 #pragma unroll
@@ -106,7 +106,9 @@ constexpr int P1_ACC_COL = 256;
 // (data exact in BF16): each tile owns one accumulator and the two tiles
 // ping-pong, so the tensor pipe works on one tile while the statistics warps
 // read the other.  NTILE = 1 (data split in two BF16 pieces): one tile
-// double-buffers the two accumulators.
+// double-buffers the two accumulators, and both statistics warp groups read
+// each chunk, half the centres apiece, merging a point's two partial maxima
+// and sums at the end.
 //
 // The kernel is a template on the operand shape -- NP 64-deep panels, KL
 // 16-deep steps used in the last one, NT data pieces -- so that the MMA
@@ -153,7 +155,9 @@ __global__ void __launch_bounds__(P1_THREADS, 1)
         mbar_init(t_done, 1);
         for (int b = 0; b < 2; b++) {
             mbar_init(&acc_full[b], 1);
-            mbar_init(&acc_empty[b], 128);
+            // the statistics threads of the accumulator's tile: one group of
+            // 128, or both groups when a CTA holds a single tile
+            mbar_init(&acc_empty[b], NTILE == 2 ? 128 : 256);
         }
         mbar_init(drain, 1);
         fence_barrier_init();
@@ -286,15 +290,22 @@ __global__ void __launch_bounds__(P1_THREADS, 1)
             failed = 1;
     } else if (warp >= 2) {
         // ---------------- statistics: one 4-warp group per point tile ----------------
+        // With a single tile per CTA (data in two pieces) both groups serve
+        // it: group g takes columns 64 g .. 64 g + 63 of each chunk, and the
+        // two partial maxima and sums of a point are merged at the end.
+        constexpr int W = (NTILE == 2) ? P1_BK : P1_BK / 2;  // columns per thread and chunk
         const int q = warp & 3;
         const int g = (warp - 2) >> 2;
+        const int tile = (NTILE == 2) ? g : 0;
+        const int cofs = (NTILE == 2) ? 0 : W * g;
+        const bool owner = (NTILE == 2) || g == 0;  // writes the point's results
         const int row = q * 32 + lane;
         const uint32_t lane_base = tmem + ((uint32_t) (q * 32) << 16);
-        const int prow = g * P1_TILE + row;
+        const int prow = tile * P1_TILE + row;
         const int n = n0 + prow;
         double t1 = 0.0, t2 = 0.0;
         bool ok = true;
-        if (g < NTILE) {
+        {
             float m = -INFINITY;
             int kstar = 0;
             // shifted sums at temperature 1 and at `temp`, FP32 with Kahan
@@ -302,34 +313,39 @@ __global__ void __launch_bounds__(P1_THREADS, 1)
             // per-chunk update); the result carries ~2 ulp of FP32
             float s1 = 0.f, s2 = 0.f, k1 = 0.f, k2 = 0.f;
             for (int c = 0; c < p.nchunk; c++) {
-                const int rg = region(g, c);
+                const int rg = region(tile, c);
                 if (!mbar_wait(&acc_full[rg], ruse(c) & 1, p.status, 15)) {
                     ok = false;
                     break;
                 }
                 tc_fence_after();
-                // copy the whole chunk out and hand the accumulator back at
-                // once, so the next chunk's MMAs overlap this arithmetic
-                uint32_t v[P1_BK];
+                // copy this thread's columns out and hand the accumulator back
+                // at once, so the next chunk's MMAs overlap this arithmetic
+                uint32_t v[W];
                 {
-                    const uint32_t col = lane_base + (uint32_t) (P1_ACC_COL + rg * P1_BK);
-                    tmem_ld32p(col, v);
-                    tmem_ld32p(col + 32, v + 32);
-                    tmem_ld32p(col + 64, v + 64);
-                    tmem_ld32p(col + 96, v + 96);
+                    const uint32_t col = lane_base + (uint32_t) (P1_ACC_COL + rg * P1_BK + cofs);
+#pragma unroll
+                    for (int u = 0; u < W / 32; u++)
+                        tmem_ld32p(col + 32 * u, v + 32 * u);
                     tmem_ld_wait();
                 }
                 tc_fence_before();
                 mbar_arrive(&acc_empty[rg]);
-                // maxima of the four 32-column blocks (four independent chains)
-                float mxq[4] = {-INFINITY, -INFINITY, -INFINITY, -INFINITY};
+                // maxima of the 32-column blocks (independent chains)
+                float mxq[W / 32];
+#pragma unroll
+                for (int u = 0; u < W / 32; u++)
+                    mxq[u] = -INFINITY;
 #pragma unroll
                 for (int j = 0; j < 32; j += 2) {
 #pragma unroll
-                    for (int u = 0; u < 4; u++)
+                    for (int u = 0; u < W / 32; u++)
                         mxq[u] = fmax3(mxq[u], __uint_as_float(v[32 * u + j]), __uint_as_float(v[32 * u + j + 1]));
                 }
-                const float mx = fmaxf(fmaxf(mxq[0], mxq[1]), fmaxf(mxq[2], mxq[3]));
+                float mx = mxq[0];
+#pragma unroll
+                for (int u = 1; u < W / 32; u++)
+                    mx = fmaxf(mx, mxq[u]);
                 if (mx > m) {
                     if (m > -INFINITY) {
                         const float f1 = ex2((m - mx) * p.c1l), f2 = ex2((m - mx) * p.c2l);
@@ -343,14 +359,14 @@ __global__ void __launch_bounds__(P1_THREADS, 1)
                     int j0;
                     if (mxq[0] == mx)
                         j0 = first_equal<0>(v, mx);
-                    else if (mxq[1] == mx)
+                    else if (W == 64 || mxq[1] == mx)
                         j0 = first_equal<1>(v, mx);
-                    else if (mxq[2] == mx)
-                        j0 = first_equal<2>(v, mx);
+                    else if (mxq[2 % (W / 32)] == mx)
+                        j0 = first_equal<2 % (W / 32)>(v, mx);
                     else
-                        j0 = first_equal<3>(v, mx);
+                        j0 = first_equal<3 % (W / 32)>(v, mx);
                     m = mx;
-                    kstar = c * P1_BK + j0;
+                    kstar = c * P1_BK + cofs + j0;
                 }
                 // four independent accumulation chains per sum (element j goes
                 // to chain j % 4), as two packed pairs: (0, 1) and (2, 3)
@@ -361,7 +377,7 @@ __global__ void __launch_bounds__(P1_THREADS, 1)
                     if (p.two_temps) {
                         const f2 k2 = f2_pack(p.c2l, p.c2l);
 #pragma unroll
-                        for (int j = 0; j < P1_BK; j += 4) {
+                        for (int j = 0; j < W; j += 4) {
                             const f2 xa = f2_sub(f2_pack(__uint_as_float(v[j]), __uint_as_float(v[j + 1])), mm);
                             const f2 xb = f2_sub(f2_pack(__uint_as_float(v[j + 2]), __uint_as_float(v[j + 3])), mm);
                             a1 = f2_add(a1, f2_ex2(f2_mul(xa, k1)));
@@ -371,7 +387,7 @@ __global__ void __launch_bounds__(P1_THREADS, 1)
                         }
                     } else {
 #pragma unroll
-                        for (int j = 0; j < P1_BK; j += 4) {
+                        for (int j = 0; j < W; j += 4) {
                             const f2 xa = f2_sub(f2_pack(__uint_as_float(v[j]), __uint_as_float(v[j + 1])), mm);
                             const f2 xb = f2_sub(f2_pack(__uint_as_float(v[j + 2]), __uint_as_float(v[j + 3])), mm);
                             a1 = f2_add(a1, f2_ex2(f2_mul(xa, k1)));
@@ -398,6 +414,37 @@ __global__ void __launch_bounds__(P1_THREADS, 1)
                     s2 = u2;
                 }
             }
+            if (NTILE == 1) {
+                // group 1 hands its partial maximum, index and compensated sums
+                // to group 0 through shared memory (the red array, written with
+                // the per-point terms only after the second barrier)
+                float *xm = (float *) red;  // [4][128]: m, s1 - k1, s2 - k2, kstar
+                if (g == 1) {
+                    xm[row] = m;
+                    xm[128 + row] = s1 - k1;
+                    xm[256 + row] = s2 - k2;
+                    xm[384 + row] = __int_as_float(kstar);
+                }
+                asm volatile("bar.sync 1, 256;" ::: "memory");
+                if (g == 0) {
+                    const float mb = xm[row], sb1 = xm[128 + row], sb2 = xm[256 + row];
+                    const int kb = __float_as_int(xm[384 + row]);
+                    const float mn = fmaxf(m, mb);
+                    if (mn > -INFINITY) {
+                        const float fa1 = ex2((m - mn) * p.c1l), fb1 = ex2((mb - mn) * p.c1l);
+                        const float fa2 = ex2((m - mn) * p.c2l), fb2 = ex2((mb - mn) * p.c2l);
+                        s1 = fmaf(s1 - k1, fa1, sb1 * fb1);
+                        s2 = fmaf(s2 - k2, fa2, sb2 * fb2);
+                        k1 = 0.f;
+                        k2 = 0.f;
+                    }
+                    // the lowest index among equal maxima
+                    if (mb > m || (mb == m && kb < kstar))
+                        kstar = kb;
+                    m = mn;
+                }
+                asm volatile("bar.sync 1, 256;" ::: "memory");
+            }
             if (!p.two_temps) {
                 s2 = s1;
                 k2 = k1;
@@ -407,7 +454,9 @@ __global__ void __launch_bounds__(P1_THREADS, 1)
             // row is read back from tensor memory (the A operand, warp-
             // collective, so outside the per-point branch), 64 dimensions per
             // batch of centre loads.
-            const bool active = ok && n < p.N;
+            // only the owning group writes a point's results (group 1 of a
+            // single-tile CTA holds unmerged partials)
+            const bool active = owner && ok && n < p.N;
             const int kb = min(kstar, p.K - 1);
             const float *yk = p.Y32 + (size_t) kb * p.D;
             float dsum = 0.f;
@@ -487,7 +536,7 @@ __global__ void __launch_bounds__(P1_THREADS, 1)
                 }
                 p.colstat[n] = make_double2(dstar, lsn);
                 p.colq[n] = cq;
-            } else if (n < p.Npad) {
+            } else if (owner && n < p.Npad) {
                 p.colq[n] = make_float4(0.f, 0.f, INFINITY, 0.f);  // padding: R = 0
             }
             if (!ok)
