@@ -139,9 +139,9 @@ constexpr float EXP_INV = (float) (64.0 / 0.69314718055994530942);
 // 1/6 as a double-float
 constexpr float SIXTH_H = (float) (1.0 / 6.0);
 constexpr float SIXTH_L = (float) (1.0 / 6.0 - (double) SIXTH_H);
-// below this argument exp(x) < 2^-64: the per-point sums (2^-63 resolution)
-// and the responsibilities (2^-48) take it as 0; K such terms change a sum
-// of at least 1 by less than 2^-48 for K < 2^16
+// below this argument exp(x) < 2^-64: the per-point sums and the
+// responsibilities (2^-48 fixed point) take it as 0; K such terms change a
+// sum of at least 1 by less than 2^-48 for K < 2^16
 constexpr float EXP_CUT = -45.0f;
 
 // The table 2^(j/64), j = 0..63, as double-floats (tab[j] = {hi, lo}).
@@ -248,47 +248,6 @@ DF_HD uint64_t fixed48r(f2x e, float &rem)
     const float bf = rintf(scaled);
     rem = fmaf(fe, 16777216.0f, sub_rn(scaled, bf));
     return ((uint64_t) top << 24) + (uint64_t) (uint32_t) bf;
-}
-
-// round(v 2^63) for an FP32 |v| < 2, from its bits (exact for |v| >= 2^-40;
-// below 2^-126 it is 0)
-DF_HD int64_t scaled63(float v)
-{
-    uint32_t b;
-#if defined(__CUDA_ARCH__)
-    b = __float_as_uint(v);
-#else
-    memcpy(&b, &v, 4);
-#endif
-    const int ex = (int) ((b >> 23) & 255u);
-    if (ex == 0)
-        return 0;
-    const uint64_t m = (uint64_t) ((b & 0x7FFFFFu) | 0x800000u);
-    const int sh = ex - 87;  // v = m 2^(ex - 150), v 2^63 = m 2^(ex - 87)
-    uint64_t r;
-    if (sh >= 0)
-        r = m << sh;
-    else if (sh > -40)
-        r = (m + (1ull << (-sh - 1))) >> (-sh);
-    else
-        r = 0;
-    return (b >> 31) ? -(int64_t) r : (int64_t) r;
-}
-
-// round(E 2^63) for 0 <= E < 2 (E a normalised double-float), modulo 2^64
-// (the low part's two's complement wraps back)
-DF_HD uint64_t fixed63(f2x e) { return (uint64_t) scaled63(e.h) + (uint64_t) scaled63(e.l); }
-
-// a 128-bit fixed-point sum at 2^-63: (hi, lo) += v
-DF_HD void acc128(uint64_t &hi, uint64_t &lo, uint64_t v)
-{
-    lo += v;
-    hi += (lo < v) ? 1u : 0u;
-}
-
-DF_HD double acc128_value(uint64_t hi, uint64_t lo)
-{
-    return (double) hi * 2.0 + ldexp((double) lo, -63);
 }
 
 }  // namespace df

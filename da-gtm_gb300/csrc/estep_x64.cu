@@ -223,13 +223,7 @@ struct X1Params {
 struct XSum {
     unsigned long long i = 0ull;
     float r = 0.f;
-    __device__ __forceinline__ void add(df::f2x e)
-    {
-        float rem;
-        i += df::fixed48r(e, rem);
-        r += rem;
-    }
-    // adds a batch sum 0 <= E < 2^SH+1: df::fixed48r of E 2^-SH (exact
+    // adds a batch sum 0 <= E < 2^(SH + 1): df::fixed48r of E 2^-SH (exact
     // scaling), so the integers step by 2^SH and the remainders are exact
     template <int SH>
     __device__ __forceinline__ void add_batch(df::f2x e)

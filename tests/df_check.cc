@@ -130,26 +130,6 @@ int main()
     }
     printf("fixed48 max_abs_units %.3Lf\n", fmax);
 
-    // fixed63: round(E 2^63) for E in [0, 2) modulo 2^64, within one unit,
-    // and a 128-bit sum of many terms against the long-double sum
-    long double gmax = 0.0L;
-    uint64_t hi = 0, lo = 0;
-    long double ssum = 0.0L;
-    for (int i = 0; i < n; i++) {
-        const double ed = (i % 3 == 0) ? uniform() * 1.9 : (i % 3 == 1) ? ldexp(uniform(), -(int) (next_u64() % 60))
-                                                              : 1.0 - uniform() * 1e-9;
-        const f2x e = from_double(ed);
-        const uint64_t f = fixed63(e);
-        const long double ref = ldexpl(ld(e), 63);
-        const unsigned __int128 r = (unsigned __int128) (ref + 0.5L);
-        const long double err = fabsl((long double) (__int128) ((unsigned __int128) f - (uint64_t) r));
-        if (err > gmax)
-            gmax = err;
-        acc128(hi, lo, f);
-        ssum += ld(e);
-    }
-    printf("fixed63 max_abs_units %.3Lf\n", gmax);
-
     // fixed48r: the integers plus the FP32 sum of remainders against the
     // long-double sum of 60000 terms below 1 (the largest K), several times
     long double rmax = 0.0L;
@@ -171,6 +151,5 @@ int main()
             rmax = relr;
     }
     printf("fixed48r sum_rel %.3Le\n", rmax);
-    printf("acc128 sum_rel %.3Le\n", fabsl((long double) acc128_value(hi, lo) - ssum) / ssum);
     return 0;
 }

@@ -8,8 +8,6 @@ checked against long-double and exact integer results (tests/df_check.cc):
   cancellation: relative error below 1e-14 of the exact integer;
 * mul: below 2e-14;
 * fixed48, round(E 2^48) for 0 <= E < 2: within one unit;
-* fixed63 (round(E 2^63) modulo 2^64) within one unit, and the 128-bit sum
-  of 2M such terms within 1e-15 of the long-double sum;
 * fixed48r: 60000 terms summed as 2^-48 integers plus an FP32 sum of the
   exact rounding remainders, within 1e-16 of the long-double sum (the form's
   per-point sums over K centres).
@@ -53,11 +51,6 @@ def test_mul(df_check):
 
 def test_fixed_point(df_check):
     assert value(df_check, "fixed48 max_abs_units") <= 1.0
-
-
-def test_fixed_point_63_and_128_bit_sum(df_check):
-    assert value(df_check, "fixed63 max_abs_units") <= 1.0
-    assert value(df_check, "acc128 sum_rel") <= 1e-15
 
 
 def test_fixed_point_48_with_remainders(df_check):
