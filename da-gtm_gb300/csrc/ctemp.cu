@@ -20,11 +20,12 @@
 //                     triangle), 4 x 4 entries of S1 and of S2 per thread,
 //                     added over the chunk's points in a fixed order and into
 //                     the running sums of the earlier chunks
-//   eig_kernel      : one CTA per (centre, block); parallel cyclic Jacobi
-//                     (round-robin pairing) on the D x D block, then the filter
+//   eig_kernel      : one CTA per (centre, block); Householder reduction of
+//                     the D x D block to tridiagonal form, then the largest
+//                     eigenvalue below the limit by Sturm-count bisection
 // Arithmetic type F: FP64 for the FP64 form.  The FP32 and split forms form
 // x and the products in FP32 (partial sums over 128 points go into FP64) and
-// run the Jacobi sweeps in FP32: their stated error is 1e-4, and GB300's FP32
+// reduce and bisect in FP32: their stated error is 1e-4, and GB300's FP32
 // pipe is about 64 times its FP64 pipe.
 #include "common.cuh"
 #include "kernels.cuh"
@@ -41,9 +42,8 @@ constexpr int SC_THREADS = 256;  // 16 x 16 threads, 4 x 4 entries each
 constexpr int SC_TILE = 64;      // output tile (rows x cols of S)
 constexpr int SC_PTS = 32;       // points per staged sub-chunk
 constexpr int SC_FLUSH = 4;      // FP32 partial sums go into FP64 every 4 sub-chunks
-// threads of the eigen kernel: 256 for small matrices (several blocks per SM);
-// above that 1024 (FP64, the matrix fills shared memory: one block per SM) or
-// 512 (FP32: two blocks per SM)
+// threads of the eigen kernel: 256 for small matrices (several blocks per SM),
+// 512 above that
 constexpr int EIG_SMALL_D = 96;
 // largest dynamic shared memory a block may opt into on sm_10x (227 KB), less
 // room for the kernel's static arrays
@@ -175,25 +175,78 @@ __global__ void __launch_bounds__(SC_THREADS, 2) scatter_kernel(
 template <typename F>
 size_t eig_smem_bytes(int D)
 {
-    const size_t npair = (size_t) (D + 1) / 2;
-    return sizeof(F) * ((size_t) D * D + 2 * npair) + sizeof(int) * 2 * npair;
+    // the matrix, then the Householder vector, M v (then w), the diagonal,
+    // the off-diagonal and 32 + 2 reduction slots
+    return sizeof(F) * ((size_t) D * D + 4 * (size_t) D + 34);
 }
 
-// blockIdx.x = centre in the batch, blockIdx.y = 0: 2 S1, 1: 2 (S1 - S2)
+template <typename F>
+__device__ __forceinline__ F warp_sum(F a)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        a += __shfl_xor_sync(0xffffffffu, a, o);
+    return a;
+}
+
+// sum over the block (every thread gets it); red: NT / 32 slots
+template <int NT, typename F>
+__device__ __forceinline__ F block_sum(F a, F *red)
+{
+    a = warp_sum(a);
+    if ((threadIdx.x & 31) == 0)
+        red[threadIdx.x >> 5] = a;
+    __syncthreads();
+    F s = F(0);
+#pragma unroll
+    for (int w = 0; w < NT / 32; w++)
+        s += red[w];
+    __syncthreads();
+    return s;
+}
+
+// number of eigenvalues below x of the symmetric tridiagonal matrix with
+// diagonal dg and squared off-diagonal od2 (Sturm sequence count; a zero pivot
+// is replaced by -pivmin)
+template <typename F>
+__device__ int count_below(const F *dg, const F *od2, int D, F x, F pivmin)
+{
+    int c = 0;
+    F q = dg[0] - x;
+    if (fabs(q) < pivmin)
+        q = -pivmin;
+    c += q < F(0);
+    for (int i = 1; i < D; i++) {
+        q = (dg[i] - x) - od2[i - 1] / q;
+        if (fabs(q) < pivmin)
+            q = -pivmin;
+        c += q < F(0);
+    }
+    return c;
+}
+
+// blockIdx.x = centre in the batch, blockIdx.y = 0: 2 S1, 1: 2 (S1 - S2).
+// Only the largest eigenvalue below the limit is wanted, so instead of a full
+// eigendecomposition the block is reduced to tridiagonal form by Householder
+// reflections (Golub and Van Loan, Matrix Computations, algorithm 8.3.1: the
+// reduction gsl_eigen_symm starts with too), and that eigenvalue is found by
+// bisection on the Sturm sequence count (32-point multisection in one warp).
 template <int EIG_THREADS, typename F>
 __global__ void __launch_bounds__(EIG_THREADS) eig_kernel(const double *__restrict__ S, int D,
                                                           int in_smem, F *__restrict__ Mg,
                                                           const double *__restrict__ gg,
                                                           double lim_scale, double *__restrict__ out)
 {
+    constexpr int NW = EIG_THREADS / 32;
     extern __shared__ __align__(16) unsigned char sh_raw[];
     F *sh = reinterpret_cast<F *>(sh_raw);
     const int kl = blockIdx.x, which = blockIdx.y;
-    const int npair = (D + 1) / 2, nslot = 2 * npair;  // slot D (odd D) is a dummy
     F *M = in_smem ? sh : Mg + ((size_t) kl * 2 + which) * D * D;
-    F *cs = in_smem ? sh + (size_t) D * D : sh;
-    F *sn = cs + npair;
-    int *pp = (int *) (sn + npair), *qq = pp + npair;
+    F *v = in_smem ? sh + (size_t) D * D : sh;  // Householder vector
+    F *p = v + D;                                // tau M v, then w
+    F *dg = p + D;                               // diagonal
+    F *od = dg + D;                              // off-diagonal, then its squares
+    F *red = od + D;                             // reduction slots
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const double *S1 = S + (size_t) kl * 2 * D * D, *S2 = S1 + (size_t) D * D;
     const double gk = gg[kl];
@@ -204,8 +257,8 @@ __global__ void __launch_bounds__(EIG_THREADS) eig_kernel(const double *__restri
         return;
     }
     // gg < GG_MIN: the reference scales H by 1 / GG_MIN before gsl_eigen_symm
-    // and the eigenvalues back.  The FP32 sweeps take H / gg (1e250 is outside
-    // FP32) and multiply the eigenvalues by gg.
+    // and the eigenvalues back.  The FP32 arithmetic takes H / gg (1e250 is
+    // outside FP32) and multiplies the eigenvalues by gg.
     double sc = 1.0, back = 1.0;
     if (sizeof(F) == 8) {
         if (gk < GG_MIN)
@@ -219,82 +272,121 @@ __global__ void __launch_bounds__(EIG_THREADS) eig_kernel(const double *__restri
         M[e] = (F) ((which == 0 ? 2.0 * S1[at] : 2.0 * (S1[at] - S2[at])) * sc);
     }
     __syncthreads();
-    // A rotation is skipped when |a_pq| <= eps sqrt|a_pp a_qq| (the threshold
-    // of Demmel and Veselic's Jacobi, SIAM J. Matrix Anal. Appl. 13, 1992);
-    // the sweeps end when one rotates nothing.
-    const F eps = sizeof(F) == 8 ? (F) DBL_EPSILON : (F) FLT_EPSILON;
-    for (int sweep = 0; sweep < 100; sweep++) {
-        int rotated = 0;
-        for (int step = 0; step < nslot - 1; step++) {
-            for (int t = threadIdx.x; t < npair; t += EIG_THREADS) {
-                // round-robin pairing: slot 0 fixed, the others rotate
-                const int a = (t == 0) ? 0 : 1 + ((t - 1 + step) % (nslot - 1));
-                const int b = 1 + ((nslot - 2 - t + step) % (nslot - 1));
-                const int p = min(a, b), q = max(a, b);
-                F cc = F(1), ss = F(0);
-                if (q < D) {
-                    const F apq = M[(size_t) p * D + q];
-                    const F app = M[(size_t) p * D + p], aqq = M[(size_t) q * D + q];
-                    if (fabs(apq) > eps * (sqrt(fabs(app)) * sqrt(fabs(aqq)))) {
-                        const F th = (aqq - app) / (F(2) * apq);
-                        const F tn = (th >= F(0) ? F(1) : F(-1)) / (fabs(th) + sqrt(th * th + F(1)));
-                        cc = F(1) / sqrt(tn * tn + F(1));
-                        ss = tn * cc;
-                        rotated |= (ss != F(0));  // 0 when th * th overflows
-                    }
-                }
-                pp[t] = p;
-                qq[t] = q;
-                cs[t] = cc;
-                sn[t] = ss;
-            }
-            __syncthreads();
-            // rows p and q of every rotation, one warp per pair
-            for (int t = warp; t < npair; t += EIG_THREADS / 32) {
-                const F ct = cs[t], st = sn[t];
-                const int p = pp[t], q = qq[t];
-                if (q >= D || st == F(0))
-                    continue;
-                F *rp = M + (size_t) p * D, *rq = M + (size_t) q * D;
-                for (int j = lane; j < D; j += 32) {
-                    const F mp = rp[j], mq = rq[j];
-                    rp[j] = ct * mp - st * mq;
-                    rq[j] = st * mp + ct * mq;
-                }
-            }
-            __syncthreads();
-            // then columns p and q
-            for (int t = warp; t < npair; t += EIG_THREADS / 32) {
-                const F ct = cs[t], st = sn[t];
-                const int p = pp[t], q = qq[t];
-                if (q >= D || st == F(0))
-                    continue;
-                for (int j = lane; j < D; j += 32) {
-                    F *r = M + (size_t) j * D;
-                    const F mp = r[p], mq = r[q];
-                    r[p] = ct * mp - st * mq;
-                    r[q] = st * mp + ct * mq;
-                }
-            }
-            __syncthreads();
+    // column k: x = M[k + 1 .., k] (row k, by symmetry) goes to alpha e_1 by
+    // H = I - tau v v^T, v = x - alpha e_1, alpha = -sign(x_0) |x|; the
+    // trailing block A becomes H A H = A - v w^T - w v^T, p = tau A v,
+    // w = p - (tau / 2)(p^T v) v
+    for (int k = 0; k + 2 < D; k++) {
+        const int m = D - k - 1;
+        const F *x = M + (size_t) k * D + k + 1;
+        F part = F(0);
+        for (int i = 1 + threadIdx.x; i < m; i += EIG_THREADS)
+            part += x[i] * x[i];
+        const F sigma = block_sum<EIG_THREADS>(part, red);
+        const F x0 = x[0];
+        if (threadIdx.x == 0)
+            dg[k] = M[(size_t) k * D + k];
+        if (sigma == F(0)) {  // the column is already reduced (the same in every thread)
+            if (threadIdx.x == 0)
+                od[k] = x0;
+            continue;
         }
-        if (!__syncthreads_or(rotated))
-            break;
+        const F mu = sqrt(x0 * x0 + sigma);
+        const F alpha = x0 <= F(0) ? mu : -mu;
+        const F v0 = x0 - alpha;  // |v0| = |x0| + mu: no cancellation
+        const F tau = F(2) / (v0 * v0 + sigma);
+        if (!isfinite(tau)) {  // |x| underflows: the column counts as reduced
+            if (threadIdx.x == 0)
+                od[k] = x0;
+            continue;
+        }
+        for (int i = threadIdx.x; i < m; i += EIG_THREADS)
+            v[i] = i == 0 ? v0 : x[i];
+        if (threadIdx.x == 0)
+            od[k] = alpha;
+        __syncthreads();
+        F *A = M + (size_t) (k + 1) * D + (k + 1);
+        for (int i = warp; i < m; i += NW) {
+            const F *ri = A + (size_t) i * D;
+            F acc = F(0);
+            for (int j = lane; j < m; j += 32)
+                acc += ri[j] * v[j];
+            acc = warp_sum(acc);
+            if (lane == 0)
+                p[i] = tau * acc;
+        }
+        __syncthreads();
+        part = F(0);
+        for (int i = threadIdx.x; i < m; i += EIG_THREADS)
+            part += p[i] * v[i];
+        const F half_k = F(0.5) * tau * block_sum<EIG_THREADS>(part, red);
+        for (int i = threadIdx.x; i < m; i += EIG_THREADS)
+            p[i] -= half_k * v[i];
+        __syncthreads();
+        for (int i = warp; i < m; i += NW) {
+            F *ri = A + (size_t) i * D;
+            const F vi = v[i], wi = p[i];
+            for (int j = lane; j < m; j += 32)
+                ri[j] -= vi * p[j] + wi * v[j];
+        }
+        __syncthreads();
     }
     if (threadIdx.x == 0) {
-        // eigenvalues at or above the limit count as 0, then the largest
-        const double limit = lim_scale * gk;
-        double mx = -INFINITY;
-        for (int i = 0; i < D; i++) {
-            double l = (double) M[(size_t) i * D + i];
-            if (back != 1.0)
-                l *= back;
-            if (l >= limit)
-                l = 0.0;
-            mx = fmax(mx, l);
+        if (D >= 2) {
+            dg[D - 2] = M[(size_t) (D - 2) * D + (D - 2)];
+            od[D - 2] = M[(size_t) (D - 2) * D + (D - 1)];
         }
-        out[(size_t) kl * 2 + which] = mx;
+        dg[D - 1] = M[(size_t) (D - 1) * D + (D - 1)];
     }
+    __syncthreads();
+    if (warp != 0)
+        return;
+    // Gershgorin bounds and the pivot floor (od becomes od^2)
+    F lo = F(INFINITY), hi = F(-INFINITY), emax = F(0);
+    for (int i = lane; i < D; i += 32) {
+        const F el = i > 0 ? fabs(od[i - 1]) : F(0), er = i + 1 < D ? fabs(od[i]) : F(0);
+        lo = fmin(lo, dg[i] - el - er);
+        hi = fmax(hi, dg[i] + el + er);
+        emax = fmax(emax, er);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+        emax = fmax(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+    }
+    __syncwarp();
+    for (int i = lane; i + 1 < D; i += 32)
+        od[i] = od[i] * od[i];
+    __syncwarp();
+    const F tiny = sizeof(F) == 8 ? (F) DBL_MIN : (F) FLT_MIN;
+    const F epsf = sizeof(F) == 8 ? (F) DBL_EPSILON : (F) FLT_EPSILON;
+    const F pivmin = tiny * fmax(F(1), emax * emax);
+    const double limit = lim_scale * gk;
+    const F lim_s = (F) (limit / back);
+    // eigenvalues at or above the limit count as 0, then the largest
+    const int c = count_below(dg, od, D, lim_s, pivmin);
+    double mx = 0.0;
+    if (c > 0) {
+        // the c-th smallest eigenvalue lies in [lo, min(hi, lim_s)]
+        const F pad = epsf * fmax(fabs(lo), fabs(hi)) + pivmin;
+        lo -= pad;
+        hi = fmin(hi + pad, lim_s);
+        for (int it = 0; it < 64 && hi - lo > F(2) * epsf * fmax(fabs(lo), fabs(hi)) + pivmin; it++) {
+            const F xl = lo + (hi - lo) * (F) (lane + 1) / F(33);
+            const unsigned up = __ballot_sync(0xffffffffu, count_below(dg, od, D, xl, pivmin) >= c);
+            // the first point with at least c eigenvalues below it
+            const int f = up ? __ffs(up) - 1 : 32;
+            const F nlo = f == 0 ? lo : __shfl_sync(0xffffffffu, xl, f - 1 < 0 ? 0 : f - 1);
+            const F nhi = f == 32 ? hi : __shfl_sync(0xffffffffu, xl, f == 32 ? 0 : f);
+            lo = nlo;
+            hi = nhi;
+        }
+        const double lam = (double) (F(0.5) * (lo + hi)) * back;
+        mx = (c < D) ? fmax(lam, 0.0) : lam;
+    }
+    if (lane == 0)
+        out[(size_t) kl * 2 + which] = mx;
 }
 
 template <int NT, typename F>
@@ -352,8 +444,6 @@ int run_batch(const CtempPlan &pl, const double *T64, const float *T32, const do
     const double *gg = gg_dev ? gg_dev : gsum_dev;
     if (D <= EIG_SMALL_D)
         return launch_eig<256, F>(kb, D, pl.eig_in_smem, S, Mg, gg, lim_scale, out_dev, s);
-    if (sizeof(F) == 8)
-        return launch_eig<1024, F>(kb, D, pl.eig_in_smem, S, Mg, gg, lim_scale, out_dev, s);
     return launch_eig<512, F>(kb, D, pl.eig_in_smem, S, Mg, gg, lim_scale, out_dev, s);
 }
 
@@ -394,7 +484,7 @@ int launch_ctemp_eig(const CtempPlan &pl, int kb, int D, const double *S, void *
     double *M = static_cast<double *>(Mg);
     if (D <= EIG_SMALL_D)
         return launch_eig<256, double>(kb, D, pl.eig_in_smem, S, M, gg, lim_scale, out, s);
-    return launch_eig<1024, double>(kb, D, pl.eig_in_smem, S, M, gg, lim_scale, out, s);
+    return launch_eig<512, double>(kb, D, pl.eig_in_smem, S, M, gg, lim_scale, out, s);
 }
 
 namespace {
