@@ -6,8 +6,9 @@ the reference does; the library takes the two D x D diagonal blocks of H
 after the orthogonal block transform.  The same responsibilities go into both
 (the FP64 form reproduces the oracle's R to ~1e-12), so the critical
 temperatures agree to FP64 eigenvalue accuracy: 1e-9 relative.  The FP32 and
-split-BF16 forms form the scatter matrices and run the eigen sweeps in FP32,
-and the split form's R carries its stated error: 1e-4 relative.  On 0/1 data
+split-BF16 forms form the scatter matrices and find the eigenvalue in FP32
+(Householder reduction to tridiagonal form, Sturm bisection), and the split
+form's R carries its stated error: 1e-4 relative.  On 0/1 data
 the split form forms the scatter as a tensor-core GEMM over pair features
 (R and R^2 against u_n = (t_i t_j, t_i, 1)); DGTM_CTEMP_PAIRS=0 selects the
 CUDA-core scatter instead, and the two agree centre by centre to 1e-4.
@@ -51,9 +52,12 @@ def oracle_ctemp(orc, T, Y, beta, temp, eps, gg=None):
     ("binary", 400, 166, 9, "fp64", 1e-9),   # D x D block just inside shared memory
     ("real", 300, 170, 9, "fp64", 1e-9),     # D x D block beyond shared memory
     ("binary", 600, 20, 64, "bf16x3", 1e-4),
-    ("binary", 400, 166, 9, "bf16x3", 1e-4),  # FP32 sweeps, 512 threads
+    ("binary", 400, 166, 9, "bf16x3", 1e-4),  # FP32 eigenvalues, 512 threads
     ("real", 500, 13, 49, "fp32", 1e-4),
     ("real", 300, 250, 4, "fp32", 1e-4),      # FP32 block beyond shared memory
+    ("real", 300, 1, 9, "fp64", 1e-9),        # 1 x 1 blocks: no reduction step
+    ("real", 300, 2, 9, "fp64", 1e-9),        # 2 x 2: the last pair only
+    ("real", 300, 3, 9, "fp32", 1e-4),        # one reflection
 ])
 def test_next_ctemp_matches_oracle(pkg, orc, kind, N, D, K, form, tol):
     T, FI, Y = problem(pkg, kind, N, D, K)
