@@ -508,7 +508,7 @@ int dgtm_mstep(dgtm_ctx *ctx, double *W, int ldW, double *Y, int ldY, double *be
     const double c = ctx->isDA ? ctx->beta / (2.0 * ctx->temp) : ctx->beta / 2.0;
     // kernels of the solve phase: form_ab (2), the solver (Cholesky and the
     // substitution, or one eigen kernel), update_y, the beta sum, the reduction
-    int npass = 1, nsmall = 4 + ((ctx->solver == DGTM_SOLVE_SVD) ? 1 : 2);
+    int npass = 1, nsmall = 4 + solve_launches(M1, ctx->solver);
     DGTM_TRY(phase_begin(ctx, DGTM_PHASE_MSTEP_PASS));
     if (ctx->x64) {
         DGTM_TRY(x64_mstep_pass(ctx->x64, c, ctx->G, ctx->RT, ctx->stream, &npass));  // cut: pass 1

@@ -71,6 +71,8 @@ int launch_form_ab(const double *FI, const double *G, const double *RT, int K, i
                    int D, double *A, double *B, double *scratch, cudaStream_t s);
 // W = A^{-1} B by Cholesky (solver 0) or symmetric-eigen pseudo-inverse (solver 1).
 // work: M1*M1 + M1 doubles (+ M1*M1 for solver 1).  flag[0] != 0 on failure.
+// kernel launches of one launch_solve
+int solve_launches(int M1, int solver);
 int launch_solve(const double *A, const double *B, int M1, int D, int solver, double *W,
                  double *work, int *flag, cudaStream_t s);
 // Copies of the centres that the E-step of a form reads, written by

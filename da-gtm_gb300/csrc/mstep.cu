@@ -207,22 +207,13 @@ __device__ __forceinline__ double rsqrt_nr(double d)
     return r;
 }
 
-// Right-looking Cholesky in one block for M1 > SMEM_SOLVE_MAX (L factorised in
-// place in global memory), one barrier per column.  Thread t
-// owns rows i = t/4, t/4 + 64, ... and in each the columns k = t (mod 4).
-// Column j stays unscaled while it is in use: after the barrier of step j
-// every thread reads the pivot's reciprocal square root r_j, updates its
-// trailing elements as L[i][k] -= (a_ij r_j^2) a_kj (a: the unscaled column
-// j), and the scaled a_ij r_j goes to the unused upper triangle at [j][i].
-// The next pivot is the first element its owner updates in a step; the
-// owner takes its reciprocal square root and publishes it before its other
-// rows.  A last pass moves the scaled columns to the lower triangle.  A pivot
-// that keeps less than CHOL_DROP of its diagonal (the column adds no new
-// direction at FP64 precision) is dropped: its diagonal and column are stored
-// as 0 and that unknown is fixed at 0, which keeps the solve defined when
-// A = FI^T diag(G) FI is numerically singular (wide basis functions).
-// L (lower triangle) goes to work[0 .. M1*M1), the reciprocal diagonal to
-// work[M1*M1 .. M1*M1 + M1) (0 for a dropped pivot); flag[1] counts the drops.
+// Cholesky with pivot drops.  A pivot that keeps less than CHOL_DROP of its
+// diagonal (the column adds no new direction at FP64 precision) is dropped:
+// its diagonal and column are stored as 0 and that unknown is fixed at 0,
+// which keeps the solve defined when A = FI^T diag(G) FI is numerically
+// singular (wide basis functions).  L (lower triangle) goes to
+// work[0 .. M1*M1), the reciprocal diagonal to work[M1*M1 .. M1*M1 + M1) (0
+// for a dropped pivot); flag[1] counts the drops.
 constexpr double CHOL_DROP = 1e-12;
 constexpr int CHOL_THREADS = 256;
 
@@ -245,59 +236,113 @@ __device__ __forceinline__ void chol_pivot(double *L, const double *adiag, int M
     rinv[j] = r;
 }
 
-__global__ void __launch_bounds__(CHOL_THREADS) cholesky_kernel(const double *__restrict__ A,
-                                                               int M1, double *__restrict__ work,
-                                                               int *flag)
+// Blocked right-looking Cholesky for M1 > SMEM_SOLVE_MAX, in panels of CHB
+// columns, so that the O(M1^3) part runs on the whole GPU: chol_panel_kernel
+// (one CTA) factorises a panel's columns one after the other over every row
+// below them, with chol_pivot's drop rule, and chol_update_kernel (one CTA per
+// 32 x 32 tile) subtracts the panel's L21 L21^T from the trailing lower
+// triangle.  The layout is that of the shared-memory kernel below: the
+// scaled L (L_ij = a_ij / sqrt(d_j)) in the lower
+// triangle of work, the reciprocal diagonal after it (0 for a dropped pivot),
+// flag[0] for a non-finite pivot and flag[1] counting the drops.
+constexpr int CHB = 32;
+constexpr int CHB_THREADS = 256;
+
+__global__ void __launch_bounds__(CHB_THREADS) chol_panel_kernel(const double *__restrict__ A,
+                                                                 int M1, int p0, int w,
+                                                                 double *__restrict__ work,
+                                                                 int *flag)
 {
-    // shared: the pivots' reciprocal square roots and A's diagonal (M1 each);
-    // L is factorised in place in work (M1 > SMEM_SOLVE_MAX)
-    extern __shared__ double sh[];
-    double *rinv = sh, *adiag = sh + M1;
     double *L = work;
+    double *rinv = work + (size_t) M1 * M1;
+    __shared__ double r_sh;
+    __shared__ double colj[CHB];  // the scaled column j in the panel's later rows
     __shared__ int bad, ndrop;
-    const int tid = threadIdx.x, q = tid & 3, r0 = tid >> 2;
-    const size_t n2 = (size_t) M1 * M1;
+    const int tid = threadIdx.x;
+    const int kend = p0 + w;
     if (tid == 0) {
         bad = 0;
         ndrop = 0;
     }
-#pragma unroll 4
-    for (size_t e = tid; e < n2; e += CHOL_THREADS)
-        L[e] = A[e];
-    for (int j = tid; j < M1; j += CHOL_THREADS)
-        adiag[j] = A[(size_t) j * M1 + j];
-    __syncthreads();
-    if (tid == 0)
-        chol_pivot(L, adiag, M1, 0, rinv, &bad, &ndrop);
-    for (int j = 0; j < M1; j++) {
+    for (int j = p0; j < kend; j++) {
         __syncthreads();
-        const double rj = rinv[j], r2 = rj * rj;
-        for (int i = r0; i < M1; i += 64) {
-            if (i <= j)
-                continue;
-            const double aij = L[(size_t) i * M1 + j];
-            if (q == 0)
-                L[(size_t) j * M1 + i] = aij * rj;
-            const double ti = aij * r2;
-            for (int k = j + 1 + ((q - j - 1) & 3); k <= i; k += 4)
-                L[(size_t) i * M1 + k] = fma(-ti, L[(size_t) k * M1 + j], L[(size_t) i * M1 + k]);
-            if (i == j + 1 && q == ((j + 1) & 3))
-                chol_pivot(L, adiag, M1, j + 1, rinv, &bad, &ndrop);
+        if (tid == 0) {
+            const size_t jj = (size_t) j * M1 + j;
+            const double d = L[jj], ajj = A[jj];
+            double r = 0.0;
+            if (!isfinite(d)) {
+                bad = 1;
+                L[jj] = 0.0;
+            } else if (!(d > CHOL_DROP * ajj)) {
+                ndrop++;
+                L[jj] = 0.0;  // marks a dropped unknown
+            } else {
+                r = rsqrt_nr(d);
+                L[jj] = d * r;
+            }
+            rinv[j] = r;
+            r_sh = r;
+        }
+        __syncthreads();
+        const double r = r_sh;
+        for (int i = j + 1 + tid; i < M1; i += CHB_THREADS)
+            L[(size_t) i * M1 + j] *= r;
+        __syncthreads();
+        if (tid < kend - j - 1)
+            colj[tid] = L[(size_t) (j + 1 + tid) * M1 + j];
+        __syncthreads();
+        // the panel's later columns k (j < k < kend), rows i >= k
+        for (int i = j + 1 + tid; i < M1; i += CHB_THREADS) {
+            double *Li = L + (size_t) i * M1;
+            const double lij = Li[j];
+            const int kmax = min(i, kend - 1);
+            for (int k = j + 1; k <= kmax; k++)
+                Li[k] = fma(-lij, colj[k - j - 1], Li[k]);
         }
     }
     __syncthreads();
-    for (size_t e = tid; e < n2; e += CHOL_THREADS) {
-        const int i = (int) (e / M1), k = (int) (e % M1);
-        if (k < i)
-            work[e] = L[(size_t) k * M1 + i];
-        else if (k == i)
-            work[e] = L[e];
-    }
-    for (int j = tid; j < M1; j += CHOL_THREADS)
-        work[n2 + j] = rinv[j];
     if (tid == 0) {
-        flag[0] = bad ? DGTM_ENONFINITE : 0;
-        flag[1] = ndrop;
+        if (bad)
+            flag[0] = DGTM_ENONFINITE;
+        flag[1] += ndrop;
+    }
+}
+
+// L[i][k] -= sum_q L[i][p0 + q] L[k][p0 + q] over the panel's w columns, for
+// i >= k >= p0 + w: tile (ti, tk), tk <= ti, from the block index
+__global__ void __launch_bounds__(256) chol_update_kernel(int M1, int p0, int w,
+                                                          double *__restrict__ work)
+{
+    __shared__ double Li[32][CHB + 1], Lk[32][CHB + 1];
+    const int t0 = p0 + w;
+    int x = blockIdx.x, ti = 0;
+    while (x > ti) {
+        x -= ti + 1;
+        ti++;
+    }
+    const int tk = x;
+    const int i0 = t0 + 32 * ti, k0 = t0 + 32 * tk;
+    double *L = work;
+    for (int e = threadIdx.x; e < 32 * w; e += 256) {
+        const int r = e / w, q = e - (e / w) * w;
+        Li[r][q] = (i0 + r < M1) ? L[(size_t) (i0 + r) * M1 + p0 + q] : 0.0;
+        Lk[r][q] = (k0 + r < M1) ? L[(size_t) (k0 + r) * M1 + p0 + q] : 0.0;
+    }
+    __syncthreads();
+    const int r = threadIdx.x >> 3, c0 = threadIdx.x & 7;
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int q = 0; q < w; q++) {
+        const double a = Li[r][q];
+#pragma unroll
+        for (int m = 0; m < 4; m++)
+            acc[m] = fma(a, Lk[c0 + 8 * m][q], acc[m]);
+    }
+    const int i = i0 + r;
+#pragma unroll
+    for (int m = 0; m < 4; m++) {
+        const int k = k0 + c0 + 8 * m;
+        if (i < M1 && k <= i)
+            L[(size_t) i * M1 + k] -= acc[m];
     }
 }
 
@@ -596,6 +641,16 @@ __global__ void __launch_bounds__(SOLVE_THREADS) jacobi_solve_kernel(const doubl
         flag[0] = 0;
 }
 
+int solve_launches(int M1, int solver)
+{
+    if (solver == DGTM_SOLVE_SVD)
+        return 1;
+    if (M1 <= SMEM_SOLVE_MAX)
+        return 2;
+    const int np = ceil_div(M1, CHB);
+    return 2 * np - 1 + 1;  // panels, trailing updates (none after the last), triangular solve
+}
+
 int launch_solve(const double *A, const double *B, int M1, int D, int solver, double *W,
                  double *work, int *flag, cudaStream_t s)
 {
@@ -619,11 +674,15 @@ int launch_solve(const double *A, const double *B, int M1, int D, int solver, do
                                                (int) smem));
             cholesky_small_kernel<<<1, CHOL_THREADS, smem, s>>>(A, M1, work, flag);
         } else {
-            const size_t smem = sizeof(double) * 2 * (size_t) M1;
-            DGTM_CUDA_TRY(cudaFuncSetAttribute(cholesky_kernel,
-                                               cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               (int) smem));
-            cholesky_kernel<<<1, CHOL_THREADS, smem, s>>>(A, M1, work, flag);
+            DGTM_CUDA_TRY(cudaMemcpyAsync(work, A, sizeof(double) * (size_t) M1 * M1,
+                                          cudaMemcpyDeviceToDevice, s));
+            for (int p0 = 0; p0 < M1; p0 += CHB) {
+                const int w = M1 - p0 < CHB ? M1 - p0 : CHB;
+                chol_panel_kernel<<<1, CHB_THREADS, 0, s>>>(A, M1, p0, w, work, flag);
+                const int nt = ceil_div(M1 - p0 - w, 32);
+                if (nt > 0)
+                    chol_update_kernel<<<nt * (nt + 1) / 2, 256, 0, s>>>(M1, p0, w, work);
+            }
         }
         DGTM_CUDA_TRY(cudaGetLastError());
         const size_t lbytes = sizeof(double) * ((size_t) M1 * M1 + M1);
