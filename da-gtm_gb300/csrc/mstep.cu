@@ -58,7 +58,8 @@ int launch_reduce_slices(const double *Gpart, const double *RTpart, int nsplit, 
     return DGTM_OK;
 }
 
-// C = FI^T [RT | diag(G) FI] (M1 x (D + M1)): B = C[:, :D], A = C[:, D:].
+// C = FI^T [RT | diag(G) FI] (M1 x (D + M1)): B = C[:, :D], A = C[:, D:]
+// (the upper triangle of A and its diagonal tiles only).
 // The K rows are cut into slices; each thread keeps a 4 x 4 FP64 tile of C
 // over its slice, fed from shared-memory copies of KC rows of FI and of the
 // right operand; the slices' partial tiles are then summed in slice order.
@@ -76,8 +77,11 @@ __global__ void __launch_bounds__(AB_THREADS) form_ab_partial_kernel(
     const int W = D + M1;
     const int nct = Wp / 4;
     const int tile = blockIdx.y * AB_THREADS + threadIdx.x;
-    const bool active = tile < (M1p / 4) * nct;
-    const int m0 = active ? (tile / nct) * 4 : 0, c0 = active ? (tile % nct) * 4 : 0;
+    const bool in_range = tile < (M1p / 4) * nct;
+    const int m0 = in_range ? (tile / nct) * 4 : 0, c0 = in_range ? (tile % nct) * 4 : 0;
+    // a tile of A strictly below the diagonal is not formed: the reduction
+    // takes A from its upper triangle and mirrors it
+    const bool active = in_range && !(c0 >= D && c0 + 3 - D < m0);
     const int kb = blockIdx.x * slice_len, ke = min(K, kb + slice_len);
     double acc[4][4];
 #pragma unroll
