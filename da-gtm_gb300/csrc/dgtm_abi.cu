@@ -548,8 +548,13 @@ int dgtm_mstep(dgtm_ctx *ctx, double *W, int ldW, double *Y, int ldY, double *be
     // ones: the centres of the last E-step stay on the device (dgtm_map_rd)
     std::swap(ctx->Y64, ctx->Yprev);
     std::swap(ctx->yy, ctx->yyprev);
+    // work (the solver's factor, no longer needed once W is out) holds W as
+    // FP32 pairs when update_y cannot keep W in shared memory
+    int nuy = 1;
     DGTM_TRY(launch_update_y(ctx->FI, ctx->FIp, ctx->W, ctx->G, ctx->RT, K, M1, D, ctx->Y64,
-                             ctx->yy, ctx->bterm, cp, ctx->flag + 2, ctx->stream));
+                             ctx->yy, ctx->bterm, cp, ctx->flag + 2, ctx->work,
+                             2 * (size_t) M1 * M1 + (size_t) M1 * D, &nuy, ctx->stream));
+    nsmall += nuy - 1;
     DGTM_TRY(launch_sum_ratio(ctx->bterm, K, ctx->sum_tt, (double) ((long long) N * D),
                               ctx->scal, ctx->stream));
     DGTM_TRY(phase_end(ctx, DGTM_PHASE_MSTEP_SOLVE, nsmall));

@@ -87,10 +87,14 @@ struct YCopies {
 // Y = FI W, yy = |y|^2, bterm_k = G_k yy_k - 2 y_k.RT_k (G/RT may be null: no
 // bterm), and the copies in cp.  FIp: FI as (hi, lo) FP32 pairs for the
 // compensated FP32 product (FP32 and split forms), or null for FP64 FMAs.
-// ticket: one device int of scratch.
+// ticket: one device int of scratch.  scratch (scratch_doubles doubles, may be
+// null): room for W as FP32 pairs when W is too large for shared memory, so
+// that the compensated product does not convert it per centre; *nlaunch
+// receives the kernels launched.
 int launch_update_y(const double *FI, const float2 *FIp, const double *W, const double *G,
                     const double *RT, int K, int M1, int D, double *Y, double *yy,
-                    double *bterm, const YCopies &cp, int *ticket, cudaStream_t s);
+                    double *bterm, const YCopies &cp, int *ticket, double *scratch,
+                    size_t scratch_doubles, int *nlaunch, cudaStream_t s);
 // dst[i] = src[i] as an unevaluated sum of two FP32 (hi, lo).
 int launch_to_pairs(const double *src, size_t n, float2 *dst, cudaStream_t s);
 // AUTO cooling (ctemp.cu).  A plan fixes the batch of centres (kb), the chunk

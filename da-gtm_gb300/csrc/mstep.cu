@@ -779,8 +779,9 @@ __global__ void __launch_bounds__(UY_THREADS) update_y_kernel(
     const double *__restrict__ FI, const float2 *__restrict__ FIp, const double *__restrict__ Wg,
     const double *__restrict__ G, const double *__restrict__ RT, int K, int M1, int D, int Dw,
     double *__restrict__ Y, double *__restrict__ yy, double *__restrict__ bterm, YCopies cp,
-    int *ticket)
+    int *ticket, const float2 *__restrict__ Wq)
 {
+    // Wq (DF without WS, may be null): W as FP32 pairs in global memory, M1 x Dw
     // M1 x Dw, zero past D: FP64 values, or (hi, lo) pairs of the same size
     extern __shared__ double Ws[];
     float2 *const Wp = reinterpret_cast<float2 *>(Ws);
@@ -824,8 +825,9 @@ __global__ void __launch_bounds__(UY_THREADS) update_y_kernel(
                     for (int c = 0; c < NC; c++) {
                         const int d = db + lane + 32 * c;
                         const float2 w = WS ? Wp[m * Dw + d]
-                                            : ((d < D) ? f64_to_pair(Wg[(size_t) m * D + d])
-                                                       : make_float2(0.f, 0.f));
+                                         : Wq ? Wq[(size_t) m * Dw + d]
+                                              : ((d < D) ? f64_to_pair(Wg[(size_t) m * D + d])
+                                                         : make_float2(0.f, 0.f));
                         dot2_step(p0[c], s0[c], x0, w);
                         dot2_step(p1[c], s1[c], x1, w);
                     }
@@ -912,7 +914,19 @@ __global__ void __launch_bounds__(UY_THREADS) update_y_kernel(
 
 using UpdateYKernel = void (*)(const double *, const float2 *, const double *, const double *,
                                const double *, int, int, int, int, double *, double *, double *,
-                               YCopies, int *);
+                               YCopies, int *, const float2 *);
+
+// W (M1 x D) as FP32 pairs, M1 x Dw with zero columns past D
+__global__ void w_pairs_kernel(const double *__restrict__ W, int M1, int D, int Dw,
+                               float2 *__restrict__ Wq)
+{
+    const size_t n = (size_t) M1 * Dw;
+    for (size_t i = blockIdx.x * (size_t) blockDim.x + threadIdx.x; i < n;
+         i += (size_t) gridDim.x * blockDim.x) {
+        const int m = (int) (i / Dw), d = (int) (i % Dw);
+        Wq[i] = d < D ? f64_to_pair(W[(size_t) m * D + d]) : make_float2(0.f, 0.f);
+    }
+}
 
 template <bool WS, bool DF>
 UpdateYKernel update_y_for(int nc)
@@ -931,7 +945,8 @@ UpdateYKernel update_y_for(int nc)
 
 int launch_update_y(const double *FI, const float2 *FIp, const double *W, const double *G,
                     const double *RT, int K, int M1, int D, double *Y, double *yy, double *bterm,
-                    const YCopies &cp, int *ticket, cudaStream_t s)
+                    const YCopies &cp, int *ticket, double *scratch, size_t scratch_doubles,
+                    int *nlaunch, cudaStream_t s)
 {
     DGTM_CUDA_TRY(cudaMemsetAsync(ticket, 0, sizeof(int), s));
     int dev = 0, sms = 0;
@@ -953,9 +968,20 @@ int launch_update_y(const double *FI, const float2 *FIp, const double *W, const 
     if (ws)
         DGTM_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int) wbytes));
+    // W beyond shared memory: converted to pairs once here, not per centre
+    float2 *Wq = nullptr;
+    int nl = 1;
+    if (!ws && df && scratch && (size_t) M1 * Dw <= scratch_doubles) {
+        Wq = reinterpret_cast<float2 *>(scratch);
+        w_pairs_kernel<<<ceil_div(M1 * Dw, 256), 256, 0, s>>>(W, M1, D, Dw, Wq);
+        DGTM_CUDA_TRY(cudaGetLastError());
+        nl++;
+    }
     k<<<blocks, UY_THREADS, ws ? wbytes : 0, s>>>(FI, FIp, W, G, RT, K, M1, D, Dw, Y, yy, bterm, cp,
-                                                 ticket);
+                                                 ticket, Wq);
     DGTM_CUDA_TRY(cudaGetLastError());
+    if (nlaunch)
+        *nlaunch = nl;
     return DGTM_OK;
 }
 
