@@ -566,7 +566,7 @@ int tc_ctemp_pairs(const TcView &v, const double *Y64, const double *gg_dev, dou
     const CtempPlan pl = ctemp_plan(N, D, K, true, true, budget / 4, 1);
     const size_t sbytes = sizeof(double) * 2 * (size_t) D * D;
     const int kb = pl.kb;
-    // the batch's S1, S2 (FP64), then the FP32 matrices of the eigen sweeps
+    // the batch's S1, S2 (FP64), then the FP32 matrices of the eigenvalue step
     // when they do not fit shared memory
     const size_t s_at = (sbytes * kb + 255) / 256 * 256;
     const size_t mg_bytes = pl.eig_in_smem ? 0 : sizeof(float) * 2 * (size_t) D * D * kb;

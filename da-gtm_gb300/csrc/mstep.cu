@@ -4,7 +4,8 @@
 //   form_ab       : A = FI^T diag(G) FI, B = FI^T RT     (dagtm/dagtm.cxx:1715-1761),
 //                   K-sliced 4 x 4 register tiles, slice partials summed in order
 //   solve         : A W = B, FP64 Cholesky (numerically dependent pivots dropped;
-//                   one-block factorisation, one warp per right-hand side)
+//                   one block for M1 <= 110, panels over the GPU above that; one
+//                   warp per right-hand side in the substitution)
 //                   or symmetric-eigen pseudo-inverse
 //                   with exactly-zero eigenvalues dropped (the semantics of
 //                   gsl_linalg_SV_solve used by dagtm_solve2, comm/comm.c:1299-1348)
@@ -190,7 +191,7 @@ int launch_form_ab(const double *FI, const double *G, const double *RT, int K, i
 }
 
 // ---------------------------------------------------------------------------
-// solvers (one block)
+// solvers
 // ---------------------------------------------------------------------------
 constexpr int SOLVE_THREADS = 512;
 constexpr int SMEM_SOLVE_MAX = 110;  // M1 up to which L lives in shared memory
