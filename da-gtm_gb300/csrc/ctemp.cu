@@ -53,13 +53,53 @@ constexpr size_t ALIGN = 256;
 
 size_t align_up(size_t b) { return (b + ALIGN - 1) / ALIGN * ALIGN; }
 
+// The power of two that brings a centre's largest responsibility into
+// [1, 2): FP32 weights keep full precision however small the FP64 ones are
+// (a centre far from every point); S1, S2 scale by it, its eigenvalues are
+// scaled back.  rmax: the largest R of each centre of the batch as bits (a
+// positive double orders as its bit pattern), or null for no scaling.
+__device__ __forceinline__ double r_scale(const unsigned long long *rmax, int kl)
+{
+    if (!rmax)
+        return 1.0;
+    const double m = __longlong_as_double((long long) rmax[kl]);
+    if (!(m > 0.0))
+        return 1.0;
+    const int e = -ilogb(m);
+    return ldexp(1.0, e > 1000 ? 1000 : (e < -1000 ? -1000 : e));
+}
+
+// rmax[kl] = max(rmax[kl], the largest R of centre kl over the chunk)
+__global__ void r_rowmax_kernel(const double *__restrict__ Rb, int nn,
+                                unsigned long long *__restrict__ rmax)
+{
+    __shared__ double wm[8];
+    const int kl = blockIdx.x;
+    double m = 0.0;
+    for (int p = threadIdx.x; p < nn; p += blockDim.x)
+        m = fmax(m, Rb[(size_t) kl * nn + p]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0)
+        wm[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int) (blockDim.x >> 5); w++)
+            m = fmax(m, wm[w]);
+        m = fmax(m, wm[0]);
+        atomicMax(&rmax[kl], (unsigned long long) __double_as_longlong(m));
+    }
+}
+
 // blockIdx.x = centre in the batch, blockIdx.y = tile pair (ti <= tj).
 // Tc: the chunk's points (nn x D, row-major); Rb: kb x nn responsibilities.
 // S (per centre: S1 then S2, D x D) holds the entries i <= j only.
 template <typename F>
 __global__ void __launch_bounds__(SC_THREADS, 2) scatter_kernel(
     const F *__restrict__ Tc, const double *__restrict__ Y, const double *__restrict__ Rb, int nn,
-    int D, int k0, int first, double *__restrict__ S, double *__restrict__ gsum)
+    int D, int k0, int first, double *__restrict__ S, double *__restrict__ gsum,
+    const unsigned long long *__restrict__ rmax)
 {
     __shared__ __align__(16) F xr[SC_PTS][SC_TILE];
     __shared__ __align__(16) F xc[SC_PTS][SC_TILE];
@@ -91,6 +131,7 @@ __global__ void __launch_bounds__(SC_THREADS, 2) scatter_kernel(
         for (int j = 0; j < 4; j++)
             a1[i][j] = a2[i][j] = F(0), d1[i][j] = d2[i][j] = 0.0;
     const double *rk = Rb + (size_t) kl * nn;
+    const double rs = r_scale(rmax, kl);  // the weights only; g stays unscaled
     double g = 0.0;  // lanes of warp 0: every 32nd point, summed at the end
     int sub = 0;
     for (int p0 = 0; p0 < nn; p0 += SC_PTS) {
@@ -99,7 +140,7 @@ __global__ void __launch_bounds__(SC_THREADS, 2) scatter_kernel(
             const int p = p0 + threadIdx.x;
             const double r = p < nn ? rk[p] : 0.0;
             g += r;
-            const F wf = (F) r;
+            const F wf = (F) (r * rs);
             w1[threadIdx.x] = wf;
             w2[threadIdx.x] = wf * wf;
         }
@@ -235,7 +276,8 @@ template <int EIG_THREADS, typename F>
 __global__ void __launch_bounds__(EIG_THREADS) eig_kernel(const double *__restrict__ S, int D,
                                                           int in_smem, F *__restrict__ Mg,
                                                           const double *__restrict__ gg,
-                                                          double lim_scale, double *__restrict__ out)
+                                                          double lim_scale, double *__restrict__ out,
+                                                          const unsigned long long *__restrict__ rmax)
 {
     constexpr int NW = EIG_THREADS / 32;
     extern __shared__ __align__(16) unsigned char sh_raw[];
@@ -258,13 +300,14 @@ __global__ void __launch_bounds__(EIG_THREADS) eig_kernel(const double *__restri
     }
     // gg < GG_MIN: the reference scales H by 1 / GG_MIN before gsl_eigen_symm
     // and the eigenvalues back.  The FP32 arithmetic takes H / gg (1e250 is
-    // outside FP32) and multiplies the eigenvalues by gg.
+    // outside FP32) and multiplies the eigenvalues by gg; H was formed with
+    // weights scaled by r_scale, which the matrix scale takes back out.
     double sc = 1.0, back = 1.0;
     if (sizeof(F) == 8) {
         if (gk < GG_MIN)
             sc = 1.0 / GG_MIN, back = GG_MIN;
     } else {
-        sc = 1.0 / gk, back = gk;
+        sc = 1.0 / (gk * r_scale(rmax, kl)), back = gk;
     }
     for (int e = threadIdx.x; e < D * D; e += EIG_THREADS) {
         const int i = e / D, j = e - i * D;
@@ -391,13 +434,15 @@ __global__ void __launch_bounds__(EIG_THREADS) eig_kernel(const double *__restri
 
 template <int NT, typename F>
 int launch_eig(int kb, int D, bool in_smem, const double *S, F *Mg, const double *gg,
-               double lim_scale, double *out, cudaStream_t s)
+               double lim_scale, double *out, cudaStream_t s,
+               const unsigned long long *rmax = nullptr)
 {
     const size_t smem = in_smem ? eig_smem_bytes<F>(D)
                                 : eig_smem_bytes<F>(D) - sizeof(F) * (size_t) D * D;
     DGTM_CUDA_TRY(cudaFuncSetAttribute(eig_kernel<NT, F>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem));
-    eig_kernel<NT, F><<<dim3(kb, 2), NT, smem, s>>>(S, D, in_smem ? 1 : 0, Mg, gg, lim_scale, out);
+    eig_kernel<NT, F><<<dim3(kb, 2), NT, smem, s>>>(S, D, in_smem ? 1 : 0, Mg, gg, lim_scale, out,
+                                                    rmax);
     DGTM_CUDA_TRY(cudaGetLastError());
     return DGTM_OK;
 }
@@ -406,7 +451,7 @@ template <typename F>
 int run_batch(const CtempPlan &pl, const double *T64, const float *T32, const double *Y,
               const double *tt, const double *yy, const double2 *colstat, int N, int D, int K,
               double c, int k0, int kb, const double *gg_dev, double lim_scale, void *scratch,
-              double *gsum_dev, double *out_dev, double dcut, cudaStream_t s)
+              double *gsum_dev, double *out_dev, double dcut, bool scale_r, cudaStream_t s)
 {
     unsigned char *base = (unsigned char *) scratch;
     double *S = (double *) base;
@@ -418,8 +463,27 @@ int run_batch(const CtempPlan &pl, const double *T64, const float *T32, const do
     }
     double *Rb = (double *) base;
     base += align_up(sizeof(double) * (size_t) pl.kb * pl.nn);
+    unsigned long long *rmax = (unsigned long long *) base;
+    base += align_up(sizeof(unsigned long long) * (size_t) pl.kb);
     float *Tbuf = (float *) base;  // FP32 copy of a chunk when the context has none
     const int ntp = ((D + SC_TILE - 1) / SC_TILE) * ((D + SC_TILE - 1) / SC_TILE + 1) / 2;
+    // FP32 weights of centres whose responsibilities may lie below FP32's
+    // range: a first pass over the points for each centre's largest R
+    const bool scaled = scale_r && !std::is_same<F, double>::value;
+    if (scaled) {
+        DGTM_CUDA_TRY(cudaMemsetAsync(rmax, 0, sizeof(unsigned long long) * (size_t) kb, s));
+        for (int n0 = 0; n0 < N; n0 += pl.nn) {
+            const int nn = (N - n0 < pl.nn) ? N - n0 : pl.nn;
+            const int r = launch_r_block(T64, Y, tt, yy, colstat, D, K, c, k0, kb, n0, nn, Rb, s,
+                                         nullptr, nullptr, dcut);
+            if (r != DGTM_OK)
+                return r;
+            r_rowmax_kernel<<<kb, 256, 0, s>>>(Rb, nn, rmax);
+            DGTM_CUDA_TRY(cudaGetLastError());
+        }
+    } else {
+        rmax = nullptr;
+    }
     for (int n0 = 0; n0 < N; n0 += pl.nn) {
         const int nn = (N - n0 < pl.nn) ? N - n0 : pl.nn;
         int r = launch_r_block(T64, Y, tt, yy, colstat, D, K, c, k0, kb, n0, nn, Rb, s, nullptr,
@@ -438,13 +502,13 @@ int run_batch(const CtempPlan &pl, const double *T64, const float *T32, const do
             Tc = Tbuf;
         }
         scatter_kernel<F><<<dim3(kb, ntp), SC_THREADS, 0, s>>>(Tc, Y, Rb, nn, D, k0, n0 == 0 ? 1 : 0,
-                                                                S, gsum_dev);
+                                                                S, gsum_dev, rmax);
         DGTM_CUDA_TRY(cudaGetLastError());
     }
     const double *gg = gg_dev ? gg_dev : gsum_dev;
     if (D <= EIG_SMALL_D)
-        return launch_eig<256, F>(kb, D, pl.eig_in_smem, S, Mg, gg, lim_scale, out_dev, s);
-    return launch_eig<512, F>(kb, D, pl.eig_in_smem, S, Mg, gg, lim_scale, out_dev, s);
+        return launch_eig<256, F>(kb, D, pl.eig_in_smem, S, Mg, gg, lim_scale, out_dev, s, rmax);
+    return launch_eig<512, F>(kb, D, pl.eig_in_smem, S, Mg, gg, lim_scale, out_dev, s, rmax);
 }
 
 }  // namespace
@@ -468,7 +532,8 @@ CtempPlan ctemp_plan(int N, int D, int K, bool f32, bool have_t32, size_t budget
     pl.kb = (int) kb;
     pl.scratch_bytes = align_up(sizeof(double) * (size_t) pl.kb * 2 * dd) +
                        (pl.eig_in_smem ? 0 : align_up(fsz * (size_t) pl.kb * 2 * dd)) +
-                       align_up(sizeof(double) * (size_t) pl.kb * pl.nn) + align_up(fixed) + ALIGN;
+                       align_up(sizeof(double) * (size_t) pl.kb * pl.nn) +
+                       align_up(sizeof(unsigned long long) * (size_t) pl.kb) + align_up(fixed) + ALIGN;
     return pl;
 }
 
@@ -526,13 +591,13 @@ int launch_ctemp_batch(const CtempPlan &pl, const double *T64, const float *T32,
                        const double *tt, const double *yy, const double2 *colstat, int N, int D,
                        int K, double c, int k0, int kb, const double *gg_dev, double lim_scale,
                        void *scratch, double *gsum_dev, double *out_dev, double dcut,
-                       cudaStream_t s)
+                       bool scale_r, cudaStream_t s)
 {
     if (pl.f32)
         return run_batch<float>(pl, T64, T32, Y, tt, yy, colstat, N, D, K, c, k0, kb, gg_dev,
-                                lim_scale, scratch, gsum_dev, out_dev, dcut, s);
+                                lim_scale, scratch, gsum_dev, out_dev, dcut, scale_r, s);
     return run_batch<double>(pl, T64, T32, Y, tt, yy, colstat, N, D, K, c, k0, kb, gg_dev,
-                             lim_scale, scratch, gsum_dev, out_dev, dcut, s);
+                             lim_scale, scratch, gsum_dev, out_dev, dcut, false, s);
 }
 
 }  // namespace dgtm

@@ -900,9 +900,10 @@ int dgtm_next_ctemp_k(dgtm_ctx *ctx, double temp, double beta, double eps, const
                                        ggs, ctx->stream);
         for (int k0 = 0; rc == DGTM_OK && e == cudaSuccess && k0 < ns; k0 += kb) {
             const int nb = (ns - k0 < kb) ? ns - k0 : kb;
+            // these centres' responsibilities can lie below FP32's range: scaled
             rc = launch_ctemp_batch(pl, ctx->T64, ctx->T32, Ys, ctx->tt, yys, ctx->colstat, N, D, K,
                                     c, k0, nb, ggs ? ggs + k0 : nullptr, lim_scale, scratch, gs + k0,
-                                    os + (size_t) 2 * k0, dcut, ctx->stream);
+                                    os + (size_t) 2 * k0, dcut, true, ctx->stream);
         }
         out_sel.resize((size_t) 2 * ns);
         gsum_sel.resize((size_t) ns);
@@ -925,7 +926,7 @@ int dgtm_next_ctemp_k(dgtm_ctx *ctx, double temp, double beta, double eps, const
         const int nb = (K - k0 < kb) ? K - k0 : kb;
         rc = launch_ctemp_batch(pl, ctx->T64, ctx->T32, ctx->Y64, ctx->tt, ctx->yy, ctx->colstat,
                                 N, D, K, c, k0, nb, gg ? dgg + k0 : nullptr, lim_scale, scratch,
-                                dgsum + k0, dout + (size_t) 2 * k0, dcut, ctx->stream);
+                                dgsum + k0, dout + (size_t) 2 * k0, dcut, false, ctx->stream);
     }
     if (rc == DGTM_OK && e == cudaSuccess)
         e = cudaMemcpyAsync(out.data(), dout, sizeof(double) * 2 * K, cudaMemcpyDeviceToHost,

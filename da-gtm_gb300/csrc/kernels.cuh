@@ -115,7 +115,7 @@ int launch_ctemp_batch(const CtempPlan &pl, const double *T64, const float *T32,
                        const double *tt, const double *yy, const double2 *colstat, int N, int D,
                        int K, double c, int k0, int kb, const double *gg_dev, double lim_scale,
                        void *scratch, double *gsum_dev, double *out_dev, double dcut,
-                       cudaStream_t s);
+                       bool scale_r, cudaStream_t s);
 // Rows idx[0..n) of Y (K x D), and of yy and gg (gg may be null), packed.
 int launch_gather_centres(const double *Y, const double *yy, const double *gg, const int *idx,
                           int n, int D, double *Ys, double *yys, double *ggs, cudaStream_t s);

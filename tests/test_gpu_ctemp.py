@@ -129,8 +129,10 @@ def test_pair_feature_gemm_chunks_and_segments(pkg, monkeypatch, pairs_case, gem
 def test_pair_feature_gemm_far_centres(pkg, orc, monkeypatch, far, finite):
     """A centre far from every point.  At 6 (beta d / 2 ~ 470) its
     responsibilities (~1e-52) are below the split form's FP32 planes, so the
-    pair-feature GEMM sees a zero row: it is redone from FP64 responsibilities
-    and matches the oracle.  At 8 (beta d / 2 ~ 865) the reference's
+    pair-feature GEMM sees a zero row: it is redone from FP64 responsibilities,
+    scaled by a power of two into FP32's range, and its own critical
+    temperature matches the FP64 one (the CUDA-core path, which does not scale,
+    is compared on the other centres only).  At 8 (beta d / 2 ~ 865) the reference's
     exp(-beta d / 2) underflows, its responsibilities are exactly 0 and
     comm/mpicomm.c:574-577 makes the critical temperature HUGE_VAL: so here."""
     T, FI, Y = problem(pkg, "binary", 3000, 166, 16, seed=13)
@@ -143,16 +145,26 @@ def test_pair_feature_gemm_far_centres(pkg, orc, monkeypatch, far, finite):
         got, got_k = c.next_ctemp(temp, beta, eps, per_centre=True)
         monkeypatch.setenv("DGTM_CTEMP_PAIRS", "0")
         simt, simt_k = c.next_ctemp(temp, beta, eps, per_centre=True)
-    assert got_k[9] == simt_k[9]  # both from the same FP64-R scatter
+    keep = np.arange(16) != 9
     if finite:
         assert 0.0 < R[9].sum() < 1e-40
         assert np.all(np.isfinite(got_k)) and np.isfinite(got)
-        np.testing.assert_allclose(got_k, simt_k, rtol=1e-4)
+        np.testing.assert_allclose(got_k[keep], simt_k[keep], rtol=1e-4)
         assert got == pytest.approx(ref, rel=1e-4)
+        # the far centre's own critical temperature, from its FP64 responsibilities
+        # (far below FP32's normal range): the spectrum of H is that of 2 S1 and
+        # of 2 (S1 - S2); eigenvalues at or above (temp - eps) gg 2 / beta count
+        # as 0; ctemp = beta / (2 gg) times the largest
+        X = T - Y[9]
+        S1 = (X * R[9][:, None]).T @ X
+        S2 = (X * (R[9] ** 2)[:, None]).T @ X
+        gk = R[9].sum()
+        lam = np.concatenate([np.linalg.eigvalsh(2 * S1), np.linalg.eigvalsh(2 * (S1 - S2))])
+        lam[lam >= (temp - eps) * gk * 2 / beta] = 0.0
+        assert got_k[9] == pytest.approx(beta / (2 * gk) * lam.max(), rel=1e-4)
     else:
         assert R[9].sum() == 0.0 and ref == np.inf
-        assert got == simt == np.inf and got_k[9] == np.inf
-        keep = np.arange(16) != 9
+        assert got == simt == np.inf and got_k[9] == simt_k[9] == np.inf
         np.testing.assert_allclose(got_k[keep], simt_k[keep], rtol=1e-4)
 
 
