@@ -652,8 +652,9 @@ int solve_launches(int M1, int solver)
         return 1;
     if (M1 <= SMEM_SOLVE_MAX)
         return 2;
+    // np panels, np - 1 trailing updates (none after the last), the substitution
     const int np = ceil_div(M1, CHB);
-    return 2 * np - 1 + 1;  // panels, trailing updates (none after the last), triangular solve
+    return np + (np - 1) + 1;
 }
 
 int launch_solve(const double *A, const double *B, int M1, int D, int solver, double *W,
